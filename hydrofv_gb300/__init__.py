@@ -1,0 +1,417 @@
+"""hydrofv_gb300 -- GB300-native finite-volume step behind hydroFV's C API.
+
+The product is the C-ABI shared library ``libhydro_gb300.so`` (built in-tree
+by :mod:`hydrofv_gb300.build`).  This module is a thin ctypes front-end for
+Python callers, tests and the benchmark: it mirrors the C structs of
+``include/*.h`` and drives the library through its public entry points
+(``system_init``, ``launch_simulation``, ``hydro_gpu_launch_simulation``,
+``hydro_gpu_solver_*``).  Nothing here computes hydrodynamics; if the library
+is missing the import of :func:`library` fails loudly.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass, field
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libhydro_gb300.so")
+
+_dp = C.POINTER(C.c_double)
+
+
+class ErrorStatus(C.Structure):
+    _fields_ = [("return_code", C.c_int), ("traceback", C.c_void_p), ("traceback_code_", C.c_int)]
+
+
+class System(C.Structure):
+    _fields_ = [
+        ("coord_sys", C.c_char_p),
+        ("gamma", C.c_double), ("gravity", C.c_double),
+        ("x_min", C.c_double), ("x_max", C.c_double),
+        ("y_min", C.c_double), ("y_max", C.c_double),
+        ("z_min", C.c_double), ("z_max", C.c_double),
+        ("num_cells_x", C.c_int), ("num_cells_y", C.c_int), ("num_cells_z", C.c_int),
+        ("num_ghost_cells_side", C.c_int),
+        ("coord_sys_flag_", C.c_int),
+        ("dx_", C.c_double), ("dy_", C.c_double), ("dz_", C.c_double),
+        ("density_", _dp), ("velocity_x_", _dp), ("velocity_y_", _dp), ("velocity_z_", _dp),
+        ("pressure_", _dp), ("mass_", _dp), ("momentum_x_", _dp), ("momentum_y_", _dp),
+        ("momentum_z_", _dp), ("energy_", _dp),
+        ("mid_points_x_", _dp), ("mid_points_y_", _dp), ("mid_points_z_", _dp),
+        ("surface_area_x_", _dp), ("surface_area_y_", _dp), ("surface_area_z_", _dp),
+        ("volume_", _dp),
+    ]
+
+
+class BoundaryConditionParam(C.Structure):
+    _fields_ = [
+        ("boundary_condition_x_min", C.c_char_p), ("boundary_condition_x_max", C.c_char_p),
+        ("boundary_condition_y_min", C.c_char_p), ("boundary_condition_y_max", C.c_char_p),
+        ("boundary_condition_z_min", C.c_char_p), ("boundary_condition_z_max", C.c_char_p),
+        ("set_boundary_condition_1d_x_min", C.c_void_p), ("set_boundary_condition_1d_x_max", C.c_void_p),
+        ("set_boundary_condition_cartesian_2d_x_min", C.c_void_p),
+        ("set_boundary_condition_cartesian_2d_x_max", C.c_void_p),
+        ("set_boundary_condition_cartesian_2d_y_min", C.c_void_p),
+        ("set_boundary_condition_cartesian_2d_y_max", C.c_void_p),
+        ("boundary_condition_flag_x_min_", C.c_int), ("boundary_condition_flag_x_max_", C.c_int),
+        ("boundary_condition_flag_y_min_", C.c_int), ("boundary_condition_flag_y_max_", C.c_int),
+        ("boundary_condition_flag_z_min_", C.c_int), ("boundary_condition_flag_z_max_", C.c_int),
+    ]
+
+
+class IntegratorParam(C.Structure):
+    _fields_ = [
+        ("integrator", C.c_char_p), ("riemann_solver", C.c_char_p), ("slope_limiter", C.c_char_p),
+        ("cfl", C.c_double), ("cfl_initial_shrink_factor", C.c_double),
+        ("cfl_initial_shrink_num_steps", C.c_int), ("tol", C.c_double),
+        ("integrator_flag_", C.c_int), ("riemann_solver_flag_", C.c_int),
+        ("slope_limiter_flag_", C.c_int),
+    ]
+
+
+class StoringParam(C.Structure):
+    _fields_ = [
+        ("output_dir", C.c_char_p), ("is_storing", C.c_bool), ("store_initial", C.c_bool),
+        ("storing_interval", C.c_double), ("storing_method_flag_", C.c_int),
+        ("store_count_", C.c_int),
+    ]
+
+
+class Settings(C.Structure):
+    _fields_ = [("verbose", C.c_int), ("no_progress_bar", C.c_bool)]
+
+
+class SimulationParam(C.Structure):
+    _fields_ = [("tf", C.c_double)]
+
+
+class SimulationStatus(C.Structure):
+    _fields_ = [("num_steps", C.c_int64), ("t", C.c_double), ("dt", C.c_double)]
+
+
+class HydroGpuOptions(C.Structure):
+    _fields_ = [
+        ("device", C.c_int), ("max_steps", C.c_int64), ("precision", C.c_int),
+        ("chunk_steps", C.c_int), ("use_graph", C.c_int), ("block_threads", C.c_int),
+        ("chunk_rows", C.c_int),
+    ]
+
+
+class HydroGpuStats(C.Structure):
+    _fields_ = [
+        ("total_ms", C.c_double), ("h2d_ms", C.c_double), ("step_ms", C.c_double),
+        ("d2h_ms", C.c_double), ("steps", C.c_int64), ("step_launches", C.c_int64),
+        ("kernel_launches", C.c_int64), ("h2d_bytes", C.c_int64), ("d2h_bytes", C.c_int64),
+        ("interior_cells", C.c_int64),
+    ]
+
+
+PRECISION_FP64 = 0
+PRECISION_FP32 = 1
+
+_P = C.POINTER
+_SIGNATURES = {
+    "get_new_system_struct": (System, []),
+    "system_init": (ErrorStatus, [_P(System)]),
+    "free_system_memory": (None, [_P(System)]),
+    "get_new_boundary_condition_param": (BoundaryConditionParam, []),
+    "finalize_boundary_condition_param": (ErrorStatus, [_P(System), _P(BoundaryConditionParam)]),
+    "set_boundary_condition": (ErrorStatus, [_P(BoundaryConditionParam), _P(System)]),
+    "convert_primitive_to_conserved": (ErrorStatus, [_P(System)]),
+    "convert_conserved_to_primitive": (ErrorStatus, [_P(System)]),
+    "get_new_integrator_param": (IntegratorParam, []),
+    "finalize_integrator_param": (ErrorStatus, [_P(IntegratorParam)]),
+    "get_new_storing_param": (StoringParam, []),
+    "finalize_storing_param": (ErrorStatus, [_P(StoringParam)]),
+    "launch_simulation": (ErrorStatus, [_P(BoundaryConditionParam), _P(System), _P(IntegratorParam),
+                                        _P(StoringParam), _P(Settings), _P(SimulationParam),
+                                        _P(SimulationStatus)]),
+    "hydro_gpu_default_options": (HydroGpuOptions, []),
+    "hydro_gpu_set_process_options": (None, [_P(HydroGpuOptions)]),
+    "hydro_gpu_launch_simulation": (ErrorStatus, [_P(BoundaryConditionParam), _P(System),
+                                                  _P(IntegratorParam), _P(StoringParam),
+                                                  _P(Settings), _P(SimulationParam),
+                                                  _P(SimulationStatus), _P(HydroGpuOptions),
+                                                  _P(HydroGpuStats)]),
+    "hydro_gpu_solver_create": (ErrorStatus, [_P(C.c_void_p), _P(BoundaryConditionParam), _P(System),
+                                              _P(IntegratorParam), _P(HydroGpuOptions)]),
+    "hydro_gpu_solver_restart": (ErrorStatus, [C.c_void_p]),
+    "hydro_gpu_solver_advance": (ErrorStatus, [C.c_void_p, C.c_int64, C.c_double,
+                                               _P(SimulationStatus), _P(C.c_double)]),
+    "hydro_gpu_solver_download": (ErrorStatus, [C.c_void_p, _P(System)]),
+    "hydro_gpu_solver_kernel_launches": (C.c_int64, [C.c_void_p]),
+    "hydro_gpu_solver_destroy": (None, [C.c_void_p]),
+    "hydro_gpu_device_count": (C.c_int, []),
+    "hydro_gpu_version": (C.c_char_p, []),
+    "free_traceback": (None, [_P(ErrorStatus)]),
+    "solve_flux_hllc_2d": (ErrorStatus, [_dp] * 4 + [C.c_double] * 10),
+    "solve_flux_exact_1d": (ErrorStatus, [_dp] * 3 + [C.c_double] * 9 + [C.c_int]),
+    "guess_p": (C.c_double, [C.c_double] * 10),
+    "limit_slope": (ErrorStatus, [_dp, _P(IntegratorParam), C.c_double, C.c_double]),
+    "get_time_step_2d": (C.c_double, [_P(System), C.c_double]),
+}
+
+_lib: C.CDLL | None = None
+
+
+def library(path: str | None = None) -> C.CDLL:
+    """Load libhydro_gb300.so (raises FileNotFoundError if it was not built)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise FileNotFoundError(
+            f"{p} not found; build it with `python -m hydrofv_gb300.build` (needs nvcc)")
+    lib = C.CDLL(p)
+    for name, (res, args) in _SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+class HydroError(RuntimeError):
+    def __init__(self, code: int, message: str):
+        super().__init__(f"[{code}] {message}")
+        self.code = code
+        self.message = message
+
+
+def _consume(lib: C.CDLL, e: ErrorStatus) -> tuple[int, str]:
+    """Return (code, traceback text) and release the traceback."""
+    msg = ""
+    if e.traceback:
+        msg = C.string_at(e.traceback).decode(errors="replace")
+    lib.free_traceback(C.byref(e))
+    return e.return_code, msg
+
+
+def device_count() -> int:
+    return int(library().hydro_gpu_device_count())
+
+
+def default_options(**kw) -> HydroGpuOptions:
+    o = library().hydro_gpu_default_options()
+    for k, v in kw.items():
+        setattr(o, k, v)
+    return o
+
+
+@dataclass
+class RunResult:
+    code: int
+    message: str
+    W: np.ndarray
+    U: np.ndarray
+    num_steps: int
+    t: float
+    dt: float
+    stats: dict = field(default_factory=dict)
+
+
+def _stats_dict(st: HydroGpuStats) -> dict:
+    return {name: getattr(st, name) for name, _ in HydroGpuStats._fields_}
+
+
+class _SystemHandle:
+    """A System allocated by system_init with W/U copied in from numpy."""
+
+    def __init__(self, lib, coord_sys: str, nx: int, ny: int, g: int, bounds, gamma: float):
+        self.lib = lib
+        self._coord = coord_sys.encode()
+        s = lib.get_new_system_struct()
+        s.coord_sys = self._coord
+        s.gamma = gamma
+        s.x_min, s.x_max = bounds[0], bounds[1]
+        if ny > 0:
+            s.y_min, s.y_max = bounds[2], bounds[3]
+            s.num_cells_y = ny
+        s.num_cells_x = nx
+        s.num_ghost_cells_side = g
+        code, msg = _consume(lib, lib.system_init(C.byref(s)))
+        if code != 0:
+            raise HydroError(code, msg)
+        self.s = s
+        self.n = (nx + 2 * g) * ((ny + 2 * g) if ny > 0 else 1)
+        self.shape = ((ny + 2 * g), (nx + 2 * g)) if ny > 0 else ((nx + 2 * g),)
+
+    def fields(self, names):
+        return [np.ctypeslib.as_array(getattr(self.s, n), shape=(self.n,)) for n in names]
+
+    def close(self):
+        if self.s is not None:
+            self.lib.free_system_memory(C.byref(self.s))
+            self.s = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+W2 = ("density_", "velocity_x_", "velocity_y_", "pressure_")
+U2 = ("mass_", "momentum_x_", "momentum_y_", "energy_")
+W1 = ("density_", "velocity_x_", "pressure_")
+U1 = ("mass_", "momentum_x_", "energy_")
+
+
+def _params(lib, bc, integrator, riemann_solver, slope_limiter, cfl, keep):
+    bcp = lib.get_new_boundary_condition_param()
+    names = ["x_min", "x_max", "y_min", "y_max"]
+    for k, b in enumerate(bc):
+        enc = b.encode() if b is not None else None
+        keep.append(enc)
+        setattr(bcp, "boundary_condition_" + names[k], enc)
+    ip = lib.get_new_integrator_param()
+    for attr, val in (("integrator", integrator), ("riemann_solver", riemann_solver),
+                      ("slope_limiter", slope_limiter)):
+        enc = val.encode() if val is not None else None
+        keep.append(enc)
+        setattr(ip, attr, enc)
+    ip.cfl = cfl
+    return bcp, ip
+
+
+def run_2d(nx: int, ny: int, g: int, bounds, gamma: float, W: np.ndarray, U: np.ndarray,
+           bc=("periodic",) * 4, integrator="muscl_hancock_2d",
+           riemann_solver="riemann_solver_hllc", slope_limiter="monotonized_central",
+           cfl=0.8, tf=1.0, max_steps=-1, options: HydroGpuOptions | None = None,
+           storing: dict | None = None) -> RunResult:
+    """Run a 2D problem through hydro_gpu_launch_simulation.  W and U are
+    (4, ny+2g, nx+2g) float64 arrays (rho,u,v,p / mass,mom_x,mom_y,energy)."""
+    lib = library()
+    h = _SystemHandle(lib, "cartesian_2d", nx, ny, g, bounds, gamma)
+    try:
+        for dst, src in zip(h.fields(W2), W):
+            dst[:] = np.ascontiguousarray(src, dtype=np.float64).reshape(-1)
+        for dst, src in zip(h.fields(U2), U):
+            dst[:] = np.ascontiguousarray(src, dtype=np.float64).reshape(-1)
+        keep: list = []
+        bcp, ip = _params(lib, bc, integrator, riemann_solver, slope_limiter, cfl, keep)
+        sp = lib.get_new_storing_param()
+        if storing:
+            sp.is_storing = True
+            sp.store_initial = bool(storing.get("store_initial", False))
+            sp.storing_interval = float(storing["interval"])
+            d = storing["output_dir"].encode()
+            keep.append(d)
+            sp.output_dir = d
+        settings = Settings(0, True)
+        simp = SimulationParam(tf)
+        st = SimulationStatus(0, 0.0, 0.0)
+        opt = options if options is not None else lib.hydro_gpu_default_options()
+        if max_steps is not None and max_steps >= 0:
+            opt.max_steps = max_steps
+        stats = HydroGpuStats()
+        code, msg = _consume(lib, lib.hydro_gpu_launch_simulation(
+            C.byref(bcp), C.byref(h.s), C.byref(ip), C.byref(sp), C.byref(settings),
+            C.byref(simp), C.byref(st), C.byref(opt), C.byref(stats)))
+        Wout = np.stack([f.copy() for f in h.fields(W2)]).reshape((4,) + h.shape)
+        Uout = np.stack([f.copy() for f in h.fields(U2)]).reshape((4,) + h.shape)
+        return RunResult(code, msg, Wout, Uout, st.num_steps, st.t, st.dt, _stats_dict(stats))
+    finally:
+        h.close()
+
+
+def run_1d(nx: int, g: int, bounds, gamma: float, W: np.ndarray, U: np.ndarray,
+           bc=("transmissive", "transmissive"), integrator="godunov_first_order_1d",
+           riemann_solver="riemann_solver_exact", slope_limiter="minmod", cfl=0.9, tf=0.2,
+           max_steps=-1, options: HydroGpuOptions | None = None) -> RunResult:
+    """Run a 1D Cartesian problem (W, U: (3, nx+2g))."""
+    lib = library()
+    h = _SystemHandle(lib, "cartesian_1d", nx, 0, g, bounds, gamma)
+    try:
+        for dst, src in zip(h.fields(W1), W):
+            dst[:] = src
+        for dst, src in zip(h.fields(U1), U):
+            dst[:] = src
+        keep: list = []
+        bcp, ip = _params(lib, list(bc) + [None, None], integrator, riemann_solver,
+                          slope_limiter, cfl, keep)
+        sp = lib.get_new_storing_param()
+        settings = Settings(0, True)
+        simp = SimulationParam(tf)
+        st = SimulationStatus(0, 0.0, 0.0)
+        opt = options if options is not None else lib.hydro_gpu_default_options()
+        if max_steps is not None and max_steps >= 0:
+            opt.max_steps = max_steps
+        stats = HydroGpuStats()
+        code, msg = _consume(lib, lib.hydro_gpu_launch_simulation(
+            C.byref(bcp), C.byref(h.s), C.byref(ip), C.byref(sp), C.byref(settings),
+            C.byref(simp), C.byref(st), C.byref(opt), C.byref(stats)))
+        Wout = np.stack([f.copy() for f in h.fields(W1)])
+        Uout = np.stack([f.copy() for f in h.fields(U1)])
+        return RunResult(code, msg, Wout, Uout, st.num_steps, st.t, st.dt, _stats_dict(stats))
+    finally:
+        h.close()
+
+
+class Solver2D:
+    """Device-resident session (hydro_gpu_solver_*): upload once, step many
+    times with the state kept in HBM."""
+
+    def __init__(self, nx, ny, g, bounds, gamma, W, U, bc=("periodic",) * 4,
+                 slope_limiter="monotonized_central", cfl=0.8,
+                 options: HydroGpuOptions | None = None):
+        self.lib = lib = library()
+        self._h = _SystemHandle(lib, "cartesian_2d", nx, ny, g, bounds, gamma)
+        for dst, src in zip(self._h.fields(W2), W):
+            dst[:] = np.ascontiguousarray(src).reshape(-1)
+        for dst, src in zip(self._h.fields(U2), U):
+            dst[:] = np.ascontiguousarray(src).reshape(-1)
+        self._keep: list = []
+        bcp, ip = _params(lib, bc, "muscl_hancock_2d", "riemann_solver_hllc", slope_limiter,
+                          cfl, self._keep)
+        self._bcp, self._ip = bcp, ip
+        opt = options if options is not None else lib.hydro_gpu_default_options()
+        self.handle = C.c_void_p()
+        code, msg = _consume(lib, lib.hydro_gpu_solver_create(
+            C.byref(self.handle), C.byref(bcp), C.byref(self._h.s), C.byref(ip), C.byref(opt)))
+        if code != 0:
+            raise HydroError(code, msg)
+        self.cells = nx * ny
+
+    def restart(self):
+        code, msg = _consume(self.lib, self.lib.hydro_gpu_solver_restart(self.handle))
+        if code != 0:
+            raise HydroError(code, msg)
+
+    def advance(self, steps: int, tf: float = 1e300) -> tuple[SimulationStatus, float]:
+        st = SimulationStatus(0, 0.0, 0.0)
+        ms = C.c_double(0.0)
+        code, msg = _consume(self.lib, self.lib.hydro_gpu_solver_advance(
+            self.handle, steps, tf, C.byref(st), C.byref(ms)))
+        if code != 0:
+            raise HydroError(code, msg)
+        return st, ms.value
+
+    def download(self) -> tuple[np.ndarray, np.ndarray]:
+        code, msg = _consume(self.lib, self.lib.hydro_gpu_solver_download(self.handle,
+                                                                          C.byref(self._h.s)))
+        if code != 0:
+            raise HydroError(code, msg)
+        W = np.stack([f.copy() for f in self._h.fields(W2)]).reshape((4,) + self._h.shape)
+        U = np.stack([f.copy() for f in self._h.fields(U2)]).reshape((4,) + self._h.shape)
+        return W, U
+
+    def kernel_launches(self) -> int:
+        return int(self.lib.hydro_gpu_solver_kernel_launches(self.handle))
+
+    def close(self):
+        if self.handle:
+            self.lib.hydro_gpu_solver_destroy(self.handle)
+            self.handle = C.c_void_p()
+        self._h.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()

@@ -1,0 +1,99 @@
+/*
+ * gpu_bridge.h -- C interface between the host C layer (parameter handling,
+ * validation, error tracebacks, storing) and the CUDA runtime.  Internal to
+ * the library; programs use hydro.h / hydro_gpu.h.
+ */
+#ifndef HYDRO_GPU_BRIDGE_H
+#define HYDRO_GPU_BRIDGE_H
+
+#include "hydro_gpu.h"
+#include "step_control.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Outcome kinds of a bridge call. */
+#define HYDRO_RUN_OK 0
+#define HYDRO_RUN_DEVICE_ERROR 1    /* numerical error raised by a kernel (code = DEV_ERR_*) */
+#define HYDRO_RUN_CUDA_ERROR 2      /* CUDA runtime error (code = cudaError_t) */
+#define HYDRO_RUN_CALLBACK_ERROR 3  /* snapshot callback failed (code = its return value) */
+#define HYDRO_RUN_UNSUPPORTED 4     /* combination not available on the GPU path */
+
+typedef struct HydroRunOutcome
+{
+    int64 num_steps;
+    double t;
+    double dt;
+    int store_count;
+    int kind;
+    int code;
+    int where;
+    char message[256];
+} HydroRunOutcome;
+
+/* A 2D Cartesian problem as the kernels see it. */
+typedef struct HydroGrid2D
+{
+    int nx, ny, g;
+    double gamma, tol;
+    double dx, dy;                /* System.dx_, dy_ */
+    double area_x, area_y, vol;   /* uniform face areas and cell volume */
+    int bc[4];                    /* BOUNDARY_CONDITION_* of x_min, x_max, y_min, y_max */
+    int limiter;                  /* SLOPE_LIMITER_* */
+    int integrator;               /* INTEGRATOR_MUSCL_HANCOCK_2D or INTEGRATOR_GODUNOV_FIRST_ORDER_2D */
+} HydroGrid2D;
+
+/* Called when a snapshot is due; W holds the padded primitive arrays
+ * (host memory, valid for the duration of the call).  Returns 0 on success. */
+typedef int (*HydroSnapshotFn)(void *ctx, double *const W[4], int64 num_steps, double t, double dt);
+
+typedef struct HydroRun2D HydroRun2D;
+
+int hydro_run2d_create(const HydroGrid2D *grid, const HydroGpuOptions *opt,
+                       HydroRun2D **out, HydroRunOutcome *oc);
+/* Upload W and U (padded host arrays); keep_initial keeps a device copy for
+ * hydro_run2d_restore. */
+int hydro_run2d_upload(HydroRun2D *run, double *const W[4], double *const U[4],
+                       int keep_initial, HydroRunOutcome *oc);
+int hydro_run2d_restore(HydroRun2D *run, HydroRunOutcome *oc);
+/* Start a run at t = 0 from the uploaded state. */
+int hydro_run2d_begin(HydroRun2D *run, const HydroStepParams *sp, double tf, int64 max_steps,
+                      int store_count, HydroRunOutcome *oc);
+/* Current step count / time of a begun run. */
+int hydro_run2d_status(HydroRun2D *run, HydroRunOutcome *oc);
+/* Move the stopping criteria of a begun run (t and the step count keep going). */
+int hydro_run2d_set_limits(HydroRun2D *run, double tf, int64 max_steps, HydroRunOutcome *oc);
+/* Step until the run stops (tf, step limit or error), storing snapshots
+ * through `snap` when due.  step_ms (may be NULL) receives the CUDA-event
+ * time of the stepping. */
+int hydro_run2d_advance(HydroRun2D *run, HydroSnapshotFn snap, void *ctx,
+                        HydroRunOutcome *oc, double *step_ms);
+/* Full padded W (ghosts filled) and U of the current state into host arrays. */
+int hydro_run2d_download(HydroRun2D *run, double *const W[4], double *const U[4],
+                         HydroRunOutcome *oc);
+void hydro_run2d_stats(const HydroRun2D *run, HydroGpuStats *stats);
+void hydro_run2d_destroy(HydroRun2D *run);
+
+/* 1D Cartesian problem (Godunov first order or MUSCL-Hancock). */
+typedef struct HydroGrid1D
+{
+    int nx, g;
+    double gamma, tol, dx, area, vol;
+    int bc[2];
+    int limiter;
+    int riemann_solver;           /* RIEMANN_SOLVER_* */
+    int integrator;               /* INTEGRATOR_GODUNOV_FIRST_ORDER_1D or INTEGRATOR_MUSCL_HANCOCK_1D */
+} HydroGrid1D;
+
+/* Whole 1D run in one launch (W, U: padded host arrays, in/out). */
+int hydro_run1d(const HydroGrid1D *grid, double *const W[3], double *const U[3],
+                const HydroStepParams *sp, double tf, int64 max_steps, int store_count,
+                HydroSnapshotFn snap, void *ctx, const HydroGpuOptions *opt,
+                HydroRunOutcome *oc, HydroGpuStats *stats);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1,0 +1,25 @@
+/*
+ * gpu_internal.h -- declarations shared by the CUDA translation units.
+ */
+#ifndef HYDRO_GPU_INTERNAL_H
+#define HYDRO_GPU_INTERNAL_H
+
+#include <cuda_runtime.h>
+
+#include "mh2d_kernel.cuh"
+
+/* Threads per 2D step CTA: a strip of MH2D_THREADS-2 interior columns. */
+#define MH2D_THREADS 128
+
+namespace hydro {
+
+template <class R>
+cudaError_t mh2d_launch_step(const Mh2dArgs<R> &a, int limiter, cudaStream_t s);
+template <class R>
+cudaError_t mh2d_launch_prepare(const Mh2dArgs<R> &a, cudaStream_t s);
+template <class R>
+cudaError_t mh2d_launch_materialize(const Mh2dArgs<R> &a, int buf, R *const out[4], cudaStream_t s);
+
+}  // namespace hydro
+
+#endif

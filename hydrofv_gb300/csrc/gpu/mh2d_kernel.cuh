@@ -1,0 +1,389 @@
+/*
+ * mh2d_kernel.cuh -- fused, unsplit MUSCL-Hancock + HLLC step for 2D
+ * Cartesian grids (one kernel launch per time step).
+ *
+ * Replaces, for one step, src/integrator_muscl_hancock.c:530-1144 (dt, the
+ * x and y sweeps, the conservative update), src/system.c:763-802 (U -> W),
+ * src/boundary.c:513-777 (built-in ghost cells) and src/utils.c:55-95 (the
+ * next step's CFL maxima).
+ *
+ * Work decomposition ("strip marching"): a CTA of NT threads owns a strip of
+ * NT-2 interior columns and a chunk of rows, and marches up the rows.  Thread
+ * t is bound to column c0-1+t; it reconstructs that column's cell in x for
+ * the current row (slots 0..sw+1 include one halo cell per side) and solves
+ * the x face between slot t and t+1, so every x face in the strip is solved
+ * once.  In y each interior thread carries its column upwards: the cell
+ * above is reconstructed once, the face between them is solved once, and the
+ * top-face state and face flux roll over to the next row.  Only the two halo
+ * columns per strip and one extra row of y work per chunk are redundant.
+ *
+ * W rows live in a 3-row shared-memory ring (5 fields: rho, u, v, p and the
+ * sound speed a, which the previous step's epilogue already computed), so a
+ * cell's W is read from HBM once per CTA.  Ghost cells are never stored:
+ * they are produced on load by index remapping (mirror, mirror with a sign
+ * flip, or periodic wrap), which yields exactly the values the reference's
+ * boundary routine copies.  For "none" boundaries the ghost primitives are
+ * converted from the ghost conserved values, as the reference's all-cell
+ * conversion does.
+ *
+ * The update is a gather in the reference's accumulation order
+ * U += F_{i-1/2}; U -= F_{i+1/2}; U += G_{j-1/2}; U -= G_{j+1/2}, each term
+ * (flux*dt)*area, so no atomics and no scatter races.  The first ghost layer
+ * receives its one-sided update too (the reference updates it and the "none"
+ * boundary reads it back).  The epilogue converts the new U to W, stores both
+ * and folds a+|u|, a+|v| into CTA maxima that become the next step's dt.
+ *
+ * Both the state and W are double-buffered (step n reads buffer n&1 and
+ * writes the other), so CTAs never read a halo another CTA has already
+ * overwritten.  Step 0 reads the caller's primitives raw (ghosts included),
+ * matching the reference, whose first step uses the W arrays as handed in.
+ */
+#ifndef HYDRO_GPU_MH2D_KERNEL_CUH
+#define HYDRO_GPU_MH2D_KERNEL_CUH
+
+#include <cuda_runtime.h>
+#include <math_constants.h>
+
+#include "numerics.cuh"
+#include "step_control.h"
+
+namespace hydro {
+
+template <class R>
+struct Mh2dArgs {
+    R *U[2][4];              /* [buffer][mass, mom_x, mom_y, energy] */
+    R *W[2][5];              /* [buffer][rho, u, v, p, a] */
+    HydroStepControl *ctrl;
+    HydroStepParams sp;
+    GasConst<R> gas;
+    int nx, ny, g, pitch;
+    int strip_w;             /* interior columns per strip (NT - 2) */
+    int chunk_h;             /* rows per CTA */
+    int bc[4];               /* x_min, x_max, y_min, y_max */
+    double dx, dy;           /* System.dx_, dy_ (for dt) */
+    double area_x, area_y, vol;
+};
+
+/* Load W at padded (r, c), remapping ghost cells to their source. */
+template <class R>
+__device__ __forceinline__ void fetch_w(const Mh2dArgs<R> &a, const R *const *Win,
+                                        const R *const *Uin, bool raw, int r, int c, R w[5])
+{
+    int rr = r, cc = c, neg = 0;
+    bool cons = false;
+    if (!raw) {
+        const int g = a.g, nx = a.nx, ny = a.ny;
+        int f = 0, k = 0;
+        if (c < g) {
+            f = a.bc[0]; k = g - 1 - c;
+            if (f == BC_NONE) cons = true;
+            else if (f == BC_PERIODIC) cc = g + nx - 1 - k;
+            else { cc = g + k; neg = (f == BC_REFLECTIVE) ? 1 : 0; }
+        } else if (c >= g + nx) {
+            f = a.bc[1]; k = c - g - nx;
+            if (f == BC_NONE) cons = true;
+            else if (f == BC_PERIODIC) cc = g + k;
+            else { cc = g + nx - 1 - k; neg = (f == BC_REFLECTIVE) ? 1 : 0; }
+        } else if (r < g) {
+            f = a.bc[2]; k = g - 1 - r;
+            if (f == BC_NONE) cons = true;
+            else if (f == BC_PERIODIC) rr = g + ny - 1 - k;
+            else { rr = g + k; neg = (f == BC_REFLECTIVE) ? 2 : 0; }
+        } else if (r >= g + ny) {
+            f = a.bc[3]; k = r - g - ny;
+            if (f == BC_NONE) cons = true;
+            else if (f == BC_PERIODIC) rr = g + k;
+            else { rr = g + ny - 1 - k; neg = (f == BC_REFLECTIVE) ? 2 : 0; }
+        }
+    }
+    const long long idx = (long long) rr * a.pitch + cc;
+    if (cons) {
+        cons_to_prim_2d(a.gas, (R) a.vol, Uin[0][idx], Uin[1][idx], Uin[2][idx], Uin[3][idx], w);
+        w[4] = sound_speed(a.gas, w[0], w[3]);
+        return;
+    }
+#pragma unroll
+    for (int q = 0; q < 5; q++) w[q] = Win[q][idx];
+    if (neg == 1) w[1] = -w[1];
+    if (neg == 2) w[2] = -w[2];
+}
+
+__device__ __forceinline__ void record_error(HydroStepControl *ctrl, int code, int where)
+{
+    if (atomicCAS(&ctrl->error_code, 0, code) == 0) ctrl->error_cell = where;
+}
+
+template <class R, int LIM, int NT>
+__global__ void __launch_bounds__(NT) mh2d_step_kernel(const Mh2dArgs<R> a)
+{
+    static_assert(NT % 32 == 0, "NT must be a whole number of warps");
+    HydroStepControl *ctrl = a.ctrl;
+    if (!*(volatile int *) &ctrl->active) return;
+
+    /* ---- dt for this step (src/integrator_muscl_hancock.c:533-549) ---- */
+    const long long n = ctrl->num_steps;
+    const double t_now = ctrl->t;
+    const double Sx = from_ordered_bits(ctrl->smax[n % 3][0]);
+    const double Sy = from_ordered_bits(ctrl->smax[n % 3][1]);
+    const double cfl = (n < a.sp.shrink_steps) ? a.sp.cfl_shrunk : a.sp.cfl;
+    double dt = cfl / (Sx / a.dx + Sy / a.dy);
+    const double tf = ctrl->tf;
+    if (t_now + dt > tf) dt = tf - t_now;
+    if (dt == 0.0) {
+        if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) {
+            ctrl->dt = dt;
+            record_error(ctrl, DEV_ERR_DT_ZERO, -1);
+            ctrl->active = 0;
+        }
+        return;
+    }
+    const R dtr = (R) dt;
+    const R dtA_x = (R) (dt * a.area_x / a.vol);
+    const R dtA_y = (R) (dt * a.area_y / a.vol);
+    const R Ax = (R) a.area_x, Ay = (R) a.area_y;
+
+    const int buf = (int) (n & 1);
+    const bool raw = (n == 0);
+    const R *const *Uin = a.U[buf];
+    R *const *Uout = a.U[buf ^ 1];
+    const R *const *Win = a.W[buf];
+    R *const *Wout = a.W[buf ^ 1];
+
+    __shared__ R ring[3][5][NT + 2];
+    __shared__ R xlo[4][NT];
+    __shared__ R xfl[4][NT];
+    __shared__ double red[2][NT / 32];
+    __shared__ int am_last;
+
+    const int tid = threadIdx.x;
+    const int g = a.g, nx = a.nx, ny = a.ny;
+    const int c0 = g + blockIdx.x * a.strip_w;
+    const int sw = min(a.strip_w, nx - (int) blockIdx.x * a.strip_w);
+    const int r_begin = g + blockIdx.y * a.chunk_h;
+    const int r_end = min(r_begin + a.chunk_h, g + ny);
+    const int col = c0 - 1 + tid;
+    const bool x_slot = tid <= sw + 1;
+    const bool x_face = tid <= sw;
+    const bool inner = tid >= 1 && tid <= sw;
+    const bool ghost_xmin = (c0 == g) && tid == 0;
+    const bool ghost_xmax = (c0 + sw == g + nx) && tid == sw + 1;
+
+    double mx_x = -CUDART_INF, mx_y = -CUDART_INF;
+    int err = DEV_OK;
+
+    /* Rows inside [r_begin, r_end) need the strip plus two halo columns per
+     * side (x work); rows outside need only the strip's own columns. */
+    auto load_row = [&](int r) {
+        const bool full = (r >= r_begin && r < r_end);
+        const int lo = full ? 0 : 2;
+        const int hi = full ? sw + 3 : sw + 1;
+        const int s = r % 3;
+        for (int u = tid; u < NT + 2; u += NT) {
+            if (u >= lo && u <= hi) {
+                R w[5];
+                fetch_w(a, Win, Uin, raw, r, c0 - 2 + u, w);
+#pragma unroll
+                for (int q = 0; q < 5; q++) ring[s][q][u] = w[q];
+            }
+        }
+    };
+
+    /* y reconstruction of this thread's cell in row r (rows r-1..r+1 in the ring).
+     * Outputs are in the y-sweep's (rho, v, u, p) order. */
+    auto recon_y = [&](int r, R lo[4], R hi[4]) {
+        const int u = tid + 1;
+        const int sb = (r + 2) % 3, sc = r % 3, st = (r + 1) % 3;
+        const R rho = ring[sc][0][u], vx = ring[sc][1][u], vy = ring[sc][2][u];
+        const R p = ring[sc][3][u], as = ring[sc][4][u];
+        R d[4];
+        d[0] = limit_slope<LIM>(rho - ring[sb][0][u], ring[st][0][u] - rho);
+        const R dvx = limit_slope<LIM>(vx - ring[sb][1][u], ring[st][1][u] - vx);
+        d[1] = limit_slope<LIM>(vy - ring[sb][2][u], ring[st][2][u] - vy);
+        d[2] = dvx;
+        d[3] = limit_slope<LIM>(p - ring[sb][3][u], ring[st][3][u] - p);
+        hancock_2d(dtA_y, dtA_y / rho, rho, vy, vx, p, as, d, dvx, lo, hi);
+    };
+
+    /* x reconstruction of slot tid in ring row s, (rho, u, v, p) order. */
+    auto recon_x = [&](int s, R lo[4], R hi[4]) {
+        const int u = tid + 1;
+        const R rho = ring[s][0][u], vx = ring[s][1][u], vy = ring[s][2][u];
+        const R p = ring[s][3][u], as = ring[s][4][u];
+        R d[4];
+        d[0] = limit_slope<LIM>(rho - ring[s][0][u - 1], ring[s][0][u + 1] - rho);
+        d[1] = limit_slope<LIM>(vx - ring[s][1][u - 1], ring[s][1][u + 1] - vx);
+        d[2] = limit_slope<LIM>(vy - ring[s][2][u - 1], ring[s][2][u + 1] - vy);
+        d[3] = limit_slope<LIM>(p - ring[s][3][u - 1], ring[s][3][u + 1] - p);
+        hancock_2d(dtA_x, dtA_x / rho, rho, vx, vy, p, as, d, d[1], lo, hi);
+    };
+
+    /* ---- prologue: the face below r_begin ---- */
+    load_row(r_begin - 2);
+    load_row(r_begin - 1);
+    load_row(r_begin);
+    __syncthreads();
+    R ytop[4], gbot[4];
+    R tmp_lo[4], prev_hi[4];
+    if (inner) recon_y(r_begin - 1, tmp_lo, prev_hi);
+    __syncthreads();
+    load_row(r_begin + 1);
+    __syncthreads();
+    if (inner) {
+        recon_y(r_begin, tmp_lo, ytop);
+        const int rc = hllc_flux_2d(a.gas, prev_hi[0], prev_hi[1], prev_hi[2], prev_hi[3],
+                                    tmp_lo[0], tmp_lo[1], tmp_lo[2], tmp_lo[3], gbot);
+        if (rc) err = rc;
+    }
+    __syncthreads();
+
+    /* ---- march up the rows ---- */
+    for (int r = r_begin; r < r_end; r++) {
+        load_row(r + 2);
+        __syncthreads();
+
+        R gtop[4], nlo[4], nhi[4];
+        if (inner) {
+            recon_y(r + 1, nlo, nhi);
+            const int rc = hllc_flux_2d(a.gas, ytop[0], ytop[1], ytop[2], ytop[3],
+                                        nlo[0], nlo[1], nlo[2], nlo[3], gtop);
+            if (rc) err = rc;
+        }
+        R xl[4], xh[4];
+        if (x_slot) {
+            recon_x(r % 3, xl, xh);
+#pragma unroll
+            for (int q = 0; q < 4; q++) xlo[q][tid] = xl[q];
+        }
+        __syncthreads();
+
+        R fx[4];
+        if (x_face) {
+            const int rc = hllc_flux_2d(a.gas, xh[0], xh[1], xh[2], xh[3],
+                                        xlo[0][tid + 1], xlo[1][tid + 1], xlo[2][tid + 1],
+                                        xlo[3][tid + 1], fx);
+            if (rc) err = rc;
+#pragma unroll
+            for (int q = 0; q < 4; q++) xfl[q][tid] = fx[q];
+        }
+        __syncthreads();
+
+        const long long rowbase = (long long) r * a.pitch;
+        if (inner) {
+            const long long idx = rowbase + col;
+            /* y fluxes come back as (mass, mom_y, mom_x, energy) */
+            const int ymap[4] = { 0, 2, 1, 3 };
+            R Un[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                R v = Uin[q][idx];
+                v = v + (xfl[q][tid - 1] * dtr) * Ax;
+                v = v - (fx[q] * dtr) * Ax;
+                v = v + (gbot[ymap[q]] * dtr) * Ay;
+                v = v - (gtop[ymap[q]] * dtr) * Ay;
+                Un[q] = v;
+                Uout[q][idx] = v;
+            }
+            R w[4];
+            cons_to_prim_2d(a.gas, (R) a.vol, Un[0], Un[1], Un[2], Un[3], w);
+            const R as = sound_speed(a.gas, w[0], w[3]);
+#pragma unroll
+            for (int q = 0; q < 4; q++) Wout[q][idx] = w[q];
+            Wout[4][idx] = as;
+            const double sx = (double) (as + fabs(w[1]));
+            const double sy = (double) (as + fabs(w[2]));
+            if (sx > mx_x) mx_x = sx;
+            if (sy > mx_y) mx_y = sy;
+
+            /* first ghost row below / above the domain: one-sided update */
+            if (r == g) {
+                const long long gi = idx - a.pitch;
+#pragma unroll
+                for (int q = 0; q < 4; q++)
+                    Uout[q][gi] = Uin[q][gi] - (gbot[ymap[q]] * dtr) * Ay;
+            }
+            if (r == g + ny - 1) {
+                const long long gi = idx + a.pitch;
+#pragma unroll
+                for (int q = 0; q < 4; q++)
+                    Uout[q][gi] = Uin[q][gi] + (gtop[ymap[q]] * dtr) * Ay;
+            }
+        }
+        /* first ghost column left / right of the domain */
+        if (ghost_xmin) {
+            const long long gi = rowbase + col;
+#pragma unroll
+            for (int q = 0; q < 4; q++) Uout[q][gi] = Uin[q][gi] - (fx[q] * dtr) * Ax;
+        }
+        if (ghost_xmax) {
+            const long long gi = rowbase + col;
+#pragma unroll
+            for (int q = 0; q < 4; q++) Uout[q][gi] = Uin[q][gi] + (xfl[q][tid - 1] * dtr) * Ax;
+        }
+
+        if (inner) {
+#pragma unroll
+            for (int q = 0; q < 4; q++) { ytop[q] = nhi[q]; gbot[q] = gtop[q]; }
+        }
+    }
+
+    if (err) record_error(ctrl, err, c0 + (int) blockIdx.y);
+
+    /* ---- CTA maxima -> device maxima for the next step's dt ---- */
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const double ox = __shfl_xor_sync(0xffffffffu, mx_x, o);
+        const double oy = __shfl_xor_sync(0xffffffffu, mx_y, o);
+        if (ox > mx_x) mx_x = ox;
+        if (oy > mx_y) mx_y = oy;
+    }
+    if ((tid & 31) == 0) {
+        red[0][tid >> 5] = mx_x;
+        red[1][tid >> 5] = mx_y;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        double bx = red[0][0], by = red[1][0];
+        for (int w = 1; w < NT / 32; w++) {
+            if (red[0][w] > bx) bx = red[0][w];
+            if (red[1][w] > by) by = red[1][w];
+        }
+        const int nxt = (int) ((n + 1) % 3);
+        atomicMax(&ctrl->smax[nxt][0], ordered_bits(bx));
+        atomicMax(&ctrl->smax[nxt][1], ordered_bits(by));
+        __threadfence();
+        const unsigned total = gridDim.x * gridDim.y;
+        am_last = (atomicAdd(&ctrl->blocks_done, 1u) == total - 1);
+    }
+    __syncthreads();
+
+    /* ---- last CTA: advance the clock (src/integrator_muscl_hancock.c:1143-1154) ---- */
+    if (am_last && tid == 0) {
+        __threadfence();
+        volatile HydroStepControl *vc = ctrl;
+        ctrl->dt = dt;
+        if (vc->error_code != 0) {
+            ctrl->active = 0;
+        } else {
+            const double tn = t_now + dt;
+            const long long nn = n + 1;
+            ctrl->t = tn;
+            ctrl->num_steps = nn;
+            const int nn2 = (int) ((n + 2) % 3);
+            ctrl->smax[nn2][0] = ordered_bits(-CUDART_INF);
+            ctrl->smax[nn2][1] = ordered_bits(-CUDART_INF);
+            int act = (tn < tf) && (vc->max_steps < 0 || nn < vc->max_steps);
+            if (a.sp.is_storing &&
+                tn >= a.sp.storing_interval *
+                          (double) (vc->store_count - a.sp.store_initial_offset + 1)) {
+                ctrl->snapshot_due = 1;
+                act = 0;
+            }
+            ctrl->active = act;
+        }
+        ctrl->blocks_done = 0;
+    }
+}
+
+}  // namespace hydro
+
+#endif

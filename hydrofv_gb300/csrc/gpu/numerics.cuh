@@ -1,0 +1,609 @@
+/*
+ * numerics.cuh -- pointwise finite-volume numerics shared by every kernel.
+ *
+ * Device (and host-callable) restatements of hydroFV's pointwise routines.
+ * Each expression keeps the reference's operand order and grouping so that
+ * the FP64 kernels, compiled with --fmad=false, perform the same IEEE-754
+ * operation sequence as the reference CPU code:
+ *
+ *   sound speed           src/utils.c:23-26
+ *   slope limiters        src/slope_limiter.c:49-91
+ *   star-pressure guess   src/riemann_solver.c:154-224
+ *   vacuum sampling       src/riemann_solver.c:230-733
+ *   HLLC 2D / 1D          src/riemann_solver_hllc.c:30-40, :42-200, :202-376
+ *   exact solver 1D       src/riemann_solver_exact.c:332-1080
+ *   Hancock predictor     src/integrator_muscl_hancock.c:682-755 (x),
+ *                         :967-1041 (y), :185-246 (1D)
+ *   U -> W conversion     src/system.c:735-802
+ *
+ * Constants the reference recomputes inline on every call (gamma+1,
+ * (gamma-1)/(gamma+1), 0.5+0.5/gamma, ...) are computed once on the host with
+ * the identical expression and passed in `GasConst`; the result is the same
+ * double, so this changes nothing but the instruction count.
+ */
+#ifndef HYDRO_GPU_NUMERICS_CUH
+#define HYDRO_GPU_NUMERICS_CUH
+
+#include <math.h>
+#include <string.h>
+#ifdef __cplusplus
+#include <cmath>
+using std::fabs;
+using std::fmin;
+using std::pow;
+using std::sqrt;
+#endif
+
+#ifdef __CUDACC__
+#define HD __host__ __device__ __forceinline__
+#else
+#define HD static inline
+#endif
+
+namespace hydro {
+
+enum : int {
+    LIM_MINMOD = 1,
+    LIM_VAN_LEER = 2,
+    LIM_MC = 3,
+};
+
+enum : int {
+    BC_NONE = 1,
+    BC_REFLECTIVE = 2,
+    BC_TRANSMISSIVE = 3,
+    BC_PERIODIC = 4,
+};
+
+/* Device error codes (mapped to ErrorStatus on the host). */
+enum : int {
+    DEV_OK = 0,
+    DEV_ERR_HLLC_WAVE_SPEED = 1,   /* src/riemann_solver_hllc.c:372-375 */
+    DEV_ERR_DT_ZERO = 2,           /* src/integrator_muscl_hancock.c:545-549 */
+    DEV_ERR_EXACT_BRACKET = 3,     /* src/riemann_solver_exact.c:702-707 */
+    DEV_ERR_EXACT_BISECTION = 4,   /* src/riemann_solver_exact.c:745-754 */
+    DEV_ERR_SPIN_LIMIT = 5,        /* a bounded device-side wait gave up */
+};
+
+template <class R>
+struct GasConst {
+    R gamma;
+    R gm1;          /* gamma - 1.0 */
+    R gp1;          /* gamma + 1.0 */
+    R half_gm1;     /* 0.5 * (gamma - 1.0) */
+    R half_gm1_g;   /* (0.5 * (gamma - 1.0)) / gamma */
+    R g_half_gm1;   /* gamma / (0.5 * (gamma - 1.0)) */
+    R q_coef;       /* 0.5 + 0.5 / gamma */
+    R gm1_gp1;      /* (gamma - 1.0) / (gamma + 1.0) */
+    R two_gp1;      /* 2.0 / (gamma + 1.0) */
+    R two_gm1;      /* 2.0 / (gamma - 1.0) */
+    R g_gm1;        /* gamma / (gamma - 1.0) */
+    R gm1_2g;       /* (gamma - 1.0) / (2.0 * gamma) */
+    R gp1_2g;       /* (gamma + 1.0) / (2.0 * gamma) */
+    R neg_gp1_2g;   /* -0.5 * (gamma + 1.0) / gamma */
+    R inv_g;        /* 1.0 / gamma */
+    R tol;          /* integrator tolerance (guess_p floor, exact solver) */
+};
+
+/* Build the constants with the reference's own expressions. */
+template <class R>
+HD GasConst<R> make_gas_const(double gamma, double tol)
+{
+    GasConst<R> c;
+    c.gamma = (R) gamma;
+    c.gm1 = (R) (gamma - 1.0);
+    c.gp1 = (R) (gamma + 1.0);
+    c.half_gm1 = (R) (0.5 * (gamma - 1.0));
+    c.half_gm1_g = (R) ((0.5 * (gamma - 1.0)) / gamma);
+    c.g_half_gm1 = (R) (gamma / (0.5 * (gamma - 1.0)));
+    c.q_coef = (R) (0.5 + 0.5 / gamma);
+    c.gm1_gp1 = (R) ((gamma - 1.0) / (gamma + 1.0));
+    c.two_gp1 = (R) (2.0 / (gamma + 1.0));
+    c.two_gm1 = (R) (2.0 / (gamma - 1.0));
+    c.g_gm1 = (R) (gamma / (gamma - 1.0));
+    c.gm1_2g = (R) ((gamma - 1.0) / (2.0 * gamma));
+    c.gp1_2g = (R) ((gamma + 1.0) / (2.0 * gamma));
+    c.neg_gp1_2g = (R) (-0.5 * (gamma + 1.0) / gamma);
+    c.inv_g = (R) (1.0 / gamma);
+    c.tol = (R) tol;
+    return c;
+}
+
+/* ------------------------------------------------------------------ basics */
+
+template <class R>
+HD R sound_speed(const GasConst<R> &c, R rho, R p)
+{
+    return sqrt(c.gamma * p / rho);
+}
+
+template <int LIM, class R>
+HD R limit_slope(R a, R b)
+{
+    if (a * b <= R(0)) return R(0);
+    if (LIM == LIM_MINMOD) return (fabs(a) < fabs(b)) ? a : b;
+    if (LIM == LIM_VAN_LEER) return R(2) * a * b / (a + b + R(1e-10));
+    if (a > R(0)) return fmin(R(0.5) * (a + b), R(2) * fmin(fabs(a), fabs(b)));
+    return -fmin(R(-0.5) * (a + b), R(2) * fmin(fabs(a), fabs(b)));
+}
+
+/* Runtime-dispatched limiter (1D paths and host exports). */
+template <class R>
+HD R limit_slope_rt(int lim, R a, R b)
+{
+    switch (lim) {
+    case LIM_MINMOD: return limit_slope<LIM_MINMOD>(a, b);
+    case LIM_VAN_LEER: return limit_slope<LIM_VAN_LEER>(a, b);
+    default: return limit_slope<LIM_MC>(a, b);
+    }
+}
+
+/* Star-pressure guess (PVRS / two-rarefaction / two-shock). */
+template <class R>
+HD R guess_p(const GasConst<R> &c, R rho_L, R u_L, R p_L, R a_L,
+             R rho_R, R u_R, R p_R, R a_R)
+{
+    const R p_min = (p_L > p_R) ? p_R : p_L;
+    const R p_max = (p_L > p_R) ? p_L : p_R;
+    const R ppv = R(0.5) * (p_L + p_R) - R(0.125) * (u_R - u_L) * (rho_L + rho_R) * (a_L + a_R);
+    R pg;
+    if (p_max / p_min <= R(2) && (p_min <= ppv && ppv <= p_max)) {
+        pg = ppv;
+    } else if (ppv < p_min) {
+        pg = (a_L + a_R - c.half_gm1 * (u_R - u_L))
+           / (a_L / pow(p_L, c.half_gm1_g) + a_R / pow(p_R, c.half_gm1_g));
+        pg = pow(pg, c.g_half_gm1);
+    } else {
+        const R gL = sqrt((R(2) / (c.gp1 * rho_L)) / (ppv + p_L * c.gm1_gp1));
+        const R gR = sqrt((R(2) / (c.gp1 * rho_R)) / (ppv + p_R * c.gm1_gp1));
+        pg = (gL * p_L + gR * p_R - (u_R - u_L)) / (gL + gR);
+    }
+    if (pg < c.tol) pg = c.tol;
+    return pg;
+}
+
+/* ---------------------------------------------------------------- vacuum */
+
+template <class R>
+HD void sample_right_vacuum(const GasConst<R> &c, R rho, R u, R v, R p, R a, R S, R o[4])
+{
+    if (S <= (u - a)) { o[0] = rho; o[1] = u; o[2] = v; o[3] = p; return; }
+    const R front = u + R(2) * a / c.gm1;
+    if (S < front) {
+        R tmp = c.two_gp1 + (u - S) * c.gm1 / (c.gp1 * a);
+        tmp = pow(tmp, c.two_gm1);
+        o[0] = rho * tmp;
+        o[1] = (a + c.half_gm1 * u + S) * R(2) / c.gp1;
+        o[2] = v;
+        o[3] = p * pow(tmp, c.gamma);
+    } else {
+        o[0] = R(0); o[1] = R(0); o[2] = R(0); o[3] = R(0);
+    }
+}
+
+template <class R>
+HD void sample_left_vacuum(const GasConst<R> &c, R rho, R u, R v, R p, R a, R S, R o[4])
+{
+    if (S >= (u + a)) { o[0] = rho; o[1] = u; o[2] = v; o[3] = p; return; }
+    const R front = u - R(2) * a / c.gm1;
+    if (S > front) {
+        R tmp = c.two_gp1 - (u - S) * c.gm1 / (c.gp1 * a);
+        tmp = pow(tmp, c.two_gm1);
+        o[0] = rho * tmp;
+        o[1] = (-a + c.half_gm1 * u + S) * R(2) / c.gp1;
+        o[2] = v;
+        o[3] = p * pow(tmp, c.gamma);
+    } else {
+        o[0] = R(0); o[1] = R(0); o[2] = R(0); o[3] = R(0);
+    }
+}
+
+/* The reference routes rho_L <= 0 to the "right vacuum" sampler fed with the
+ * left state, and uses 2a/(gamma-1) (no velocity term) as the
+ * vacuum-generation front speeds; both are kept as written. */
+template <class R>
+HD void solve_vacuum(const GasConst<R> &c,
+                     R rho_L, R u_L, R v_L, R p_L, R a_L,
+                     R rho_R, R u_R, R v_R, R p_R, R a_R, R S, R o[4])
+{
+    if (rho_L <= R(0) && rho_R <= R(0)) { o[0] = o[1] = o[2] = o[3] = R(0); return; }
+    if (rho_L <= R(0)) { sample_right_vacuum(c, rho_L, u_L, v_L, p_L, a_L, S, o); return; }
+    if (rho_R <= R(0)) { sample_left_vacuum(c, rho_R, u_R, v_R, p_R, a_R, S, o); return; }
+    const R SL = R(2) * a_L / c.gm1;
+    const R SR = R(2) * a_R / c.gm1;
+    if (S <= SL) { sample_right_vacuum(c, rho_L, u_L, v_L, p_L, a_L, S, o); return; }
+    if (SR <= S) { sample_left_vacuum(c, rho_R, u_R, v_R, p_R, a_R, S, o); return; }
+    o[0] = o[1] = o[2] = o[3] = R(0);
+}
+
+/* ------------------------------------------------------------------ HLLC */
+
+template <class R>
+HD R hllc_q(const GasConst<R> &c, R p_X, R p_star)
+{
+    if (p_star <= p_X) return R(1);
+    return sqrt(R(1) + c.q_coef * (p_star / p_X - R(1)));
+}
+
+/*
+ * HLLC flux, 2D form.  (u = normal velocity, v = tangential.)  F receives
+ * (mass, normal momentum, tangential momentum, energy).  Returns DEV_OK or
+ * DEV_ERR_HLLC_WAVE_SPEED (no branch matched, i.e. a NaN wave speed).
+ */
+template <class R>
+HD int hllc_flux_2d(const GasConst<R> &c, R rho_L, R u_L, R v_L, R p_L,
+                    R rho_R, R u_R, R v_R, R p_R, R F[4])
+{
+    const R a_L = (rho_L > R(0)) ? sound_speed(c, rho_L, p_L) : R(0);
+    const R a_R = (rho_R > R(0)) ? sound_speed(c, rho_R, p_R) : R(0);
+    if (rho_L <= R(0) || rho_R <= R(0) || ((a_L + a_R) * R(2) / c.gp1) <= (u_R - u_L)) {
+        R s[4];
+        solve_vacuum(c, rho_L, u_L, v_L, p_L, a_L, rho_R, u_R, v_R, p_R, a_R, R(0), s);
+        const R E = s[0] * (R(0.5) * (s[1] * s[1] + s[2] * s[2]) + s[3] / (s[0] * c.gm1));
+        F[0] = s[0] * s[1];
+        F[1] = s[0] * s[1] * s[1] + s[3];
+        F[2] = s[0] * s[1] * s[2];
+        F[3] = s[1] * (E + s[3]);
+        return DEV_OK;
+    }
+    const R ps = guess_p(c, rho_L, u_L, p_L, a_L, rho_R, u_R, p_R, a_R);
+    const R S_L = u_L - a_L * hllc_q(c, p_L, ps);
+    const R S_R = u_R + a_R * hllc_q(c, p_R, ps);
+    const R S_s = (p_R - p_L + rho_L * u_L * (S_L - u_L) - rho_R * u_R * (S_R - u_R))
+                / (rho_L * (S_L - u_L) - rho_R * (S_R - u_R));
+    if (R(0) <= S_L) {
+        const R E = rho_L * (R(0.5) * (u_L * u_L + v_L * v_L) + p_L / (rho_L * c.gm1));
+        F[0] = rho_L * u_L;
+        F[1] = rho_L * u_L * u_L + p_L;
+        F[2] = rho_L * u_L * v_L;
+        F[3] = u_L * (E + p_L);
+        return DEV_OK;
+    }
+    if (S_L <= R(0) && R(0) <= S_s) {
+        const R E = rho_L * (R(0.5) * (u_L * u_L + v_L * v_L) + p_L / (rho_L * c.gm1));
+        const R fm = rho_L * u_L;
+        const R rs = rho_L * (S_L - u_L) / (S_L - S_s);
+        const R es = rs * (E / rho_L + (S_s - u_L) * (S_s + p_L / (rho_L * (S_L - u_L))));
+        F[0] = fm + S_L * (rs - rho_L);
+        F[1] = (fm * u_L + p_L) + S_L * (rs * S_s - rho_L * u_L);
+        F[2] = fm * v_L + S_L * (rs * v_L - rho_L * v_L);
+        F[3] = u_L * (E + p_L) + S_L * (es - E);
+        return DEV_OK;
+    }
+    if (S_s <= R(0) && R(0) <= S_R) {
+        const R E = rho_R * (R(0.5) * (u_R * u_R + v_R * v_R) + p_R / (rho_R * c.gm1));
+        const R fm = rho_R * u_R;
+        const R rs = rho_R * (S_R - u_R) / (S_R - S_s);
+        const R es = rs * (E / rho_R + (S_s - u_R) * (S_s + p_R / (rho_R * (S_R - u_R))));
+        F[0] = fm + S_R * (rs - rho_R);
+        F[1] = (fm * u_R + p_R) + S_R * (rs * S_s - rho_R * u_R);
+        F[2] = fm * v_R + S_R * (rs * v_R - rho_R * v_R);
+        F[3] = u_R * (E + p_R) + S_R * (es - E);
+        return DEV_OK;
+    }
+    if (S_R <= R(0)) {
+        const R E = rho_R * (R(0.5) * (u_R * u_R + v_R * v_R) + p_R / (rho_R * c.gm1));
+        F[0] = rho_R * u_R;
+        F[1] = rho_R * u_R * u_R + p_R;
+        F[2] = rho_R * u_R * v_R;
+        F[3] = u_R * (E + p_R);
+        return DEV_OK;
+    }
+    return DEV_ERR_HLLC_WAVE_SPEED;
+}
+
+/* HLLC flux, 1D form (energy density groups 0.5*u*u as (0.5*u)*u). */
+template <class R>
+HD int hllc_flux_1d(const GasConst<R> &c, R rho_L, R u_L, R p_L, R rho_R, R u_R, R p_R, R F[3])
+{
+    const R a_L = (rho_L > R(0)) ? sound_speed(c, rho_L, p_L) : R(0);
+    const R a_R = (rho_R > R(0)) ? sound_speed(c, rho_R, p_R) : R(0);
+    if (rho_L <= R(0) || rho_R <= R(0) || ((a_L + a_R) * R(2) / c.gp1) <= (u_R - u_L)) {
+        R s[4];
+        solve_vacuum(c, rho_L, u_L, R(0), p_L, a_L, rho_R, u_R, R(0), p_R, a_R, R(0), s);
+        const R E = s[0] * (R(0.5) * s[1] * s[1] + s[3] / (s[0] * c.gm1));
+        F[0] = s[0] * s[1];
+        F[1] = s[0] * s[1] * s[1] + s[3];
+        F[2] = s[1] * (E + s[3]);
+        return DEV_OK;
+    }
+    const R ps = guess_p(c, rho_L, u_L, p_L, a_L, rho_R, u_R, p_R, a_R);
+    const R S_L = u_L - a_L * hllc_q(c, p_L, ps);
+    const R S_R = u_R + a_R * hllc_q(c, p_R, ps);
+    const R S_s = (p_R - p_L + rho_L * u_L * (S_L - u_L) - rho_R * u_R * (S_R - u_R))
+                / (rho_L * (S_L - u_L) - rho_R * (S_R - u_R));
+    if (R(0) <= S_L) {
+        const R E = rho_L * (R(0.5) * u_L * u_L + p_L / (rho_L * c.gm1));
+        F[0] = rho_L * u_L;
+        F[1] = rho_L * u_L * u_L + p_L;
+        F[2] = u_L * (E + p_L);
+        return DEV_OK;
+    }
+    if (S_L <= R(0) && R(0) <= S_s) {
+        const R E = rho_L * (R(0.5) * u_L * u_L + p_L / (rho_L * c.gm1));
+        const R fm = rho_L * u_L;
+        const R rs = rho_L * (S_L - u_L) / (S_L - S_s);
+        const R es = rs * (E / rho_L + (S_s - u_L) * (S_s + p_L / (rho_L * (S_L - u_L))));
+        F[0] = fm + S_L * (rs - rho_L);
+        F[1] = (fm * u_L + p_L) + S_L * (rs * S_s - rho_L * u_L);
+        F[2] = u_L * (E + p_L) + S_L * (es - E);
+        return DEV_OK;
+    }
+    if (S_s <= R(0) && R(0) <= S_R) {
+        const R E = rho_R * (R(0.5) * u_R * u_R + p_R / (rho_R * c.gm1));
+        const R fm = rho_R * u_R;
+        const R rs = rho_R * (S_R - u_R) / (S_R - S_s);
+        const R es = rs * (E / rho_R + (S_s - u_R) * (S_s + p_R / (rho_R * (S_R - u_R))));
+        F[0] = fm + S_R * (rs - rho_R);
+        F[1] = (fm * u_R + p_R) + S_R * (rs * S_s - rho_R * u_R);
+        F[2] = u_R * (E + p_R) + S_R * (es - E);
+        return DEV_OK;
+    }
+    if (S_R <= R(0)) {
+        const R E = rho_R * (R(0.5) * u_R * u_R + p_R / (rho_R * c.gm1));
+        F[0] = rho_R * u_R;
+        F[1] = rho_R * u_R * u_R + p_R;
+        F[2] = u_R * (E + p_R);
+        return DEV_OK;
+    }
+    return DEV_ERR_HLLC_WAVE_SPEED;
+}
+
+/* ---------------------------------------------------------- exact solver */
+
+template <class R>
+HD R exact_fK(const GasConst<R> &c, R rho, R p, R a, R ps)
+{
+    if (ps > p) {
+        const R A = R(2) / (c.gp1 * rho);
+        const R B = p * c.gm1_gp1;
+        return (ps - p) * sqrt(A / (ps + B));
+    }
+    return R(2) * a * (pow((ps / p), c.gm1_2g) - R(1)) / c.gm1;
+}
+
+/* Derivative; the shock branch's (B - p*) follows the reference
+ * (src/riemann_solver_exact.c:550-556). */
+template <class R>
+HD R exact_dfK(const GasConst<R> &c, R rho, R p, R a, R ps)
+{
+    if (ps > p) {
+        const R A = R(2) / (c.gp1 * rho);
+        const R B = p * c.gm1_gp1;
+        return (R(1) - R(0.5) * (ps - p) / (B - ps)) * sqrt(A / (B + ps));
+    }
+    return pow(ps / p, c.neg_gp1_2g) / (p * a);
+}
+
+template <class R>
+HD R exact_f(const GasConst<R> &c, R rho_L, R u_L, R p_L, R a_L, R rho_R, R u_R, R p_R, R a_R, R ps)
+{
+    return exact_fK(c, rho_L, p_L, a_L, ps) + exact_fK(c, rho_R, p_R, a_R, ps) + (u_R - u_L);
+}
+
+/* Newton-Raphson (<= 100 iterations) with a bracketed bisection fallback
+ * (<= 5000 iterations): every loop is bounded. */
+template <class R>
+HD int exact_p_star(const GasConst<R> &c, R rho_L, R u_L, R p_L, R a_L,
+                    R rho_R, R u_R, R p_R, R a_R, R *out)
+{
+    const R pg = guess_p(c, rho_L, u_L, p_L, a_L, rho_R, u_R, p_R, a_R);
+    bool bracket = false;
+    R p_hi = pg;
+    R f_hi = exact_f(c, rho_L, u_L, p_L, a_L, rho_R, u_R, p_R, a_R, p_hi);
+    R p_lo = R(0), f_lo = R(0);
+    R p0 = pg;
+    for (int it = 0; it < 100; it++) {
+        const R f = exact_f(c, rho_L, u_L, p_L, a_L, rho_R, u_R, p_R, a_R, p0);
+        const R fp = exact_dfK(c, rho_L, p_L, a_L, p0) + exact_dfK(c, rho_R, p_R, a_R, p0);
+        if (!bracket && f * f_hi < R(0)) {
+            bracket = true;
+            f_lo = f;
+            p_lo = p0;
+        }
+        const R p1 = p0 - f / fp;
+        if (p1 < R(0)) break;
+        if (R(2) * fabs(p1 - p0) / (p1 + p0) < c.tol) {
+            *out = p1;
+            return DEV_OK;
+        }
+        p0 = p1;
+    }
+    if (!bracket) {
+        p_lo = R(0);
+        f_lo = exact_f(c, rho_L, u_L, p_L, a_L, rho_R, u_R, p_R, a_R, p_lo);
+        if (f_lo * f_hi >= R(0)) {
+            p_hi *= R(10);
+            const R dp = (p_hi - p_lo) / R(100);
+            for (int i = 0; i < 100; i++) {
+                const R a = p_lo + R(i) * dp;
+                const R b = p_lo + R(i + 1) * dp;
+                const R fa = exact_f(c, rho_L, u_L, p_L, a_L, rho_R, u_R, p_R, a_R, a);
+                const R fb = exact_f(c, rho_L, u_L, p_L, a_L, rho_R, u_R, p_R, a_R, b);
+                if (fa * fb < R(0)) {
+                    p_lo = a; f_lo = fa; p_hi = b; f_hi = fb;
+                    break;
+                }
+            }
+            if (f_lo * f_hi >= R(0)) return DEV_ERR_EXACT_BRACKET;
+        }
+    }
+    for (int count = 1; count <= 5001; count++) {
+        const R pm = R(0.5) * (p_lo + p_hi);
+        if (p_hi - p_lo < c.tol) {
+            *out = pm;
+            return DEV_OK;
+        }
+        const R fm = exact_f(c, rho_L, u_L, p_L, a_L, rho_R, u_R, p_R, a_R, pm);
+        if (fm * f_lo < R(0)) { p_hi = pm; f_hi = fm; }
+        else { p_lo = pm; f_lo = fm; }
+    }
+    return DEV_ERR_EXACT_BISECTION;
+}
+
+template <class R>
+HD void exact_sample(const GasConst<R> &c, R rho_L, R u_L, R p_L, R a_L,
+                     R rho_R, R u_R, R p_R, R a_R, R us, R ps, R S, R o[3])
+{
+    if (S < us) {
+        if (ps > p_L) {
+            const R r = ps / p_L;
+            const R SL = u_L - a_L * sqrt(c.gp1_2g * r + c.gm1_2g);
+            if (S < SL) { o[0] = rho_L; o[1] = u_L; o[2] = p_L; return; }
+            const R k = c.gm1_gp1;
+            o[0] = rho_L * (r + k) / (k * r + R(1));
+            o[1] = us;
+            o[2] = ps;
+            return;
+        }
+        const R SH = u_L - a_L;
+        if (S < SH) { o[0] = rho_L; o[1] = u_L; o[2] = p_L; return; }
+        const R as = a_L * pow(ps / p_L, c.gm1_2g);
+        if (S < us - as) {
+            const R cm = pow((c.two_gp1 + (u_L - S) * (c.gm1 / (a_L * c.gp1))), c.two_gm1);
+            o[0] = rho_L * cm;
+            o[1] = c.two_gp1 * (a_L + R(0.5) * u_L * c.gm1 + S);
+            o[2] = p_L * pow(cm, c.gamma);
+            return;
+        }
+        o[0] = rho_L * pow(ps / p_L, c.inv_g);
+        o[1] = us;
+        o[2] = ps;
+        return;
+    }
+    if (ps > p_R) {
+        const R r = ps / p_R;
+        const R SR = u_R + a_R * sqrt(r * c.gp1 / (R(2) * c.gamma) + c.gm1_2g);
+        if (S > SR) { o[0] = rho_R; o[1] = u_R; o[2] = p_R; return; }
+        const R k = c.gm1_gp1;
+        o[0] = rho_R * (r + k) / (k * r + R(1));
+        o[1] = us;
+        o[2] = ps;
+        return;
+    }
+    const R SH = u_R + a_R;
+    if (S > SH) { o[0] = rho_R; o[1] = u_R; o[2] = p_R; return; }
+    const R as = a_R * pow(ps / p_R, c.gm1_2g);
+    if (S > us + as) {
+        const R cm = pow((c.two_gp1 - (u_R - S) * c.gm1 / (a_R * c.gp1)), c.two_gm1);
+        o[0] = rho_R * cm;
+        o[1] = c.two_gp1 * (-a_R + R(0.5) * u_R * c.gm1 + S);
+        o[2] = p_R * pow(cm, c.gamma);
+        return;
+    }
+    o[0] = rho_R * pow(ps / p_R, c.inv_g);
+    o[1] = us;
+    o[2] = ps;
+}
+
+/* Exact solution sampled at x/t = S (src/riemann_solver_exact.c:332-469).
+ * o = (rho, u, p).  On a p* failure o is zeroed and the error returned. */
+template <class R>
+HD int exact_solve_1d(const GasConst<R> &c, R rho_L, R u_L, R p_L, R rho_R, R u_R, R p_R, R S, R o[3])
+{
+    const R a_L = (rho_L > R(0)) ? sound_speed(c, rho_L, p_L) : R(0);
+    const R a_R = (rho_R > R(0)) ? sound_speed(c, rho_R, p_R) : R(0);
+    if (rho_L <= R(0) || rho_R <= R(0) || ((a_L + a_R) * R(2) / c.gp1) <= (u_R - u_L)) {
+        R s[4];
+        solve_vacuum(c, rho_L, u_L, R(0), p_L, a_L, rho_R, u_R, R(0), p_R, a_R, S, s);
+        o[0] = s[0]; o[1] = s[1]; o[2] = s[3];
+        return DEV_OK;
+    }
+    R ps = R(0);
+    const int rc = exact_p_star(c, rho_L, u_L, p_L, a_L, rho_R, u_R, p_R, a_R, &ps);
+    if (rc != DEV_OK) { o[0] = o[1] = o[2] = R(0); return rc; }
+    const R us = R(0.5) * (u_L + u_R)
+               + R(0.5) * (exact_fK(c, rho_R, p_R, a_R, ps) - exact_fK(c, rho_L, p_L, a_L, ps));
+    exact_sample(c, rho_L, u_L, p_L, a_L, rho_R, u_R, p_R, a_R, us, ps, S, o);
+    return DEV_OK;
+}
+
+/* Exact Godunov flux at x/t = S (src/riemann_solver_exact.c:471-510). */
+template <class R>
+HD int exact_flux_1d(const GasConst<R> &c, R rho_L, R u_L, R p_L, R rho_R, R u_R, R p_R, R S, R F[3])
+{
+    R s[3];
+    const int rc = exact_solve_1d(c, rho_L, u_L, p_L, rho_R, u_R, p_R, S, s);
+    F[0] = s[0] * s[1];
+    F[1] = s[0] * s[1] * s[1] + s[2];
+    F[2] = (s[2] * c.g_gm1 + R(0.5) * s[0] * s[1] * s[1]) * s[1];
+    return rc;
+}
+
+/* ------------------------------------------------------------- predictor */
+
+/*
+ * Hancock half-step predictor of one cell along one direction.  q = (rho, n,
+ * t, p) with n the velocity along the sweep; d = limited slopes of q;
+ * d_rho_vel is the slope entering the density row: the reference uses the
+ * slope of the x velocity in both sweeps (:688-693 and :988-993), so the
+ * y sweep passes the x-velocity slope here, not d[1].  The literal "+ 0.0"
+ * terms of the reference only turn -0.0 into +0.0 and are kept.
+ * lo = extrapolated state at the cell's low face, hi = at its high face.
+ */
+template <class R>
+HD void hancock_2d(R dtA, R dtA_rho, R rho, R n, R t, R p, R a,
+                   const R d[4], R d_rho_vel, R lo[4], R hi[4])
+{
+    const R up = R(1) + dtA * n;
+    const R um = R(1) - dtA * n;
+    const R dr = dtA * rho;
+    const R draa = dr * a * a * d[1];
+    lo[0] = rho + R(-0.5) * (up * d[0] + dr * d_rho_vel + R(0) + R(0));
+    lo[1] = n + R(-0.5) * (R(0) + up * d[1] + R(0) + dtA_rho * d[3]);
+    lo[2] = t + R(-0.5) * (R(0) + R(0) + up * d[2] + R(0));
+    lo[3] = p + R(-0.5) * (R(0) + draa + R(0) + up * d[3]);
+    hi[0] = rho + R(0.5) * (um * d[0] - dr * d_rho_vel + R(0) + R(0));
+    hi[1] = n + R(0.5) * (R(0) + um * d[1] + R(0) - dtA_rho * d[3]);
+    hi[2] = t + R(0.5) * (R(0) + R(0) + um * d[2] + R(0));
+    hi[3] = p + R(0.5) * (R(0) + R(0) - draa + um * d[3]);
+}
+
+/* 1D predictor (src/integrator_muscl_hancock.c:185-246). */
+template <class R>
+HD void hancock_1d(R dtA, R rho, R u, R p, R a, const R d[3], R lo[3], R hi[3])
+{
+    const R up = R(1) + dtA * u;
+    const R um = R(1) - dtA * u;
+    const R dr = dtA * rho;
+    const R drd = dtA / rho;
+    lo[0] = rho + R(-0.5) * (up * d[0] + dr * d[1] + R(0));
+    lo[1] = u + R(-0.5) * (R(0) + up * d[1] + drd * d[2]);
+    lo[2] = p + R(-0.5) * (R(0) + dr * a * a * d[1] + up * d[2]);
+    hi[0] = rho + R(0.5) * (um * d[0] - dr * d[1] + R(0));
+    hi[1] = u + R(0.5) * (R(0) + um * d[1] - drd * d[2]);
+    hi[2] = p + R(0.5) * (R(0) + -dtA * rho * a * a * d[1] + um * d[2]);
+}
+
+/* ------------------------------------------------------------ conversion */
+
+/* U (volume totals) -> W, 2D (src/system.c:763-802). */
+template <class R>
+HD void cons_to_prim_2d(const GasConst<R> &c, R vol, R m, R mx, R my, R E, R w[4])
+{
+    w[0] = m / vol;
+    w[1] = mx / m;
+    w[2] = my / m;
+    w[3] = c.gm1 * (E - R(0.5) * m * (w[1] * w[1] + w[2] * w[2])) / vol;
+}
+
+/* Ordered-bits encoding of a double, monotone for every non-NaN value, so a
+ * device-wide maximum is one unsigned 64-bit atomicMax. */
+HD unsigned long long ordered_bits(double x)
+{
+    unsigned long long b;
+    memcpy(&b, &x, sizeof b);
+    return (b >> 63) ? ~b : (b | 0x8000000000000000ull);
+}
+
+HD double from_ordered_bits(unsigned long long e)
+{
+    const unsigned long long b = (e >> 63) ? (e & 0x7fffffffffffffffull) : ~e;
+    double x;
+    memcpy(&x, &b, sizeof x);
+    return x;
+}
+
+}  // namespace hydro
+
+#endif

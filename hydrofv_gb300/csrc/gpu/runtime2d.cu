@@ -1,0 +1,487 @@
+/*
+ * runtime2d.cu -- device memory, streams, graphs and the host-side stepping
+ * loop for 2D grids (the part of src/integrator_muscl_hancock.c:385-1225
+ * that is not arithmetic).
+ *
+ * Memory: one device slab holds, per field, the padded grid with the same
+ * row-major layout as the host arrays (pitch = nx + 2G): U double-buffered
+ * (2 x 4 fields), W double-buffered (2 x 5 fields incl. sound speed), a
+ * 4-field materialization target for snapshots / download, and optionally
+ * a copy of the initial U and W for rewinding.  A 2048^2 FP64 run needs
+ * ~0.7 GB; an 8192^2 run ~12 GB.
+ *
+ * Stepping: all stepping state lives in a device HydroStepControl, so the
+ * host only enqueues step kernels.  With a fixed step count every step is
+ * enqueued up front (as CUDA-graph replays of a 32-step chunk) and the host
+ * waits once; when running to tf the host enqueues chunks sized from the
+ * last dt and polls the control block between them.  Steps enqueued past
+ * the stop are no-ops (the kernel returns after reading `active`).
+ */
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <climits>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+
+#include "gpu_bridge.h"
+#include "gpu_internal.h"
+
+using namespace hydro;
+
+namespace {
+
+constexpr int kGraphSteps = 32;
+
+void set_cuda_error(HydroRunOutcome *oc, cudaError_t e, const char *what)
+{
+    if (!oc) return;
+    oc->kind = HYDRO_RUN_CUDA_ERROR;
+    oc->code = (int) e;
+    snprintf(oc->message, sizeof oc->message, "CUDA error in %s: %s", what, cudaGetErrorString(e));
+}
+
+#define CK(call, what)                                  \
+    do {                                                \
+        cudaError_t e_ = (call);                        \
+        if (e_ != cudaSuccess) {                        \
+            set_cuda_error(oc, e_, what);               \
+            return -1;                                  \
+        }                                               \
+    } while (0)
+
+double now_ms()
+{
+    using namespace std::chrono;
+    return duration<double, std::milli>(steady_clock::now().time_since_epoch()).count();
+}
+
+}  // namespace
+
+struct HydroRun2D {
+    HydroGrid2D grid{};
+    HydroGpuOptions opt{};
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int tx = 0, ty = 0;
+    size_t ncell = 0;
+    double *slab = nullptr;
+    double *init_slab = nullptr;    /* initial U and W, kept for rewinding */
+    double *init_U[4] = {};
+    double *init_W[4] = {};
+    double *snap_d[4] = {};
+    double *snap_h = nullptr;       /* pinned, 4 * ncell */
+    HydroStepControl *ctrl_d = nullptr;
+    HydroStepControl *ctrl_h = nullptr;   /* pinned */
+    Mh2dArgs<double> args{};
+    cudaGraphExec_t graph = nullptr;
+    cudaEvent_t ev[6] = {};
+    bool begun = false;
+    bool have_initial = false;
+    /* statistics */
+    double h2d_ms = 0, step_ms = 0, d2h_ms = 0;
+    long long step_launches = 0, kernel_launches = 0;
+    long long h2d_bytes = 0, d2h_bytes = 0;
+};
+
+static void fill_outcome(const HydroRun2D *run, HydroRunOutcome *oc)
+{
+    oc->num_steps = run->ctrl_h->num_steps;
+    oc->t = run->ctrl_h->t;
+    oc->dt = run->ctrl_h->dt;
+    oc->store_count = run->ctrl_h->store_count;
+}
+
+extern "C" int hydro_run2d_create(const HydroGrid2D *grid, const HydroGpuOptions *opt,
+                                  HydroRun2D **out, HydroRunOutcome *oc)
+{
+    memset(oc, 0, sizeof *oc);
+    *out = nullptr;
+    if (grid->integrator != INTEGRATOR_MUSCL_HANCOCK_2D) {
+        oc->kind = HYDRO_RUN_UNSUPPORTED;
+        snprintf(oc->message, sizeof oc->message,
+                 "The GPU 2D path implements muscl_hancock_2d only.");
+        return -1;
+    }
+    if (grid->nx < grid->g || grid->ny < grid->g) {
+        oc->kind = HYDRO_RUN_UNSUPPORTED;
+        snprintf(oc->message, sizeof oc->message,
+                 "The GPU 2D path needs at least num_ghost_cells_side interior cells per "
+                 "direction (got %d x %d, G = %d).", grid->nx, grid->ny, grid->g);
+        return -1;
+    }
+    HydroRun2D *run = new (std::nothrow) HydroRun2D();
+    if (!run) {
+        oc->kind = HYDRO_RUN_CUDA_ERROR;
+        snprintf(oc->message, sizeof oc->message, "Host allocation failed.");
+        return -1;
+    }
+    run->grid = *grid;
+    run->opt = *opt;
+    run->device = opt->device;
+    run->tx = grid->nx + 2 * grid->g;
+    run->ty = grid->ny + 2 * grid->g;
+    run->ncell = (size_t) run->tx * (size_t) run->ty;
+    *out = run;
+
+    CK(cudaSetDevice(run->device), "cudaSetDevice");
+    CK(cudaStreamCreateWithFlags(&run->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+    for (auto &e : run->ev) CK(cudaEventCreate(&e), "cudaEventCreate");
+
+    /* 8 (U) + 10 (W) + 4 (snapshot) fields; the initial copy is separate */
+    const size_t nfield = 22;
+    CK(cudaMalloc(&run->slab, nfield * run->ncell * sizeof(double)), "cudaMalloc(state)");
+    double *p = run->slab;
+    Mh2dArgs<double> &a = run->args;
+    for (int b = 0; b < 2; b++)
+        for (int q = 0; q < 4; q++) { a.U[b][q] = p; p += run->ncell; }
+    for (int b = 0; b < 2; b++)
+        for (int q = 0; q < 5; q++) { a.W[b][q] = p; p += run->ncell; }
+    for (int q = 0; q < 4; q++) { run->snap_d[q] = p; p += run->ncell; }
+    CK(cudaMalloc(&run->ctrl_d, sizeof(HydroStepControl)), "cudaMalloc(control)");
+    CK(cudaMallocHost(&run->ctrl_h, sizeof(HydroStepControl)), "cudaMallocHost(control)");
+    memset(run->ctrl_h, 0, sizeof(HydroStepControl));
+
+    a.ctrl = run->ctrl_d;
+    a.gas = make_gas_const<double>(grid->gamma, grid->tol);
+    a.nx = grid->nx;
+    a.ny = grid->ny;
+    a.g = grid->g;
+    a.pitch = run->tx;
+    a.strip_w = MH2D_THREADS - 2;
+    a.chunk_h = opt->chunk_rows > 0 ? opt->chunk_rows : 64;
+    for (int s = 0; s < 4; s++) a.bc[s] = grid->bc[s];
+    a.dx = grid->dx;
+    a.dy = grid->dy;
+    a.area_x = grid->area_x;
+    a.area_y = grid->area_y;
+    a.vol = grid->vol;
+    return 0;
+}
+
+extern "C" int hydro_run2d_upload(HydroRun2D *run, double *const W[4], double *const U[4],
+                                  int keep_initial, HydroRunOutcome *oc)
+{
+    memset(oc, 0, sizeof *oc);
+    CK(cudaSetDevice(run->device), "cudaSetDevice");
+    const size_t bytes = run->ncell * sizeof(double);
+    Mh2dArgs<double> &a = run->args;
+    CK(cudaEventRecord(run->ev[0], run->stream), "cudaEventRecord");
+    for (int q = 0; q < 4; q++) {
+        CK(cudaMemcpyAsync(a.U[0][q], U[q], bytes, cudaMemcpyHostToDevice, run->stream), "H2D U");
+        CK(cudaMemcpyAsync(a.W[0][q], W[q], bytes, cudaMemcpyHostToDevice, run->stream), "H2D W");
+    }
+    for (int q = 0; q < 4; q++)
+        CK(cudaMemcpyAsync(a.U[1][q], a.U[0][q], bytes, cudaMemcpyDeviceToDevice, run->stream), "D2D U");
+    if (keep_initial) {
+        if (!run->init_slab) {
+            CK(cudaMalloc(&run->init_slab, 8 * bytes), "cudaMalloc(initial state)");
+            for (int q = 0; q < 4; q++) {
+                run->init_U[q] = run->init_slab + q * run->ncell;
+                run->init_W[q] = run->init_slab + (4 + q) * run->ncell;
+            }
+        }
+        for (int q = 0; q < 4; q++) {
+            CK(cudaMemcpyAsync(run->init_U[q], a.U[0][q], bytes, cudaMemcpyDeviceToDevice, run->stream), "D2D");
+            CK(cudaMemcpyAsync(run->init_W[q], a.W[0][q], bytes, cudaMemcpyDeviceToDevice, run->stream), "D2D");
+        }
+        run->have_initial = true;
+    }
+    CK(cudaEventRecord(run->ev[1], run->stream), "cudaEventRecord");
+    CK(cudaEventSynchronize(run->ev[1]), "upload");
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, run->ev[0], run->ev[1]), "cudaEventElapsedTime");
+    run->h2d_ms += ms;
+    run->h2d_bytes += (long long) (8 * bytes);
+    run->begun = false;
+    return 0;
+}
+
+extern "C" int hydro_run2d_restore(HydroRun2D *run, HydroRunOutcome *oc)
+{
+    memset(oc, 0, sizeof *oc);
+    if (!run->have_initial) {
+        oc->kind = HYDRO_RUN_UNSUPPORTED;
+        snprintf(oc->message, sizeof oc->message, "No initial state was kept on the device.");
+        return -1;
+    }
+    CK(cudaSetDevice(run->device), "cudaSetDevice");
+    const size_t bytes = run->ncell * sizeof(double);
+    Mh2dArgs<double> &a = run->args;
+    for (int q = 0; q < 4; q++) {
+        CK(cudaMemcpyAsync(a.U[0][q], run->init_U[q], bytes, cudaMemcpyDeviceToDevice, run->stream), "D2D");
+        CK(cudaMemcpyAsync(a.U[1][q], run->init_U[q], bytes, cudaMemcpyDeviceToDevice, run->stream), "D2D");
+        CK(cudaMemcpyAsync(a.W[0][q], run->init_W[q], bytes, cudaMemcpyDeviceToDevice, run->stream), "D2D");
+    }
+    CK(cudaStreamSynchronize(run->stream), "restore");
+    run->begun = false;
+    return 0;
+}
+
+static int push_control(HydroRun2D *run, HydroRunOutcome *oc)
+{
+    CK(cudaMemcpyAsync(run->ctrl_d, run->ctrl_h, sizeof(HydroStepControl), cudaMemcpyHostToDevice,
+                       run->stream), "H2D control");
+    return 0;
+}
+
+static int pull_control(HydroRun2D *run, HydroRunOutcome *oc)
+{
+    CK(cudaMemcpyAsync(run->ctrl_h, run->ctrl_d, sizeof(HydroStepControl), cudaMemcpyDeviceToHost,
+                       run->stream), "D2H control");
+    CK(cudaStreamSynchronize(run->stream), "step chunk");
+    return 0;
+}
+
+static int recompute_active(HydroStepControl *c)
+{
+    return (c->t < c->tf) && (c->max_steps < 0 || c->num_steps < c->max_steps) && !c->snapshot_due &&
+           c->error_code == 0;
+}
+
+extern "C" int hydro_run2d_begin(HydroRun2D *run, const HydroStepParams *sp, double tf,
+                                 int64 max_steps, int store_count, HydroRunOutcome *oc)
+{
+    memset(oc, 0, sizeof *oc);
+    CK(cudaSetDevice(run->device), "cudaSetDevice");
+    run->args.sp = *sp;
+    HydroStepControl *c = run->ctrl_h;
+    memset(c, 0, sizeof *c);
+    c->tf = tf;
+    c->max_steps = max_steps;
+    c->store_count = store_count;
+    const unsigned long long ninf = ordered_bits(-INFINITY);
+    for (int k = 0; k < 3; k++) c->smax[k][0] = c->smax[k][1] = ninf;
+    c->active = recompute_active(c);
+    if (push_control(run, oc)) return -1;
+    CK(mh2d_launch_prepare<double>(run->args, run->stream), "prepare kernel");
+    run->kernel_launches++;
+    CK(cudaStreamSynchronize(run->stream), "prepare");
+    /* The kernel arguments changed: any recorded graph is stale. */
+    if (run->graph) {
+        cudaGraphExecDestroy(run->graph);
+        run->graph = nullptr;
+    }
+    run->begun = true;
+    fill_outcome(run, oc);
+    return 0;
+}
+
+extern "C" int hydro_run2d_set_limits(HydroRun2D *run, double tf, int64 max_steps, HydroRunOutcome *oc)
+{
+    memset(oc, 0, sizeof *oc);
+    CK(cudaSetDevice(run->device), "cudaSetDevice");
+    if (pull_control(run, oc)) return -1;
+    HydroStepControl *c = run->ctrl_h;
+    c->tf = tf;
+    c->max_steps = max_steps;
+    c->active = recompute_active(c);
+    if (push_control(run, oc)) return -1;
+    CK(cudaStreamSynchronize(run->stream), "set limits");
+    fill_outcome(run, oc);
+    return 0;
+}
+
+extern "C" int hydro_run2d_status(HydroRun2D *run, HydroRunOutcome *oc)
+{
+    memset(oc, 0, sizeof *oc);
+    CK(cudaSetDevice(run->device), "cudaSetDevice");
+    if (pull_control(run, oc)) return -1;
+    fill_outcome(run, oc);
+    return 0;
+}
+
+static int record_graph(HydroRun2D *run, HydroRunOutcome *oc)
+{
+    cudaGraph_t g = nullptr;
+    CK(cudaStreamBeginCapture(run->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
+    cudaError_t le = cudaSuccess;
+    for (int k = 0; k < kGraphSteps && le == cudaSuccess; k++)
+        le = mh2d_launch_step<double>(run->args, run->grid.limiter, run->stream);
+    cudaError_t ce = cudaStreamEndCapture(run->stream, &g);
+    if (le != cudaSuccess) { set_cuda_error(oc, le, "step kernel (capture)"); if (g) cudaGraphDestroy(g); return -1; }
+    if (ce != cudaSuccess) { set_cuda_error(oc, ce, "end capture"); return -1; }
+    cudaError_t ie = cudaGraphInstantiate(&run->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (ie != cudaSuccess) { set_cuda_error(oc, ie, "graph instantiate"); return -1; }
+    return 0;
+}
+
+/* Enqueue `k` step kernels. */
+static int enqueue_steps(HydroRun2D *run, long long k, HydroRunOutcome *oc)
+{
+    const bool graphs = run->opt.use_graph && k >= kGraphSteps;
+    if (graphs && !run->graph && record_graph(run, oc)) return -1;
+    while (k > 0) {
+        if (graphs && k >= kGraphSteps) {
+            CK(cudaGraphLaunch(run->graph, run->stream), "graph launch");
+            k -= kGraphSteps;
+            run->step_launches += kGraphSteps;
+            run->kernel_launches += kGraphSteps;
+        } else {
+            CK(mh2d_launch_step<double>(run->args, run->grid.limiter, run->stream), "step kernel");
+            k -= 1;
+            run->step_launches += 1;
+            run->kernel_launches += 1;
+        }
+    }
+    return 0;
+}
+
+static int materialize_to_host(HydroRun2D *run, double *const W[4], HydroRunOutcome *oc)
+{
+    const int buf = (int) (run->ctrl_h->num_steps & 1);
+    CK(mh2d_launch_materialize<double>(run->args, buf, run->snap_d, run->stream), "materialize kernel");
+    run->kernel_launches++;
+    const size_t bytes = run->ncell * sizeof(double);
+    for (int q = 0; q < 4; q++)
+        CK(cudaMemcpyAsync(W[q], run->snap_d[q], bytes, cudaMemcpyDeviceToHost, run->stream), "D2H W");
+    return 0;
+}
+
+extern "C" int hydro_run2d_advance(HydroRun2D *run, HydroSnapshotFn snap, void *ctx,
+                                   HydroRunOutcome *oc, double *step_ms)
+{
+    memset(oc, 0, sizeof *oc);
+    CK(cudaSetDevice(run->device), "cudaSetDevice");
+    if (!run->begun) {
+        oc->kind = HYDRO_RUN_UNSUPPORTED;
+        snprintf(oc->message, sizeof oc->message, "Run not begun.");
+        return -1;
+    }
+    HydroStepControl *c = run->ctrl_h;
+    double elapsed = 0.0;
+    for (;;) {
+        if (!c->active) break;
+        /* How many steps to enqueue before looking at the control block. */
+        const long long remaining = (c->max_steps >= 0) ? c->max_steps - c->num_steps : LLONG_MAX;
+        const bool open_ended = !(c->tf < 1e290);   /* stopping by step count only */
+        long long k;
+        if (run->opt.chunk_steps > 0) {
+            k = run->opt.chunk_steps;
+        } else if (open_ended && !run->args.sp.is_storing && remaining != LLONG_MAX) {
+            k = remaining;
+        } else if (c->num_steps == 0 || !(c->dt > 0.0)) {
+            k = 16;
+        } else {
+            double horizon = c->tf - c->t;
+            if (run->args.sp.is_storing) {
+                const double next = run->args.sp.storing_interval *
+                                    (double) (c->store_count - run->args.sp.store_initial_offset + 1);
+                if (next - c->t < horizon) horizon = next - c->t;
+            }
+            double est = horizon / c->dt + 2.0;
+            if (!(est < 4096.0)) est = 4096.0;
+            k = (long long) est;
+        }
+        if (k > remaining) k = remaining;
+        if (k < 1) k = 1;
+        CK(cudaEventRecord(run->ev[2], run->stream), "cudaEventRecord");
+        if (enqueue_steps(run, k, oc)) return -1;
+        CK(cudaEventRecord(run->ev[3], run->stream), "cudaEventRecord");
+        if (pull_control(run, oc)) return -1;
+        float ms = 0;
+        CK(cudaEventElapsedTime(&ms, run->ev[2], run->ev[3]), "cudaEventElapsedTime");
+        elapsed += ms;
+        if (c->error_code) {
+            fill_outcome(run, oc);
+            oc->kind = HYDRO_RUN_DEVICE_ERROR;
+            oc->code = c->error_code;
+            oc->where = c->error_cell;
+            run->step_ms += elapsed;
+            if (step_ms) *step_ms = elapsed;
+            return -1;
+        }
+        if (c->snapshot_due) {
+            if (snap) {
+                if (!run->snap_h) {
+                    CK(cudaMallocHost(&run->snap_h, 4 * run->ncell * sizeof(double)), "cudaMallocHost(snapshot)");
+                }
+                double *Wh[4];
+                for (int q = 0; q < 4; q++) Wh[q] = run->snap_h + q * run->ncell;
+                if (materialize_to_host(run, Wh, oc)) return -1;
+                CK(cudaStreamSynchronize(run->stream), "snapshot");
+                const int rc = snap(ctx, Wh, c->num_steps, c->t, c->dt);
+                if (rc != 0) {
+                    fill_outcome(run, oc);
+                    oc->kind = HYDRO_RUN_CALLBACK_ERROR;
+                    oc->code = rc;
+                    run->step_ms += elapsed;
+                    if (step_ms) *step_ms = elapsed;
+                    return -1;
+                }
+            }
+            c->store_count += 1;
+            c->snapshot_due = 0;
+            c->active = recompute_active(c);
+            if (push_control(run, oc)) return -1;
+        }
+    }
+    run->step_ms += elapsed;
+    if (step_ms) *step_ms = elapsed;
+    fill_outcome(run, oc);
+    return 0;
+}
+
+extern "C" int hydro_run2d_download(HydroRun2D *run, double *const W[4], double *const U[4],
+                                    HydroRunOutcome *oc)
+{
+    memset(oc, 0, sizeof *oc);
+    CK(cudaSetDevice(run->device), "cudaSetDevice");
+    const int buf = (int) (run->ctrl_h->num_steps & 1);
+    const size_t bytes = run->ncell * sizeof(double);
+    CK(cudaEventRecord(run->ev[4], run->stream), "cudaEventRecord");
+    if (materialize_to_host(run, W, oc)) return -1;
+    for (int q = 0; q < 4; q++)
+        CK(cudaMemcpyAsync(U[q], run->args.U[buf][q], bytes, cudaMemcpyDeviceToHost, run->stream), "D2H U");
+    CK(cudaEventRecord(run->ev[5], run->stream), "cudaEventRecord");
+    CK(cudaEventSynchronize(run->ev[5]), "download");
+    float ms = 0;
+    CK(cudaEventElapsedTime(&ms, run->ev[4], run->ev[5]), "cudaEventElapsedTime");
+    run->d2h_ms += ms;
+    run->d2h_bytes += (long long) (8 * bytes);
+    fill_outcome(run, oc);
+    return 0;
+}
+
+extern "C" void hydro_run2d_stats(const HydroRun2D *run, HydroGpuStats *st)
+{
+    st->h2d_ms = run->h2d_ms;
+    st->step_ms = run->step_ms;
+    st->d2h_ms = run->d2h_ms;
+    st->steps = run->ctrl_h ? run->ctrl_h->num_steps : 0;
+    st->step_launches = run->step_launches;
+    st->kernel_launches = run->kernel_launches;
+    st->h2d_bytes = run->h2d_bytes;
+    st->d2h_bytes = run->d2h_bytes;
+    st->interior_cells = (int64) run->grid.nx * (int64) run->grid.ny;
+}
+
+extern "C" void hydro_run2d_destroy(HydroRun2D *run)
+{
+    if (!run) return;
+    cudaSetDevice(run->device);
+    if (run->stream) cudaStreamSynchronize(run->stream);
+    if (run->graph) cudaGraphExecDestroy(run->graph);
+    for (auto &e : run->ev)
+        if (e) cudaEventDestroy(e);
+    cudaFree(run->slab);
+    cudaFree(run->init_slab);
+    cudaFree(run->ctrl_d);
+    if (run->ctrl_h) cudaFreeHost(run->ctrl_h);
+    if (run->snap_h) cudaFreeHost(run->snap_h);
+    if (run->stream) cudaStreamDestroy(run->stream);
+    delete run;
+}
+
+extern "C" int hydro_gpu_device_count(void)
+{
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}

@@ -1,0 +1,513 @@
+/*
+ * integrate_gpu.c -- the integrators of the hydroFV API, running on the GPU.
+ *
+ * Each integrator keeps the reference's contract (src/integrator_*.c):
+ * validate the coordinate system, reset SimulationStatus, optionally store
+ * the initial snapshot, step while t < tf with the CFL dt (shrunk for the
+ * first steps) clipped to tf, store snapshots when
+ * t >= interval * (count - offset + 1), and leave the final W and U in the
+ * System's host arrays.  What changes is where the loop runs: the state is
+ * uploaded once, stepped in HBM, and copied back at the end (and for each
+ * snapshot, through pinned buffers).
+ *
+ * There is no CPU fallback: a CUDA failure is reported as an error.
+ */
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "gpu_bridge.h"
+#include "hydro.h"
+#include "hydro_gpu.h"
+#include "host_internal.h"
+#include "progress_bar.h"
+#include "source_term.h"
+
+/* ---------------------------------------------------------------- options */
+
+static int g_have_process_options = 0;
+static HydroGpuOptions g_process_options;
+
+HydroGpuOptions hydro_gpu_default_options(void)
+{
+    HydroGpuOptions o;
+    memset(&o, 0, sizeof o);
+    o.device = 0;
+    o.max_steps = -1;
+    o.precision = HYDRO_GPU_PRECISION_FP64;
+    o.chunk_steps = 0;
+    o.use_graph = 1;
+    o.block_threads = 0;
+    o.chunk_rows = 0;
+    return o;
+}
+
+void hydro_gpu_set_process_options(const HydroGpuOptions *options)
+{
+    if (options)
+    {
+        g_process_options = *options;
+        g_have_process_options = 1;
+    }
+    else
+    {
+        g_have_process_options = 0;
+    }
+}
+
+static HydroGpuOptions process_options(void)
+{
+    if (g_have_process_options) return g_process_options;
+    HydroGpuOptions o = hydro_gpu_default_options();
+    const char *dev = getenv("HYDRO_GPU_DEVICE");
+    if (dev && *dev) o.device = atoi(dev);
+    const char *ms = getenv("HYDRO_GPU_MAX_STEPS");
+    if (ms && *ms) o.max_steps = atoll(ms);
+    return o;
+}
+
+const char *hydro_gpu_version(void)
+{
+    return "hydrofv-gb300 0.1 (sm_103a)";
+}
+
+/* ------------------------------------------------------- error mapping */
+
+/* Turn a bridge outcome into the reference's ErrorStatus. */
+static ErrorStatus outcome_error(const HydroRunOutcome *oc)
+{
+    switch (oc->kind)
+    {
+        case HYDRO_RUN_DEVICE_ERROR:
+            return hydro_device_error_status(oc->code);
+        case HYDRO_RUN_UNSUPPORTED:
+            return WRAP_RAISE_ERROR(NOT_IMPLEMENTED_ERROR, oc->message);
+        case HYDRO_RUN_CALLBACK_ERROR:
+            return WRAP_RAISE_ERROR(OS_ERROR, "Storing a snapshot failed.");
+        case HYDRO_RUN_CUDA_ERROR:
+        default:
+            if (strstr(oc->message, "cudaMalloc") || strstr(oc->message, "out of memory"))
+                return WRAP_RAISE_ERROR(MEMORY_ERROR, oc->message);
+            return WRAP_RAISE_ERROR(FAILURE, oc->message);
+    }
+}
+
+/* -------------------------------------------------------- 2D set-up */
+
+static int uniform(const double *a, long long n)
+{
+    for (long long k = 1; k < n; k++)
+        if (a[k] != a[0]) return 0;
+    return 1;
+}
+
+/* Checks shared by the 2D integrators; fills grid. */
+static ErrorStatus setup_grid2d(const BoundaryConditionParam *bcp, const System *s,
+                                const IntegratorParam *ip, HydroGrid2D *grid)
+{
+    if (s->coord_sys_flag_ != COORD_SYS_CARTESIAN_2D)
+    {
+        char msg[256];
+        snprintf(msg, sizeof msg,
+                 "Wrong coordinate system. Supported coordinate system: \"cartesian_2d\", got: \"%s\"",
+                 s->coord_sys);
+        return WRAP_RAISE_ERROR(VALUE_ERROR, msg);
+    }
+    const int flags[4] = { bcp->boundary_condition_flag_x_min_, bcp->boundary_condition_flag_x_max_,
+                           bcp->boundary_condition_flag_y_min_, bcp->boundary_condition_flag_y_max_ };
+    for (int k = 0; k < 4; k++)
+    {
+        if (flags[k] == BOUNDARY_CONDITION_CUSTOM)
+            return WRAP_RAISE_ERROR(NOT_IMPLEMENTED_ERROR,
+                                    "Custom boundary conditions are not available on the GPU path.");
+        if (flags[k] < BOUNDARY_CONDITION_NONE || flags[k] > BOUNDARY_CONDITION_PERIODIC)
+            return WRAP_RAISE_ERROR(VALUE_ERROR, "Boundary condition flag not recognized.");
+        grid->bc[k] = flags[k];
+    }
+    if (s->gravity != 0.0)
+    {
+        return WRAP_RAISE_ERROR(NOT_IMPLEMENTED_ERROR,
+                                "A non-zero gravity source is not available on the GPU path.");
+    }
+    const int g = s->num_ghost_cells_side;
+    const long long tx = s->num_cells_x + 2 * g, ty = s->num_cells_y + 2 * g;
+    if (!uniform(s->surface_area_x_, tx) || !uniform(s->surface_area_y_, ty) || !uniform(s->volume_, tx * ty))
+    {
+        return WRAP_RAISE_ERROR(NOT_IMPLEMENTED_ERROR,
+                                "The GPU path needs uniform face areas and cell volumes (as system_init sets them).");
+    }
+    grid->nx = s->num_cells_x;
+    grid->ny = s->num_cells_y;
+    grid->g = g;
+    grid->gamma = s->gamma;
+    grid->tol = ip->tol;
+    grid->dx = s->dx_;
+    grid->dy = s->dy_;
+    grid->area_x = s->surface_area_x_[0];
+    grid->area_y = s->surface_area_y_[0];
+    grid->vol = s->volume_[0];
+    grid->limiter = ip->slope_limiter_flag_;
+    grid->integrator = ip->integrator_flag_;
+    return make_success_error_status();
+}
+
+typedef struct SnapCtx
+{
+    const BoundaryConditionParam *bcp;
+    const System *system;
+    const IntegratorParam *ip;
+    StoringParam *sp;
+    ErrorStatus status;
+} SnapCtx;
+
+/* Snapshot callback: a System view whose primitive arrays are the pinned
+ * buffers holding the materialized state. */
+static int snapshot_cb(void *vctx, double *const W[4], int64 num_steps, double t, double dt)
+{
+    SnapCtx *ctx = vctx;
+    System view = *ctx->system;
+    view.density_ = W[0];
+    view.velocity_x_ = W[1];
+    if (view.coord_sys_flag_ == COORD_SYS_CARTESIAN_2D)
+    {
+        view.velocity_y_ = W[2];
+        view.pressure_ = W[3];
+    }
+    else
+    {
+        view.pressure_ = W[2];
+    }
+    SimulationStatus st = { num_steps, t, dt };
+    ctx->status = WRAP_TRACEBACK(store_snapshot(ctx->bcp, &view, ctx->ip, &st, ctx->sp));
+    return ctx->status.return_code == SUCCESS ? 0 : 1;
+}
+
+static HydroStepParams step_params(const IntegratorParam *ip, const StoringParam *sp)
+{
+    HydroStepParams p;
+    memset(&p, 0, sizeof p);
+    p.cfl = ip->cfl;
+    p.cfl_shrunk = ip->cfl * ip->cfl_initial_shrink_factor;
+    p.shrink_steps = ip->cfl_initial_shrink_num_steps;
+    p.is_storing = sp->is_storing ? 1 : 0;
+    p.store_initial_offset = (sp->is_storing && sp->store_initial) ? 1 : 0;
+    p.storing_interval = sp->storing_interval;
+    return p;
+}
+
+static ErrorStatus run_2d(
+    BoundaryConditionParam *__restrict bcp,
+    System *__restrict s,
+    IntegratorParam *__restrict ip,
+    StoringParam *__restrict sp,
+    Settings *__restrict settings,
+    SimulationParam *__restrict simp,
+    SimulationStatus *__restrict status,
+    const HydroGpuOptions *opt,
+    HydroGpuStats *stats
+)
+{
+    const double t_start = hydro_get_current_time();
+    HydroGrid2D grid;
+    memset(&grid, 0, sizeof grid);
+    ErrorStatus e = setup_grid2d(bcp, s, ip, &grid);
+    if (e.return_code != SUCCESS) return e;
+    if (opt->precision != HYDRO_GPU_PRECISION_FP64)
+    {
+        return WRAP_RAISE_ERROR(NOT_IMPLEMENTED_ERROR, "Requested precision is not available for this integrator.");
+    }
+
+    status->num_steps = 0;
+    status->dt = 0.0;
+    status->t = 0.0;
+    sp->store_count_ = 0;
+    if (sp->is_storing && sp->store_initial)
+    {
+        e = WRAP_TRACEBACK(store_snapshot(bcp, s, ip, status, sp));
+        if (e.return_code != SUCCESS) return e;
+    }
+    ProgressBarParam bar;
+    if (!settings->no_progress_bar) start_progress_bar(&bar, simp->tf);
+
+    HydroRunOutcome oc;
+    HydroRun2D *run = NULL;
+    double *W[4] = { s->density_, s->velocity_x_, s->velocity_y_, s->pressure_ };
+    double *U[4] = { s->mass_, s->momentum_x_, s->momentum_y_, s->energy_ };
+    const HydroStepParams params = step_params(ip, sp);
+    SnapCtx ctx = { bcp, s, ip, sp, make_success_error_status() };
+
+    int rc = hydro_run2d_create(&grid, opt, &run, &oc);
+    if (rc == 0) rc = hydro_run2d_upload(run, W, U, 0, &oc);
+    if (rc == 0) rc = hydro_run2d_begin(run, &params, simp->tf, opt->max_steps, sp->store_count_, &oc);
+    int advanced = 0;
+    HydroRunOutcome aoc;
+    memset(&aoc, 0, sizeof aoc);
+    if (rc == 0)
+    {
+        advanced = 1;
+        rc = hydro_run2d_advance(run, snapshot_cb, &ctx, &aoc, NULL);
+        if (rc != 0) oc = aoc;
+    }
+    /* Whatever happened, hand back the last consistent state. */
+    if (advanced)
+    {
+        status->num_steps = aoc.num_steps;
+        status->t = aoc.t;
+        status->dt = aoc.dt;
+        sp->store_count_ = aoc.store_count;
+        if (aoc.num_steps > 0)
+        {
+            HydroRunOutcome doc;
+            if (hydro_run2d_download(run, W, U, &doc) != 0 && rc == 0)
+            {
+                rc = -1;
+                oc = doc;
+            }
+        }
+    }
+    if (stats && run) hydro_run2d_stats(run, stats);
+    hydro_run2d_destroy(run);
+    if (!settings->no_progress_bar) update_progress_bar(&bar, status->t, true);
+    if (stats) stats->total_ms = (hydro_get_current_time() - t_start) * 1e3;
+
+    if (rc != 0)
+    {
+        if (oc.kind == HYDRO_RUN_CALLBACK_ERROR && ctx.status.return_code != SUCCESS) return ctx.status;
+        free_traceback(&ctx.status);
+        return outcome_error(&oc);
+    }
+    return make_success_error_status();
+}
+
+/* --------------------------------------------------------- integrators */
+
+ErrorStatus muscl_hancock_2d(
+    BoundaryConditionParam *__restrict bcp,
+    System *__restrict system,
+    IntegratorParam *__restrict ip,
+    StoringParam *__restrict sp,
+    Settings *__restrict settings,
+    SimulationParam *__restrict simp,
+    SimulationStatus *__restrict status
+)
+{
+    const HydroGpuOptions opt = process_options();
+    return run_2d(bcp, system, ip, sp, settings, simp, status, &opt, NULL);
+}
+
+ErrorStatus godunov_first_order_2d(
+    BoundaryConditionParam *__restrict bcp,
+    System *__restrict system,
+    IntegratorParam *__restrict ip,
+    StoringParam *__restrict sp,
+    Settings *__restrict settings,
+    SimulationParam *__restrict simp,
+    SimulationStatus *__restrict status
+)
+{
+    const HydroGpuOptions opt = process_options();
+    return run_2d(bcp, system, ip, sp, settings, simp, status, &opt, NULL);
+}
+
+ErrorStatus godunov_first_order_1d(
+    BoundaryConditionParam *__restrict bcp,
+    System *__restrict system,
+    IntegratorParam *__restrict ip,
+    StoringParam *__restrict sp,
+    Settings *__restrict settings,
+    SimulationParam *__restrict simp,
+    SimulationStatus *__restrict status
+)
+{
+    (void) bcp; (void) system; (void) ip; (void) sp; (void) settings; (void) simp; (void) status;
+    return WRAP_RAISE_ERROR(NOT_IMPLEMENTED_ERROR, "godunov_first_order_1d is not available yet.");
+}
+
+ErrorStatus muscl_hancock_1d(
+    BoundaryConditionParam *__restrict bcp,
+    System *__restrict system,
+    IntegratorParam *__restrict ip,
+    StoringParam *__restrict sp,
+    Settings *__restrict settings,
+    SimulationParam *__restrict simp,
+    SimulationStatus *__restrict status
+)
+{
+    (void) bcp; (void) system; (void) ip; (void) sp; (void) settings; (void) simp; (void) status;
+    return WRAP_RAISE_ERROR(NOT_IMPLEMENTED_ERROR, "muscl_hancock_1d is not available yet.");
+}
+
+ErrorStatus random_choice_1d(
+    BoundaryConditionParam *__restrict bcp,
+    System *__restrict system,
+    IntegratorParam *__restrict ip,
+    StoringParam *__restrict sp,
+    Settings *__restrict settings,
+    SimulationParam *__restrict simp,
+    SimulationStatus *__restrict status
+)
+{
+    (void) bcp; (void) system; (void) ip; (void) sp; (void) settings; (void) simp; (void) status;
+    return WRAP_RAISE_ERROR(NOT_IMPLEMENTED_ERROR,
+                            "random_choice_1d is not part of the GPU library (use godunov_first_order_1d).");
+}
+
+/* ------------------------------------------------------- extension API */
+
+ErrorStatus hydro_gpu_launch_simulation(
+    BoundaryConditionParam *__restrict bcp,
+    System *__restrict system,
+    IntegratorParam *__restrict ip,
+    StoringParam *__restrict sp,
+    Settings *__restrict settings,
+    SimulationParam *__restrict simp,
+    SimulationStatus *__restrict status,
+    const HydroGpuOptions *options,
+    HydroGpuStats *stats
+)
+{
+    if (stats) memset(stats, 0, sizeof *stats);
+    const HydroGpuOptions opt = options ? *options : hydro_gpu_default_options();
+    /* The same finalize / check sequence as launch_simulation (src/hydro.c:29-91). */
+    ErrorStatus e = WRAP_TRACEBACK(finalize_boundary_condition_param(system, bcp));
+    if (e.return_code != SUCCESS) return e;
+    e = WRAP_TRACEBACK(finalize_integrator_param(ip));
+    if (e.return_code != SUCCESS) return e;
+    e = WRAP_TRACEBACK(finalize_storing_param(sp));
+    if (e.return_code != SUCCESS) return e;
+    e = WRAP_TRACEBACK(hydro_final_check(system, ip));
+    if (e.return_code != SUCCESS) return e;
+    switch (ip->integrator_flag_)
+    {
+        case INTEGRATOR_MUSCL_HANCOCK_2D:
+        case INTEGRATOR_GODUNOV_FIRST_ORDER_2D:
+            return WRAP_TRACEBACK(run_2d(bcp, system, ip, sp, settings, simp, status, &opt, stats));
+        default:
+        {
+            const int had = g_have_process_options;
+            const HydroGpuOptions saved = g_process_options;
+            hydro_gpu_set_process_options(&opt);
+            e = WRAP_TRACEBACK(integrator_launch_simulation(bcp, system, ip, sp, settings, simp, status));
+            g_process_options = saved;
+            g_have_process_options = had;
+            return e;
+        }
+    }
+}
+
+/* ------------------------------------------------------------ session */
+
+struct HydroGpuSolver
+{
+    HydroRun2D *run;
+    HydroGrid2D grid;
+    HydroStepParams params;
+    int begun;
+    int64 launches_at_create;
+};
+
+ErrorStatus hydro_gpu_solver_create(
+    HydroGpuSolver **out,
+    BoundaryConditionParam *__restrict bcp,
+    System *__restrict system,
+    IntegratorParam *__restrict ip,
+    const HydroGpuOptions *options
+)
+{
+    *out = NULL;
+    ErrorStatus e = WRAP_TRACEBACK(finalize_boundary_condition_param(system, bcp));
+    if (e.return_code != SUCCESS) return e;
+    e = WRAP_TRACEBACK(finalize_integrator_param(ip));
+    if (e.return_code != SUCCESS) return e;
+    if (ip->integrator_flag_ != INTEGRATOR_MUSCL_HANCOCK_2D)
+        return WRAP_RAISE_ERROR(NOT_IMPLEMENTED_ERROR, "The solver session supports muscl_hancock_2d.");
+    if (system->num_ghost_cells_side < 2)
+        return WRAP_RAISE_ERROR(VALUE_ERROR, "Number of ghost cells must be at least 2.");
+    HydroGpuSolver *sv = calloc(1, sizeof *sv);
+    if (!sv) return WRAP_RAISE_ERROR(MEMORY_ERROR, "Failed to allocate the solver.");
+    e = setup_grid2d(bcp, system, ip, &sv->grid);
+    if (e.return_code != SUCCESS)
+    {
+        free(sv);
+        return e;
+    }
+    const HydroGpuOptions opt = options ? *options : hydro_gpu_default_options();
+    StoringParam none = get_new_storing_param();
+    sv->params = step_params(ip, &none);
+    HydroRunOutcome oc;
+    double *W[4] = { system->density_, system->velocity_x_, system->velocity_y_, system->pressure_ };
+    double *U[4] = { system->mass_, system->momentum_x_, system->momentum_y_, system->energy_ };
+    int rc = hydro_run2d_create(&sv->grid, &opt, &sv->run, &oc);
+    if (rc == 0) rc = hydro_run2d_upload(sv->run, W, U, 1, &oc);
+    if (rc != 0)
+    {
+        hydro_run2d_destroy(sv->run);
+        free(sv);
+        return outcome_error(&oc);
+    }
+    *out = sv;
+    return make_success_error_status();
+}
+
+ErrorStatus hydro_gpu_solver_restart(HydroGpuSolver *sv)
+{
+    HydroRunOutcome oc;
+    if (hydro_run2d_restore(sv->run, &oc) != 0) return outcome_error(&oc);
+    sv->begun = 0;
+    return make_success_error_status();
+}
+
+ErrorStatus hydro_gpu_solver_advance(
+    HydroGpuSolver *sv,
+    int64 num_steps,
+    double tf,
+    SimulationStatus *__restrict status,
+    double *step_ms
+)
+{
+    HydroRunOutcome oc;
+    if (!sv->begun)
+    {
+        if (hydro_run2d_begin(sv->run, &sv->params, tf, num_steps, 0, &oc) != 0) return outcome_error(&oc);
+        sv->begun = 1;
+    }
+    else
+    {
+        if (hydro_run2d_status(sv->run, &oc) != 0) return outcome_error(&oc);
+        if (hydro_run2d_set_limits(sv->run, tf, oc.num_steps + num_steps, &oc) != 0) return outcome_error(&oc);
+    }
+    const int rc = hydro_run2d_advance(sv->run, NULL, NULL, &oc, step_ms);
+    if (status)
+    {
+        status->num_steps = oc.num_steps;
+        status->t = oc.t;
+        status->dt = oc.dt;
+    }
+    if (rc != 0) return outcome_error(&oc);
+    return make_success_error_status();
+}
+
+ErrorStatus hydro_gpu_solver_download(HydroGpuSolver *sv, System *__restrict system)
+{
+    HydroRunOutcome oc;
+    double *W[4] = { system->density_, system->velocity_x_, system->velocity_y_, system->pressure_ };
+    double *U[4] = { system->mass_, system->momentum_x_, system->momentum_y_, system->energy_ };
+    if (hydro_run2d_download(sv->run, W, U, &oc) != 0) return outcome_error(&oc);
+    return make_success_error_status();
+}
+
+int64 hydro_gpu_solver_kernel_launches(const HydroGpuSolver *sv)
+{
+    HydroGpuStats st;
+    memset(&st, 0, sizeof st);
+    hydro_run2d_stats(sv->run, &st);
+    return st.kernel_launches;
+}
+
+void hydro_gpu_solver_destroy(HydroGpuSolver *sv)
+{
+    if (!sv) return;
+    hydro_run2d_destroy(sv->run);
+    free(sv);
+}

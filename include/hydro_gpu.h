@@ -1,0 +1,130 @@
+/*
+ * hydro_gpu.h -- GB300 extensions to the hydroFV-compatible C API.
+ *
+ * Everything in hydro.h keeps the reference's semantics; launch_simulation
+ * itself runs on the GPU.  This header adds what the reference has no way to
+ * express:
+ *
+ *   - HydroGpuOptions: device, fixed step count, precision, chunking;
+ *   - hydro_gpu_launch_simulation: launch_simulation with options and
+ *     device-timed statistics (H2D / stepping / D2H, bytes moved, launches);
+ *   - HydroGpuSolver: a device-resident session (upload once, step many
+ *     times, download when asked) for benchmarks and drivers that keep the
+ *     state in HBM between calls.
+ *
+ * No struct declared in hydro.h changes layout.  All functions are C ABI,
+ * take plain pointers and sizes, and return ErrorStatus like the rest of
+ * the API.
+ */
+#ifndef HYDRO_GPU_H
+#define HYDRO_GPU_H
+
+#include "hydro.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Arithmetic of the 2D step. */
+#define HYDRO_GPU_PRECISION_FP64 0   /* the drop-in: matches the reference */
+#define HYDRO_GPU_PRECISION_FP32 1   /* FP32 state/flux, FP64 where needed */
+
+typedef struct HydroGpuOptions
+{
+    int device;             /* CUDA device ordinal (default 0) */
+    int64 max_steps;        /* stop after this many steps; < 0: run to tf only */
+    int precision;          /* HYDRO_GPU_PRECISION_* (default FP64) */
+    int chunk_steps;        /* steps enqueued between host polls (0: auto) */
+    int use_graph;          /* replay step chunks as CUDA graphs (default 1) */
+    int block_threads;      /* threads per step CTA (0: tuned default) */
+    int chunk_rows;         /* grid rows per step CTA (0: tuned default) */
+} HydroGpuOptions;
+
+typedef struct HydroGpuStats
+{
+    double total_ms;        /* host wall clock of the whole call */
+    double h2d_ms;          /* CUDA-event time of host -> device staging */
+    double step_ms;         /* CUDA-event time of the stepping phase */
+    double d2h_ms;          /* CUDA-event time of the final device -> host copies */
+    int64 steps;            /* completed time steps */
+    int64 step_launches;    /* step kernels launched (no-op tail launches included) */
+    int64 kernel_launches;  /* every kernel of this library launched by the call */
+    int64 h2d_bytes;
+    int64 d2h_bytes;
+    int64 interior_cells;   /* cells updated per step */
+} HydroGpuStats;
+
+/* Defaults: device 0, no step limit, FP64, auto chunking, graphs on. */
+HydroGpuOptions hydro_gpu_default_options(void);
+
+/* Options used by plain launch_simulation() in this process.  Lets programs
+ * written for hydroFV pick a device or a step limit without code changes
+ * (the environment variables HYDRO_GPU_DEVICE and HYDRO_GPU_MAX_STEPS are
+ * read when this has not been called).  Not thread-safe against concurrent
+ * calls of itself. */
+void hydro_gpu_set_process_options(const HydroGpuOptions *options);
+
+/* launch_simulation with explicit options; `stats` may be NULL. */
+ErrorStatus hydro_gpu_launch_simulation(
+    BoundaryConditionParam *__restrict boundary_condition_param,
+    System *__restrict system,
+    IntegratorParam *__restrict integrator_param,
+    StoringParam *__restrict storing_param,
+    Settings *__restrict settings,
+    SimulationParam *__restrict simulation_param,
+    SimulationStatus *__restrict simulation_status,
+    const HydroGpuOptions *options,
+    HydroGpuStats *stats
+);
+
+/* ------------------------------------------------------------------ */
+/* Device-resident session (2D Cartesian MUSCL-Hancock / Godunov).     */
+/* ------------------------------------------------------------------ */
+
+typedef struct HydroGpuSolver HydroGpuSolver;
+
+/* Finalize the parameters, allocate device memory and upload the System's
+ * W and U arrays.  The initial state is also kept on the device so
+ * hydro_gpu_solver_restart can rewind without host traffic. */
+ErrorStatus hydro_gpu_solver_create(
+    HydroGpuSolver **solver,
+    BoundaryConditionParam *__restrict boundary_condition_param,
+    System *__restrict system,
+    IntegratorParam *__restrict integrator_param,
+    const HydroGpuOptions *options
+);
+
+/* Rewind to the uploaded initial state (t = 0, no steps taken). */
+ErrorStatus hydro_gpu_solver_restart(HydroGpuSolver *solver);
+
+/* Advance by up to `num_steps` steps, stopping early at tf.  `status`
+ * receives num_steps / t / dt since the last restart; `step_ms` (may be
+ * NULL) the CUDA-event time of this call's stepping. */
+ErrorStatus hydro_gpu_solver_advance(
+    HydroGpuSolver *solver,
+    int64 num_steps,
+    double tf,
+    SimulationStatus *__restrict status,
+    double *step_ms
+);
+
+/* Copy the current state (W with ghost cells filled, and U) into the
+ * System's host arrays. */
+ErrorStatus hydro_gpu_solver_download(HydroGpuSolver *solver, System *__restrict system);
+
+/* Kernels launched by this solver so far. */
+int64 hydro_gpu_solver_kernel_launches(const HydroGpuSolver *solver);
+
+void hydro_gpu_solver_destroy(HydroGpuSolver *solver);
+
+/* Number of visible CUDA devices (0 when none; never fails). */
+int hydro_gpu_device_count(void);
+
+/* Library version string. */
+const char *hydro_gpu_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif
