@@ -145,6 +145,7 @@ _SIGNATURES = {
     "hydro_gpu_solver_kernel_launches": (C.c_int64, [C.c_void_p]),
     "hydro_gpu_solver_destroy": (None, [C.c_void_p]),
     "hydro_gpu_device_count": (C.c_int, []),
+    "hydro_gpu_calibrate": (C.c_int, [C.c_int, _dp, _dp]),
     "hydro_gpu_version": (C.c_char_p, []),
     "free_traceback": (None, [_P(ErrorStatus)]),
     "solve_flux_hllc_2d": (ErrorStatus, [_dp] * 4 + [C.c_double] * 10),
@@ -194,6 +195,14 @@ def _consume(lib: C.CDLL, e: ErrorStatus) -> tuple[int, str]:
 
 def device_count() -> int:
     return int(library().hydro_gpu_device_count())
+
+
+def calibrate(device: int = 0) -> tuple[float, float]:
+    """Measured (FP64, FP32) FMA throughput in TFLOP/s."""
+    f64, f32 = C.c_double(0), C.c_double(0)
+    if library().hydro_gpu_calibrate(device, C.byref(f64), C.byref(f32)) != 0:
+        raise HydroError(1, "calibration kernel failed")
+    return f64.value, f32.value
 
 
 def default_options(**kw) -> HydroGpuOptions:

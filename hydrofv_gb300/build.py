@@ -32,6 +32,7 @@ CUDA_SOURCES = [
     ("gpu/mh2d.cu", ["--fmad=false"]),
     ("gpu/runtime2d.cu", []),
     ("gpu/host_numerics.cu", ["--fmad=false"]),
+    ("gpu/calibrate.cu", []),
 ]
 C_SOURCES = [
     "host/error.c",

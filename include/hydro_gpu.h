@@ -117,6 +117,11 @@ int64 hydro_gpu_solver_kernel_launches(const HydroGpuSolver *solver);
 
 void hydro_gpu_solver_destroy(HydroGpuSolver *solver);
 
+/* Measure the device's FMA throughput (TFLOP/s, 1 FMA = 2 FLOP) in FP64 and
+ * FP32 with a short calibration kernel; either pointer may be NULL.  Used
+ * for roofline reporting.  Returns 0 on success. */
+int hydro_gpu_calibrate(int device, double *fp64_tflops, double *fp32_tflops);
+
 /* Number of visible CUDA devices (0 when none; never fails). */
 int hydro_gpu_device_count(void);
 

@@ -15,14 +15,16 @@ initial-condition generators used by the parity tests and the benchmark.
 from __future__ import annotations
 
 import ctypes as C
-import math
 import os
+import sys
 import subprocess
 from dataclasses import dataclass, field
 
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
+if os.path.dirname(HERE) not in sys.path:
+    sys.path.insert(0, os.path.dirname(HERE))
 BUILD = os.path.join(HERE, "_build")
 REFDIR = os.path.join(HERE, "_ref")
 
@@ -86,70 +88,6 @@ def load(kind: str = "oracle") -> "Backend":
 
 def reference_available() -> bool:
     return os.path.exists(os.path.join(REFDIR, "libhydro_ref_omp.so"))
-
-
-@dataclass
-class Problem2D:
-    """A 2D Cartesian problem in the reference's padded layout."""
-    nx: int
-    ny: int
-    g: int
-    x_min: float
-    x_max: float
-    y_min: float
-    y_max: float
-    gamma: float
-    W: np.ndarray              # (4, ny+2g, nx+2g): rho, u, v, p
-    U: np.ndarray              # (4, ny+2g, nx+2g): mass, mom_x, mom_y, energy
-    bc: tuple = ("periodic",) * 4
-    integrator: str = "muscl_hancock_2d"
-    riemann_solver: str = "riemann_solver_hllc"
-    slope_limiter: str = "monotonized_central"
-    cfl: float = 0.8
-    tf: float = 1.0
-    max_steps: int = -1
-    name: str = ""
-
-    def copy(self) -> "Problem2D":
-        import copy
-        p = copy.copy(self)
-        p.W = self.W.copy()
-        p.U = self.U.copy()
-        return p
-
-    @property
-    def dx(self) -> float:
-        return (self.x_max - self.x_min) / (self.nx + 2 * self.g)
-
-    @property
-    def dy(self) -> float:
-        return (self.y_max - self.y_min) / (self.ny + 2 * self.g)
-
-
-@dataclass
-class Problem1D:
-    nx: int
-    g: int
-    x_min: float
-    x_max: float
-    gamma: float
-    W: np.ndarray              # (3, nx+2g): rho, u, p
-    U: np.ndarray              # (3, nx+2g): mass, mom, energy
-    bc: tuple = ("transmissive", "transmissive")
-    integrator: str = "godunov_first_order_1d"
-    riemann_solver: str = "riemann_solver_exact"
-    slope_limiter: str = "minmod"
-    cfl: float = 0.9
-    tf: float = 0.2
-    max_steps: int = -1
-    name: str = ""
-
-    def copy(self) -> "Problem1D":
-        import copy
-        p = copy.copy(self)
-        p.W = self.W.copy()
-        p.U = self.U.copy()
-        return p
 
 
 @dataclass
@@ -232,206 +170,13 @@ class Backend:
         return rc, out.value
 
 
-# --------------------------------------------------------------------------
-# Seeded initial conditions (one documented PRNG: numpy PCG64 via
-# np.random.default_rng(seed)).  Geometry follows the reference: dx includes
-# the ghost cells (src/system.c:291-309), mid points are x_min + (i+1/2) dx
-# over the padded range (:318-356).
-# --------------------------------------------------------------------------
-
-def primitive_to_conserved_2d(W: np.ndarray, gamma: float, vol: float) -> np.ndarray:
-    """src/system.c:885-905, element-wise in numpy (same IEEE operation order)."""
-    rho, u, v, p = W
-    m = rho * vol
-    U = np.empty_like(W)
-    U[0] = m
-    U[1] = m * u
-    U[2] = m * v
-    U[3] = vol * (0.5 * rho * (u * u + v * v) + p / (gamma - 1.0))
-    return U
-
-
-def primitive_to_conserved_1d(W: np.ndarray, gamma: float, vol: float) -> np.ndarray:
-    """src/system.c:868-882."""
-    rho, u, p = W
-    U = np.empty_like(W)
-    U[0] = rho * vol
-    U[1] = U[0] * u
-    U[2] = vol * (0.5 * rho * u * u + p / (gamma - 1.0))
-    return U
-
-
-def apply_bc_2d(W: np.ndarray, g: int, nx: int, ny: int, bc) -> None:
-    """Built-in ghost fill on W in place (src/boundary.c:513-777)."""
-    flags = list(bc)
-    for side in (0, 1):
-        f = flags[side]
-        if f == "none" or (f == "periodic" and side == 0):
-            continue
-        for k in range(g):
-            rows = slice(g, g + ny)
-            if f == "periodic":
-                W[:, rows, g + nx + k] = W[:, rows, g + k]
-                W[:, rows, g - 1 - k] = W[:, rows, g + nx - 1 - k]
-                continue
-            dst, src = (g - 1 - k, g + k) if side == 0 else (g + nx + k, g + nx - 1 - k)
-            W[:, rows, dst] = W[:, rows, src]
-            if f == "reflective":
-                W[1, rows, dst] = -W[1, rows, src]
-    for side in (0, 1):
-        f = flags[2 + side]
-        if f == "none" or (f == "periodic" and side == 0):
-            continue
-        cols = slice(g, g + nx)
-        for k in range(g):
-            if f == "periodic":
-                W[:, g + ny + k, cols] = W[:, g + k, cols]
-                W[:, g - 1 - k, cols] = W[:, g + ny - 1 - k, cols]
-                continue
-            dst, src = (g - 1 - k, g + k) if side == 0 else (g + ny + k, g + ny - 1 - k)
-            W[:, dst, cols] = W[:, src, cols]
-            if f == "reflective":
-                W[2, dst, cols] = -W[2, src, cols]
-
-
-def mid_points(lo: float, hi: float, n: int, g: int) -> np.ndarray:
-    d = (hi - lo) / (n + 2 * g)
-    return lo + (np.arange(n + 2 * g) + 0.5) * d
-
-
-def shear_layer(n: int, g: int = 2, seed: int = 2024, steps: int = 200,
-                limiter: str = "monotonized_central") -> Problem2D:
-    """Shear layer on [0,1]^2, periodic, gamma=5/3: rho=2, vx=+0.5 for
-    |y-0.5|<0.25 else rho=1, vx=-0.5; p=2.5; vy=0.01 sin(4 pi x); seeded
-    uniform noise U[-1e-3, 1e-3] on vx then vy (row-major over the interior).
-    MUSCL-Hancock + HLLC + MC, CFL 0.8, fixed step count."""
-    gamma = 5.0 / 3.0
-    N = n + 2 * g
-    x = mid_points(0.0, 1.0, n, g)
-    y = mid_points(0.0, 1.0, n, g)
-    X, Y = np.meshgrid(x, y)
-    W = np.zeros((4, N, N))
-    inner = np.abs(Y - 0.5) < 0.25
-    rho = np.where(inner, 2.0, 1.0)
-    vx = np.where(inner, 0.5, -0.5)
-    vy = 0.01 * np.sin(4.0 * math.pi * X)
-    rng = np.random.default_rng(seed)
-    noise_x = rng.uniform(-1e-3, 1e-3, size=(n, n))
-    noise_y = rng.uniform(-1e-3, 1e-3, size=(n, n))
-    I = (slice(g, g + n), slice(g, g + n))
-    W[0][I] = rho[I]
-    W[1][I] = vx[I] + noise_x
-    W[2][I] = vy[I] + noise_y
-    W[3][I] = 2.5
-    bc = ("periodic",) * 4
-    apply_bc_2d(W, g, n, n, bc)
-    dx = 1.0 / N
-    U = primitive_to_conserved_2d(W, gamma, dx * dx)
-    return Problem2D(n, n, g, 0.0, 1.0, 0.0, 1.0, gamma, W, U, bc,
-                     "muscl_hancock_2d", "riemann_solver_hllc", limiter,
-                     cfl=0.8, tf=1e300, max_steps=steps, name=f"shear_layer_{n}")
-
-
-def point_blast(n: int, g: int = 2, steps: int = 1000) -> Problem2D:
-    """Point blast on [-1,1]^2, reflective, gamma=1.4, rho=1, u=v=0, background
-    p=1e-5; total energy 1.0 shared equally by the cells with r < 2 dx and
-    added as pressure p = (gamma-1) E_c / V.  Van Leer, CFL 0.4."""
-    gamma = 1.4
-    N = n + 2 * g
-    x = mid_points(-1.0, 1.0, n, g)
-    X, Y = np.meshgrid(x, x)
-    dx = 2.0 / N
-    vol = dx * dx
-    W = np.zeros((4, N, N))
-    I = (slice(g, g + n), slice(g, g + n))
-    W[0][I] = 1.0
-    W[3][I] = 1e-5
-    r = np.sqrt(X * X + Y * Y)
-    hot = np.zeros((N, N), dtype=bool)
-    hot[I] = (r < 2.0 * dx)[I]
-    count = int(hot.sum())
-    E_c = 1.0 / count
-    W[3][hot] += (gamma - 1.0) * E_c / vol
-    bc = ("reflective",) * 4
-    apply_bc_2d(W, g, n, n, bc)
-    U = primitive_to_conserved_2d(W, gamma, vol)
-    return Problem2D(n, n, g, -1.0, 1.0, -1.0, 1.0, gamma, W, U, bc,
-                     "muscl_hancock_2d", "riemann_solver_hllc", "van_leer",
-                     cfl=0.4, tf=1e300, max_steps=steps, name=f"point_blast_{n}")
-
-
-def four_quadrant(n: int, rng: np.random.Generator, g: int = 2, steps: int = 500,
-                  limiter: str = "minmod") -> Problem2D:
-    """Four-quadrant Riemann problem on [0,1]^2, transmissive, gamma=1.4:
-    quadrant states rho,p ~ U[0.1,2], u,v ~ U[-1,1], split at x=y=0.5."""
-    gamma = 1.4
-    N = n + 2 * g
-    x = mid_points(0.0, 1.0, n, g)
-    X, Y = np.meshgrid(x, x)
-    q = rng.uniform(size=(4, 4))
-    states = np.stack([0.1 + 1.9 * q[:, 0], -1.0 + 2.0 * q[:, 1],
-                       -1.0 + 2.0 * q[:, 2], 0.1 + 1.9 * q[:, 3]], axis=1)
-    quad = (X >= 0.5).astype(int) + 2 * (Y >= 0.5).astype(int)
-    W = np.zeros((4, N, N))
-    I = (slice(g, g + n), slice(g, g + n))
-    for k in range(4):
-        W[k][I] = states[quad, k][I]
-    bc = ("transmissive",) * 4
-    apply_bc_2d(W, g, n, n, bc)
-    dx = 1.0 / N
-    U = primitive_to_conserved_2d(W, gamma, dx * dx)
-    return Problem2D(n, n, g, 0.0, 1.0, 0.0, 1.0, gamma, W, U, bc,
-                     "muscl_hancock_2d", "riemann_solver_hllc", limiter,
-                     cfl=0.8, tf=1e300, max_steps=steps, name=f"four_quadrant_{n}")
-
-
-def random_problem_2d(nx: int, ny: int, seed: int, bc, limiter: str, steps: int,
-                      g: int = 2, integrator: str = "muscl_hancock_2d",
-                      smooth: bool = False) -> Problem2D:
-    """Random smooth-ish or blocky states for edge-case parity tests."""
-    rng = np.random.default_rng(seed)
-    gamma = float(rng.choice([1.4, 5.0 / 3.0, 1.2]))
-    N = (ny + 2 * g, nx + 2 * g)
-    W = np.zeros((4,) + N)
-    if smooth:
-        x = mid_points(0.0, 1.0, nx, g)
-        y = mid_points(0.0, 1.0, ny, g)
-        X, Y = np.meshgrid(x, y)
-        W[0] = 1.0 + 0.3 * np.sin(2 * math.pi * X) * np.cos(2 * math.pi * Y)
-        W[1] = 0.3 * np.cos(2 * math.pi * Y)
-        W[2] = 0.2 * np.sin(2 * math.pi * X)
-        W[3] = 1.0 + 0.2 * np.cos(2 * math.pi * (X + Y))
-        W += rng.uniform(-1e-3, 1e-3, size=W.shape)
-    else:
-        W[0] = rng.uniform(0.2, 2.0, size=N)
-        W[1] = rng.uniform(-1.0, 1.0, size=N)
-        W[2] = rng.uniform(-1.0, 1.0, size=N)
-        W[3] = rng.uniform(0.2, 2.0, size=N)
-    apply_bc_2d(W, g, nx, ny, bc)
-    dx = 1.0 / (nx + 2 * g)
-    dy = 1.0 / (ny + 2 * g)
-    U = primitive_to_conserved_2d(W, gamma, dx * dy)
-    return Problem2D(nx, ny, g, 0.0, 1.0, 0.0, 1.0, gamma, W, U, tuple(bc),
-                     integrator, "riemann_solver_hllc", limiter, cfl=0.5,
-                     tf=1e300, max_steps=steps, name=f"random_{nx}x{ny}_{seed}")
-
-
-def sod_1d(n: int = 1000, g: int = 2) -> Problem1D:
-    """Sod shock tube as in examples/sod_shock_1d/sod_shock_1d.c:47-62: left
-    (1, 0, 1) for x < 0.5, right (0.125, 0, 0.1), set over the padded range;
-    transmissive; Godunov first order + exact solver; CFL 0.9, tf = 0.2."""
-    gamma = 1.4
-    x = mid_points(0.0, 1.0, n, g)
-    left = x < 0.5
-    W = np.zeros((3, n + 2 * g))
-    W[0] = np.where(left, 1.0, 0.125)
-    W[1] = 0.0
-    W[2] = np.where(left, 1.0, 0.1)
-    vol = 1.0 / (n + 2 * g)
-    U = primitive_to_conserved_1d(W, gamma, vol)
-    return Problem1D(n, g, 0.0, 1.0, gamma, W, U, ("transmissive", "transmissive"),
-                     "godunov_first_order_1d", "riemann_solver_exact", "minmod",
-                     cfl=0.9, tf=0.2, max_steps=-1, name=f"sod_{n}")
+# Seeded workloads live with the package (hydrofv_gb300/problems.py); they are
+# re-exported here so tests can use one namespace.
+from hydrofv_gb300.problems import (  # noqa: E402,F401
+    Problem1D, Problem2D, apply_bc_2d, four_quadrant, mid_points, point_blast,
+    primitive_to_conserved_1d, primitive_to_conserved_2d, random_problem_2d, shear_layer,
+    sod_1d,
+)
 
 
 def rel_l1(a: np.ndarray, b: np.ndarray, g: int) -> np.ndarray:
