@@ -33,6 +33,7 @@ CUDA_SOURCES = [
     ("gpu/runtime2d.cu", []),
     ("gpu/host_numerics.cu", ["--fmad=false"]),
     ("gpu/calibrate.cu", []),
+    ("gpu/noalloc2d.cu", []),
 ]
 C_SOURCES = [
     "host/error.c",

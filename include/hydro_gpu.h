@@ -122,6 +122,47 @@ void hydro_gpu_solver_destroy(HydroGpuSolver *solver);
  * for roofline reporting.  Returns 0 on success. */
 int hydro_gpu_calibrate(int device, double *fp64_tflops, double *fp32_tflops);
 
+/* ------------------------------------------------------------------ */
+/* Allocation-free run.  No counterpart in the reference.              */
+/* ------------------------------------------------------------------ */
+
+/* Largest padded grid ((nx + 2G) * (ny + 2G) cells) the allocation-free
+ * entry point accepts; its device state lives in a static array of about
+ * 5.5 MiB that every GPU loading this library keeps until process exit. */
+#define HYDRO_GPU_NOALLOC_MAX_CELLS 32768
+
+/* MUSCL-Hancock 2D run (HLLC, built-in boundaries) that allocates nothing:
+ * no cudaMalloc / cudaFree / cudaMallocHost, no stream or event creation, no
+ * heap traceback.  For callers that must not allocate while they step: a
+ * program whose device memory belongs to another allocator (a framework's
+ * caching pool or a budget fixed at start-up, where a private cudaMalloc can
+ * fail or fragment it), or a latency-sensitive loop that cannot take
+ * cudaFree's device-wide synchronisation.  Same inputs and outputs as
+ * launch_simulation for that integrator: the System's host arrays are read
+ * and receive the final W and U; names in `boundary_condition_param` and
+ * `integrator_param` are resolved here (finalize_* need not be called).
+ * Runs on the calling thread's current device, until tf or `max_steps`
+ * (< 0: no limit), synchronously.  No snapshots.
+ *
+ * Limits: grids above HYDRO_GPU_NOALLOC_MAX_CELLS padded cells are rejected
+ * with VALUE_ERROR.  The first call on a device looks up the static array's
+ * device address (cudaGetSymbolAddress) with that device current; make that
+ * first call before any stream capture.  All calls share the array: calls
+ * that overlap on the GPU (from several threads or streams) race.
+ *
+ * Returns SUCCESS or an error code of error.h; the message goes into
+ * error_message (may be NULL). */
+int hydro_gpu_muscl_hancock_2d_noalloc(
+    const BoundaryConditionParam *boundary_condition_param,
+    System *system,
+    const IntegratorParam *integrator_param,
+    double tf,
+    int64 max_steps,
+    SimulationStatus *simulation_status,
+    char *error_message,
+    int error_message_size
+);
+
 /* Number of visible CUDA devices (0 when none; never fails). */
 int hydro_gpu_device_count(void);
 
