@@ -34,6 +34,7 @@ CUDA_SOURCES = [
     ("gpu/host_numerics.cu", ["--fmad=false"]),
     ("gpu/calibrate.cu", []),
     ("gpu/noalloc2d.cu", []),
+    ("gpu/run1d.cu", ["--fmad=false"]),
 ]
 C_SOURCES = [
     "host/error.c",

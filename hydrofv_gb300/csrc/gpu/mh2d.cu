@@ -82,10 +82,10 @@ __global__ void mh2d_materialize_kernel(const Mh2dArgs<R> a, int buf, R *out0, R
 
 /* ------------------------------------------------------------- launchers */
 
-template <class R, int LIM>
+template <class R, int LIM, int FIRST_ORDER>
 static cudaError_t launch_step_lim(const Mh2dArgs<R> &a, dim3 grid, cudaStream_t s)
 {
-    mh2d_step_kernel<R, LIM, MH2D_THREADS><<<grid, MH2D_THREADS, 0, s>>>(a);
+    mh2d_step_kernel<R, LIM, MH2D_THREADS, FIRST_ORDER><<<grid, MH2D_THREADS, 0, s>>>(a);
     return cudaGetLastError();
 }
 
@@ -93,10 +93,11 @@ template <class R>
 cudaError_t mh2d_launch_step(const Mh2dArgs<R> &a, int limiter, cudaStream_t s)
 {
     dim3 grid((a.nx + a.strip_w - 1) / a.strip_w, (a.ny + a.chunk_h - 1) / a.chunk_h);
+    if (a.first_order) return launch_step_lim<R, LIM_MINMOD, 1>(a, grid, s);
     switch (limiter) {
-    case LIM_MINMOD: return launch_step_lim<R, LIM_MINMOD>(a, grid, s);
-    case LIM_VAN_LEER: return launch_step_lim<R, LIM_VAN_LEER>(a, grid, s);
-    default: return launch_step_lim<R, LIM_MC>(a, grid, s);
+    case LIM_MINMOD: return launch_step_lim<R, LIM_MINMOD, 0>(a, grid, s);
+    case LIM_VAN_LEER: return launch_step_lim<R, LIM_VAN_LEER, 0>(a, grid, s);
+    default: return launch_step_lim<R, LIM_MC, 0>(a, grid, s);
     }
 }
 

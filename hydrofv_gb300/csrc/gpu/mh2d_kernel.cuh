@@ -62,6 +62,7 @@ struct Mh2dArgs {
     int bc[4];               /* x_min, x_max, y_min, y_max */
     double dx, dy;           /* System.dx_, dy_ (for dt) */
     double area_x, area_y, vol;
+    int first_order;         /* 1: Godunov first order (face states = cell states) */
 };
 
 /* Load W at padded (r, c), remapping ghost cells to their source. */
@@ -113,7 +114,7 @@ __device__ __forceinline__ void record_error(HydroStepControl *ctrl, int code, i
     if (atomicCAS(&ctrl->error_code, 0, code) == 0) ctrl->error_cell = where;
 }
 
-template <class R, int LIM, int NT>
+template <class R, int LIM, int NT, int FIRST_ORDER>
 __global__ void __launch_bounds__(NT) mh2d_step_kernel(const Mh2dArgs<R> a)
 {
     static_assert(NT % 32 == 0, "NT must be a whole number of warps");
@@ -172,14 +173,19 @@ __global__ void __launch_bounds__(NT) mh2d_step_kernel(const Mh2dArgs<R> a)
     int err = DEV_OK;
 
     /* Rows inside [r_begin, r_end) need the strip plus two halo columns per
-     * side (x work); rows outside need only the strip's own columns. */
+     * side (x work); rows outside need only the strip's own columns.  Cells
+     * outside the padded grid (first order with one ghost layer) are never
+     * read and are not loaded. */
+    const int tx = nx + 2 * g, ty = ny + 2 * g;
     auto load_row = [&](int r) {
+        if (r < 0 || r >= ty) return;
         const bool full = (r >= r_begin && r < r_end);
         const int lo = full ? 0 : 2;
         const int hi = full ? sw + 3 : sw + 1;
         const int s = r % 3;
         for (int u = tid; u < NT + 2; u += NT) {
-            if (u >= lo && u <= hi) {
+            const int c = c0 - 2 + u;
+            if (u >= lo && u <= hi && c >= 0 && c < tx) {
                 R w[5];
                 fetch_w(a, Win, Uin, raw, r, c0 - 2 + u, w);
 #pragma unroll
@@ -195,6 +201,10 @@ __global__ void __launch_bounds__(NT) mh2d_step_kernel(const Mh2dArgs<R> a)
         const int sb = (r + 2) % 3, sc = r % 3, st = (r + 1) % 3;
         const R rho = ring[sc][0][u], vx = ring[sc][1][u], vy = ring[sc][2][u];
         const R p = ring[sc][3][u], as = ring[sc][4][u];
+        if (FIRST_ORDER) {
+            lo[0] = hi[0] = rho; lo[1] = hi[1] = vy; lo[2] = hi[2] = vx; lo[3] = hi[3] = p;
+            return;
+        }
         R d[4];
         d[0] = limit_slope<LIM>(rho - ring[sb][0][u], ring[st][0][u] - rho);
         const R dvx = limit_slope<LIM>(vx - ring[sb][1][u], ring[st][1][u] - vx);
@@ -209,6 +219,10 @@ __global__ void __launch_bounds__(NT) mh2d_step_kernel(const Mh2dArgs<R> a)
         const int u = tid + 1;
         const R rho = ring[s][0][u], vx = ring[s][1][u], vy = ring[s][2][u];
         const R p = ring[s][3][u], as = ring[s][4][u];
+        if (FIRST_ORDER) {
+            lo[0] = hi[0] = rho; lo[1] = hi[1] = vx; lo[2] = hi[2] = vy; lo[3] = hi[3] = p;
+            return;
+        }
         R d[4];
         d[0] = limit_slope<LIM>(rho - ring[s][0][u - 1], ring[s][0][u + 1] - rho);
         d[1] = limit_slope<LIM>(vx - ring[s][1][u - 1], ring[s][1][u + 1] - vx);

@@ -99,10 +99,11 @@ extern "C" int hydro_run2d_create(const HydroGrid2D *grid, const HydroGpuOptions
 {
     memset(oc, 0, sizeof *oc);
     *out = nullptr;
-    if (grid->integrator != INTEGRATOR_MUSCL_HANCOCK_2D) {
+    if (grid->integrator != INTEGRATOR_MUSCL_HANCOCK_2D &&
+        grid->integrator != INTEGRATOR_GODUNOV_FIRST_ORDER_2D) {
         oc->kind = HYDRO_RUN_UNSUPPORTED;
         snprintf(oc->message, sizeof oc->message,
-                 "The GPU 2D path implements muscl_hancock_2d only.");
+                 "The GPU 2D path implements muscl_hancock_2d and godunov_first_order_2d.");
         return -1;
     }
     if (grid->nx < grid->g || grid->ny < grid->g) {
@@ -158,6 +159,7 @@ extern "C" int hydro_run2d_create(const HydroGrid2D *grid, const HydroGpuOptions
     a.area_x = grid->area_x;
     a.area_y = grid->area_y;
     a.vol = grid->vol;
+    a.first_order = (grid->integrator == INTEGRATOR_GODUNOV_FIRST_ORDER_2D) ? 1 : 0;
     return 0;
 }
 

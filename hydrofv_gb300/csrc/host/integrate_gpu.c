@@ -310,6 +310,106 @@ ErrorStatus godunov_first_order_2d(
     return run_2d(bcp, system, ip, sp, settings, simp, status, &opt, NULL);
 }
 
+/* Shared body of the 1D integrators (src/integrator_godunov_first_order.c:26-261,
+ * src/integrator_muscl_hancock.c:26-383), Cartesian grids. */
+static ErrorStatus run_1d(
+    BoundaryConditionParam *__restrict bcp,
+    System *__restrict s,
+    IntegratorParam *__restrict ip,
+    StoringParam *__restrict sp,
+    Settings *__restrict settings,
+    SimulationParam *__restrict simp,
+    SimulationStatus *__restrict status,
+    const HydroGpuOptions *opt,
+    HydroGpuStats *stats
+)
+{
+    const int cs = s->coord_sys_flag_;
+    if (cs != COORD_SYS_CARTESIAN_1D && cs != COORD_SYS_CYLINDRICAL_1D && cs != COORD_SYS_SPHERICAL_1D)
+    {
+        char msg[256];
+        snprintf(msg, sizeof msg,
+                 "Wrong coordinate system. Supported coordinate system: \"cartesian_1d\", "
+                 "\"cylindrical_1d\" and \"spherical_1d\", got: \"%s\"", s->coord_sys);
+        return WRAP_RAISE_ERROR(VALUE_ERROR, msg);
+    }
+    if (cs != COORD_SYS_CARTESIAN_1D)
+    {
+        return WRAP_RAISE_ERROR(NOT_IMPLEMENTED_ERROR,
+                                "Cylindrical and spherical grids (geometric source term) are not available on the GPU path.");
+    }
+    const int flags[2] = { bcp->boundary_condition_flag_x_min_, bcp->boundary_condition_flag_x_max_ };
+    for (int k = 0; k < 2; k++)
+    {
+        if (flags[k] == BOUNDARY_CONDITION_CUSTOM)
+            return WRAP_RAISE_ERROR(NOT_IMPLEMENTED_ERROR,
+                                    "Custom boundary conditions are not available on the GPU path.");
+        if (flags[k] < BOUNDARY_CONDITION_NONE || flags[k] > BOUNDARY_CONDITION_PERIODIC)
+            return WRAP_RAISE_ERROR(VALUE_ERROR, "Boundary condition flag not recognized.");
+    }
+    if (opt->precision != HYDRO_GPU_PRECISION_FP64)
+    {
+        return WRAP_RAISE_ERROR(NOT_IMPLEMENTED_ERROR, "Requested precision is not available for this integrator.");
+    }
+    const int g = s->num_ghost_cells_side;
+    const long long tx = s->num_cells_x + 2 * g;
+    if (!uniform(s->surface_area_x_, tx + 1) || !uniform(s->volume_, tx))
+    {
+        return WRAP_RAISE_ERROR(NOT_IMPLEMENTED_ERROR,
+                                "The GPU path needs uniform face areas and cell volumes (as system_init sets them).");
+    }
+    if (s->num_cells_x < g)
+    {
+        return WRAP_RAISE_ERROR(NOT_IMPLEMENTED_ERROR,
+                                "The GPU path needs at least num_ghost_cells_side interior cells.");
+    }
+    HydroGrid1D grid;
+    memset(&grid, 0, sizeof grid);
+    grid.nx = s->num_cells_x;
+    grid.g = g;
+    grid.gamma = s->gamma;
+    grid.tol = ip->tol;
+    grid.dx = s->dx_;
+    grid.area = s->surface_area_x_[0];
+    grid.vol = s->volume_[0];
+    grid.bc[0] = flags[0];
+    grid.bc[1] = flags[1];
+    grid.limiter = ip->slope_limiter_flag_;
+    grid.riemann_solver = ip->riemann_solver_flag_;
+    grid.integrator = ip->integrator_flag_;
+
+    status->num_steps = 0;
+    status->dt = 0.0;
+    status->t = 0.0;
+    sp->store_count_ = 0;
+    if (sp->is_storing && sp->store_initial)
+    {
+        ErrorStatus e = WRAP_TRACEBACK(store_snapshot(bcp, s, ip, status, sp));
+        if (e.return_code != SUCCESS) return e;
+    }
+    ProgressBarParam bar;
+    if (!settings->no_progress_bar) start_progress_bar(&bar, simp->tf);
+    double *W[3] = { s->density_, s->velocity_x_, s->pressure_ };
+    double *U[3] = { s->mass_, s->momentum_x_, s->energy_ };
+    const HydroStepParams params = step_params(ip, sp);
+    SnapCtx ctx = { bcp, s, ip, sp, make_success_error_status() };
+    HydroRunOutcome oc;
+    const int rc = hydro_run1d(&grid, W, U, &params, simp->tf, opt->max_steps, sp->store_count_,
+                               snapshot_cb, &ctx, opt, &oc, stats);
+    status->num_steps = oc.num_steps;
+    status->t = oc.t;
+    status->dt = oc.dt;
+    sp->store_count_ = oc.store_count;
+    if (!settings->no_progress_bar) update_progress_bar(&bar, status->t, true);
+    if (rc != 0)
+    {
+        if (oc.kind == HYDRO_RUN_CALLBACK_ERROR && ctx.status.return_code != SUCCESS) return ctx.status;
+        free_traceback(&ctx.status);
+        return outcome_error(&oc);
+    }
+    return make_success_error_status();
+}
+
 ErrorStatus godunov_first_order_1d(
     BoundaryConditionParam *__restrict bcp,
     System *__restrict system,
@@ -320,8 +420,8 @@ ErrorStatus godunov_first_order_1d(
     SimulationStatus *__restrict status
 )
 {
-    (void) bcp; (void) system; (void) ip; (void) sp; (void) settings; (void) simp; (void) status;
-    return WRAP_RAISE_ERROR(NOT_IMPLEMENTED_ERROR, "godunov_first_order_1d is not available yet.");
+    const HydroGpuOptions opt = process_options();
+    return run_1d(bcp, system, ip, sp, settings, simp, status, &opt, NULL);
 }
 
 ErrorStatus muscl_hancock_1d(
@@ -334,8 +434,8 @@ ErrorStatus muscl_hancock_1d(
     SimulationStatus *__restrict status
 )
 {
-    (void) bcp; (void) system; (void) ip; (void) sp; (void) settings; (void) simp; (void) status;
-    return WRAP_RAISE_ERROR(NOT_IMPLEMENTED_ERROR, "muscl_hancock_1d is not available yet.");
+    const HydroGpuOptions opt = process_options();
+    return run_1d(bcp, system, ip, sp, settings, simp, status, &opt, NULL);
 }
 
 ErrorStatus random_choice_1d(
@@ -383,6 +483,9 @@ ErrorStatus hydro_gpu_launch_simulation(
         case INTEGRATOR_MUSCL_HANCOCK_2D:
         case INTEGRATOR_GODUNOV_FIRST_ORDER_2D:
             return WRAP_TRACEBACK(run_2d(bcp, system, ip, sp, settings, simp, status, &opt, stats));
+        case INTEGRATOR_GODUNOV_FIRST_ORDER_1D:
+        case INTEGRATOR_MUSCL_HANCOCK_1D:
+            return WRAP_TRACEBACK(run_1d(bcp, system, ip, sp, settings, simp, status, &opt, stats));
         default:
         {
             const int had = g_have_process_options;

@@ -277,3 +277,21 @@ def sod_1d(n: int = 1000, g: int = 2) -> Problem1D:
                      cfl=0.9, tf=0.2, max_steps=-1, name=f"sod_{n}")
 
 
+
+
+def random_problem_1d(nx: int, seed: int, bc, integrator: str = "godunov_first_order_1d",
+                      riemann_solver: str = "riemann_solver_exact", limiter: str = "minmod",
+                      steps: int = 20, g: int = 2) -> Problem1D:
+    """Smooth random 1D states (plus a jump) for edge-case parity tests."""
+    rng = np.random.default_rng(seed)
+    gamma = float(rng.choice([1.4, 5.0 / 3.0]))
+    x = mid_points(0.0, 1.0, nx, g)
+    W = np.zeros((3, nx + 2 * g))
+    W[0] = 1.0 + 0.3 * np.sin(2 * math.pi * x) + np.where(x < 0.5, 0.5, 0.0)
+    W[1] = 0.2 * np.cos(2 * math.pi * x)
+    W[2] = 1.0 + 0.2 * np.cos(4 * math.pi * x) + np.where(x < 0.3, 0.4, 0.0)
+    W += rng.uniform(-1e-3, 1e-3, size=W.shape)
+    vol = 1.0 / (nx + 2 * g)
+    U = primitive_to_conserved_1d(W, gamma, vol)
+    return Problem1D(nx, g, 0.0, 1.0, gamma, W, U, tuple(bc), integrator, riemann_solver,
+                     limiter, cfl=0.8, tf=1e300, max_steps=steps, name=f"random1d_{nx}_{seed}")

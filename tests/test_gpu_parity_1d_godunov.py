@@ -1,0 +1,110 @@
+"""GPU parity of the 1D integrators and of Godunov first order 2D.
+
+1D: the Sod tube of the first benchmark configuration (1000 cells, Godunov
+first order + exact Riemann solver, CFL 0.9, t = 0.2) is compared cell by
+cell with the unmodified reference's output (golden fixture), and MUSCL-
+Hancock 1D (HLLC and exact) likewise; random problems cover every built-in
+boundary.  2D Godunov is compared with the golden fixture and the oracle,
+including one ghost layer (the minimum the reference allows for it).
+"""
+import os
+
+import numpy as np
+import pytest
+
+import hydrofv_gb300 as H
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+REL_L1_TOL = 1e-12
+
+
+def run1(p):
+    return H.run_1d(p.nx, p.g, (p.x_min, p.x_max), p.gamma, p.W, p.U, bc=p.bc,
+                    integrator=p.integrator, riemann_solver=p.riemann_solver,
+                    slope_limiter=p.slope_limiter, cfl=p.cfl, tf=p.tf, max_steps=p.max_steps)
+
+
+def run2(p):
+    return H.run_2d(p.nx, p.ny, p.g, (p.x_min, p.x_max, p.y_min, p.y_max), p.gamma, p.W, p.U,
+                    bc=p.bc, integrator=p.integrator, riemann_solver=p.riemann_solver,
+                    slope_limiter=p.slope_limiter, cfl=p.cfl, tf=p.tf, max_steps=p.max_steps)
+
+
+def rel_l1_1d(a, b, g):
+    ia, ib = a[:, g:-g], b[:, g:-g]
+    return np.abs(ia - ib).sum(axis=1) / np.abs(ib).sum(axis=1)
+
+
+@pytest.mark.parametrize("name", ["sod_1000_godunov_exact", "sod_200_muscl_hllc_vl",
+                                  "sod_100_muscl_exact_mc"])
+def test_sod_against_reference_golden(gpu_available, name):
+    import sys
+    sys.path.insert(0, GOLDEN)
+    import make_golden as MG
+    p = MG.cases_1d()[name]
+    g = np.load(os.path.join(GOLDEN, f"{name}.npz"))
+    r = run1(p)
+    assert r.code == 0, r.message
+    assert r.num_steps == int(g["num_steps"])
+    assert r.t == pytest.approx(float(g["t"]), rel=1e-14)
+    assert np.all(rel_l1_1d(r.U, g["U"], p.g) <= REL_L1_TOL)
+    # every cell, ghost cells included
+    assert np.max(np.abs(r.W - g["W"])) <= 1e-12 * np.max(np.abs(g["W"]))
+    assert np.max(np.abs(r.U - g["U"])) <= 1e-12 * np.max(np.abs(g["U"]))
+
+
+@pytest.mark.parametrize("bc", [("transmissive", "transmissive"), ("reflective", "reflective"),
+                                ("periodic", "periodic"), ("none", "reflective")])
+@pytest.mark.parametrize("integ,solver,lim", [("godunov_first_order_1d", "riemann_solver_exact", "minmod"),
+                                              ("godunov_first_order_1d", "riemann_solver_hllc", "minmod"),
+                                              ("muscl_hancock_1d", "riemann_solver_hllc", "monotonized_central"),
+                                              ("muscl_hancock_1d", "riemann_solver_exact", "van_leer")])
+def test_random_1d_against_oracle(gpu_available, oracle_mod, bc, integ, solver, lim):
+    from hydrofv_gb300.problems import random_problem_1d
+    p = random_problem_1d(300, 4, bc, integ, solver, lim, steps=40)
+    ref = oracle_mod.load("oracle").run_1d(p)
+    r = run1(p)
+    assert r.code == 0 and ref.rc == 0, r.message
+    assert r.num_steps == ref.num_steps == 40
+    assert np.all(rel_l1_1d(r.U, ref.U, p.g) <= REL_L1_TOL)
+
+
+def test_1d_large_grid_runs_in_one_cta(gpu_available, oracle_mod):
+    from hydrofv_gb300.problems import random_problem_1d
+    p = random_problem_1d(5000, 8, ("periodic", "periodic"), "muscl_hancock_1d",
+                          "riemann_solver_hllc", "minmod", steps=25)
+    ref = oracle_mod.load("oracle").run_1d(p)
+    r = run1(p)
+    assert r.code == 0, r.message
+    assert np.all(rel_l1_1d(r.U, ref.U, p.g) <= REL_L1_TOL)
+
+
+def test_godunov_2d_against_golden(gpu_available):
+    import sys
+    sys.path.insert(0, GOLDEN)
+    import make_golden as MG
+    name = "random_17x11_periodic_godunov_10"
+    p = MG.cases_2d()[name]
+    g = np.load(os.path.join(GOLDEN, f"{name}.npz"))
+    r = run2(p)
+    assert r.code == 0, r.message
+    assert r.num_steps == int(g["num_steps"])
+    ia, ib = r.U[:, p.g:-p.g, p.g:-p.g], g["U"][:, p.g:-p.g, p.g:-p.g]
+    assert np.all(np.abs(ia - ib).sum(axis=(1, 2)) / np.abs(ib).sum(axis=(1, 2)) <= REL_L1_TOL)
+
+
+@pytest.mark.parametrize("g", [1, 2, 3])
+@pytest.mark.parametrize("bc", [("reflective", "transmissive", "periodic", "periodic"),
+                                ("none", "none", "reflective", "transmissive")])
+def test_godunov_2d_against_oracle(gpu_available, oracle_mod, g, bc):
+    O = oracle_mod
+    p = O.random_problem_2d(140, 37, 13, bc, "minmod", 15, g=g, integrator="godunov_first_order_2d",
+                            smooth=True)
+    ref = O.load("oracle").run_2d(p)
+    r = run2(p)
+    assert r.code == 0 and ref.rc == 0, r.message
+    assert r.num_steps == ref.num_steps
+    assert np.all(O.rel_l1(r.U, ref.U, p.g) <= REL_L1_TOL)
+    assert np.all(O.rel_l1(r.W, ref.W, p.g) <= REL_L1_TOL)
