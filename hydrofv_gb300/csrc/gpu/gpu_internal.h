@@ -16,6 +16,8 @@ namespace hydro {
 template <class R>
 cudaError_t mh2d_launch_step(const Mh2dArgs<R> &a, int limiter, cudaStream_t s);
 template <class R>
+int mh2d_resident_ctas(int limiter, int first_order, int device);
+template <class R>
 cudaError_t mh2d_launch_prepare(const Mh2dArgs<R> &a, cudaStream_t s);
 template <class R>
 cudaError_t mh2d_launch_materialize(const Mh2dArgs<R> &a, int buf, R *const out[4], cudaStream_t s);

@@ -83,7 +83,7 @@ __global__ void mh2d_materialize_kernel(const Mh2dArgs<R> a, int buf, R *out0, R
 /* ------------------------------------------------------------- launchers */
 
 template <class R, int LIM, int FIRST_ORDER>
-static cudaError_t launch_step_lim(const Mh2dArgs<R> &a, dim3 grid, cudaStream_t s)
+static cudaError_t launch_step_lim(const Mh2dArgs<R> &a, int grid, cudaStream_t s)
 {
     mh2d_step_kernel<R, LIM, MH2D_THREADS, FIRST_ORDER><<<grid, MH2D_THREADS, 0, s>>>(a);
     return cudaGetLastError();
@@ -92,7 +92,8 @@ static cudaError_t launch_step_lim(const Mh2dArgs<R> &a, dim3 grid, cudaStream_t
 template <class R>
 cudaError_t mh2d_launch_step(const Mh2dArgs<R> &a, int limiter, cudaStream_t s)
 {
-    dim3 grid((a.nx + a.strip_w - 1) / a.strip_w, (a.ny + a.chunk_h - 1) / a.chunk_h);
+    const int n_items = ((a.nx + a.strip_w - 1) / a.strip_w) * ((a.ny + a.chunk_h - 1) / a.chunk_h);
+    const int grid = (a.grid_ctas > 0 && a.grid_ctas < n_items) ? a.grid_ctas : n_items;
     if (a.first_order) return launch_step_lim<R, LIM_MINMOD, 1>(a, grid, s);
     switch (limiter) {
     case LIM_MINMOD: return launch_step_lim<R, LIM_MINMOD, 0>(a, grid, s);
@@ -115,6 +116,26 @@ cudaError_t mh2d_launch_materialize(const Mh2dArgs<R> &a, int buf, R *const out[
     return cudaGetLastError();
 }
 
+/* CTAs of the step kernel that fit on the device at once. */
+template <class R>
+int mh2d_resident_ctas(int limiter, int first_order, int device)
+{
+    int per_sm = 0, sms = 0;
+    cudaError_t e;
+    if (first_order)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mh2d_step_kernel<R, LIM_MINMOD, MH2D_THREADS, 1>, MH2D_THREADS, 0);
+    else if (limiter == LIM_MINMOD)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mh2d_step_kernel<R, LIM_MINMOD, MH2D_THREADS, 0>, MH2D_THREADS, 0);
+    else if (limiter == LIM_VAN_LEER)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mh2d_step_kernel<R, LIM_VAN_LEER, MH2D_THREADS, 0>, MH2D_THREADS, 0);
+    else
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mh2d_step_kernel<R, LIM_MC, MH2D_THREADS, 0>, MH2D_THREADS, 0);
+    if (e != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess)
+        return 0;
+    return per_sm * sms;
+}
+
+template int mh2d_resident_ctas<double>(int, int, int);
 template cudaError_t mh2d_launch_step<double>(const Mh2dArgs<double> &, int, cudaStream_t);
 template cudaError_t mh2d_launch_prepare<double>(const Mh2dArgs<double> &, cudaStream_t);
 template cudaError_t mh2d_launch_materialize<double>(const Mh2dArgs<double> &, int,

@@ -63,6 +63,7 @@ struct Mh2dArgs {
     double dx, dy;           /* System.dx_, dy_ (for dt) */
     double area_x, area_y, vol;
     int first_order;         /* 1: Godunov first order (face states = cell states) */
+    int grid_ctas;           /* persistent CTAs per step launch (0: one per work item) */
 };
 
 /* Load W at padded (r, c), remapping ghost cells to their source. */
@@ -114,8 +115,88 @@ __device__ __forceinline__ void record_error(HydroStepControl *ctrl, int code, i
     if (atomicCAS(&ctrl->error_code, 0, code) == 0) ctrl->error_cell = where;
 }
 
+/* Shared memory of one CTA: the W row ring and one batch of faces. */
+template <class R, int NT>
+struct Mh2dShared {
+    R ring[3][5][NT + 2];       /* W rows (rho, u, v, p, a), columns c0-2 .. c0+NT-1 */
+    R FL[4][2 * NT];            /* left face states; overwritten by the face flux */
+    R FR[4][2 * NT];            /* right face states */
+    R aL[2 * NT], aR[2 * NT];   /* sound speeds of the face states */
+    R pg[2 * NT];               /* star-pressure guess (before the tol floor) */
+    unsigned char reg[2 * NT];  /* PREG_* regime of each face */
+    short listT[2 * NT];        /* faces needing the two-rarefaction guess */
+    short listS[2 * NT];        /* faces needing the two-shock guess */
+    int nT, nS;
+    int item;
+    int am_last;
+    double red[2][NT / 32];
+};
+
+/*
+ * Solve faces 0..nF-1 of the batch in sm.FL / sm.FR (normal velocity in
+ * slot 1) with the HLLC flux, as three dense passes over the CTA:
+ * classify (sound speeds, vacuum test, guess regime), the expensive guesses
+ * on compacted lists (two-rarefaction: three pow; two-shock: five divides
+ * and two square roots), and the finish (wave speeds, S*, region flux).
+ * Compaction keeps lanes busy where neighbouring faces fall into different
+ * regimes, which the one-face-per-thread form serialises.  The flux
+ * replaces the left state in sm.FL.  Ends with a barrier.
+ */
+template <class R, int NT>
+__device__ __forceinline__ int solve_faces(Mh2dShared<R, NT> &sm, const GasConst<R> &gas, int nF)
+{
+    const int tid = threadIdx.x;
+    int err = DEV_OK;
+    for (int f = tid; f < nF; f += NT) {
+        R aL, aR, ppv;
+        const int reg = hllc_classify(gas, sm.FL[0][f], sm.FL[1][f], sm.FL[3][f],
+                                      sm.FR[0][f], sm.FR[1][f], sm.FR[3][f], aL, aR, ppv);
+        sm.aL[f] = aL;
+        sm.aR[f] = aR;
+        sm.pg[f] = ppv;
+        sm.reg[f] = (unsigned char) reg;
+        if (reg == PREG_TRRS) sm.listT[atomicAdd(&sm.nT, 1)] = (short) f;
+        else if (reg == PREG_TSRS) sm.listS[atomicAdd(&sm.nS, 1)] = (short) f;
+    }
+    __syncthreads();
+    const int nT = sm.nT, nS = sm.nS;
+    for (int i = tid; i < nT + nS; i += NT) {
+        if (i < nT) {
+            const int f = sm.listT[i];
+            sm.pg[f] = guess_p_trrs(gas, sm.FL[1][f], sm.FL[3][f], sm.aL[f],
+                                    sm.FR[1][f], sm.FR[3][f], sm.aR[f]);
+        } else {
+            const int f = sm.listS[i - nT];
+            sm.pg[f] = guess_p_tsrs(gas, sm.FL[0][f], sm.FL[1][f], sm.FL[3][f],
+                                    sm.FR[0][f], sm.FR[1][f], sm.FR[3][f], sm.pg[f]);
+        }
+    }
+    __syncthreads();
+    for (int f = tid; f < nF; f += NT) {
+        R F[4];
+        const R rl = sm.FL[0][f], ul = sm.FL[1][f], vl = sm.FL[2][f], pl = sm.FL[3][f];
+        const R rr = sm.FR[0][f], ur = sm.FR[1][f], vr = sm.FR[2][f], pr = sm.FR[3][f];
+        if (sm.reg[f] == PREG_VACUUM) {
+            hllc_vacuum_flux(gas, rl, ul, vl, pl, sm.aL[f], rr, ur, vr, pr, sm.aR[f], F);
+        } else {
+            const int rc = hllc_finish(gas, rl, ul, vl, pl, sm.aL[f], rr, ur, vr, pr, sm.aR[f],
+                                       sm.pg[f], F);
+            if (rc) err = rc;
+        }
+#pragma unroll
+        for (int q = 0; q < 4; q++) sm.FL[q][f] = F[q];
+    }
+    __syncthreads();
+    return err;
+}
+
+/*
+ * One time step.  The grid is persistent: each CTA takes (strip, row chunk)
+ * items from a device counter until none are left, so SMs that finish early
+ * take more work (the FP64 pipe of an SM is shared by its CTAs).
+ */
 template <class R, int LIM, int NT, int FIRST_ORDER>
-__global__ void __launch_bounds__(NT) mh2d_step_kernel(const Mh2dArgs<R> a)
+__global__ void __launch_bounds__(NT, 4) mh2d_step_kernel(const Mh2dArgs<R> a)
 {
     static_assert(NT % 32 == 0, "NT must be a whole number of warps");
     HydroStepControl *ctrl = a.ctrl;
@@ -131,7 +212,7 @@ __global__ void __launch_bounds__(NT) mh2d_step_kernel(const Mh2dArgs<R> a)
     const double tf = ctrl->tf;
     if (t_now + dt > tf) dt = tf - t_now;
     if (dt == 0.0) {
-        if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) {
             ctrl->dt = dt;
             record_error(ctrl, DEV_ERR_DT_ZERO, -1);
             ctrl->active = 0;
@@ -150,197 +231,214 @@ __global__ void __launch_bounds__(NT) mh2d_step_kernel(const Mh2dArgs<R> a)
     const R *const *Win = a.W[buf];
     R *const *Wout = a.W[buf ^ 1];
 
-    __shared__ R ring[3][5][NT + 2];
-    __shared__ R xlo[4][NT];
-    __shared__ R xfl[4][NT];
-    __shared__ double red[2][NT / 32];
-    __shared__ int am_last;
+    __shared__ Mh2dShared<R, NT> sm;
 
     const int tid = threadIdx.x;
     const int g = a.g, nx = a.nx, ny = a.ny;
-    const int c0 = g + blockIdx.x * a.strip_w;
-    const int sw = min(a.strip_w, nx - (int) blockIdx.x * a.strip_w);
-    const int r_begin = g + blockIdx.y * a.chunk_h;
-    const int r_end = min(r_begin + a.chunk_h, g + ny);
-    const int col = c0 - 1 + tid;
-    const bool x_slot = tid <= sw + 1;
-    const bool x_face = tid <= sw;
-    const bool inner = tid >= 1 && tid <= sw;
-    const bool ghost_xmin = (c0 == g) && tid == 0;
-    const bool ghost_xmax = (c0 + sw == g + nx) && tid == sw + 1;
+    const int tx = nx + 2 * g, ty = ny + 2 * g;
+    const int n_strips = (nx + a.strip_w - 1) / a.strip_w;
+    const int n_items = n_strips * ((ny + a.chunk_h - 1) / a.chunk_h);
+    const int ymap[4] = { 0, 2, 1, 3 };   /* y fluxes come back as (mass, mom_y, mom_x, energy) */
 
     double mx_x = -CUDART_INF, mx_y = -CUDART_INF;
     int err = DEV_OK;
 
-    /* Rows inside [r_begin, r_end) need the strip plus two halo columns per
-     * side (x work); rows outside need only the strip's own columns.  Cells
-     * outside the padded grid (first order with one ghost layer) are never
-     * read and are not loaded. */
-    const int tx = nx + 2 * g, ty = ny + 2 * g;
-    auto load_row = [&](int r) {
-        if (r < 0 || r >= ty) return;
-        const bool full = (r >= r_begin && r < r_end);
-        const int lo = full ? 0 : 2;
-        const int hi = full ? sw + 3 : sw + 1;
-        const int s = r % 3;
-        for (int u = tid; u < NT + 2; u += NT) {
-            const int c = c0 - 2 + u;
-            if (u >= lo && u <= hi && c >= 0 && c < tx) {
-                R w[5];
-                fetch_w(a, Win, Uin, raw, r, c0 - 2 + u, w);
-#pragma unroll
-                for (int q = 0; q < 5; q++) ring[s][q][u] = w[q];
-            }
-        }
-    };
-
-    /* y reconstruction of this thread's cell in row r (rows r-1..r+1 in the ring).
-     * Outputs are in the y-sweep's (rho, v, u, p) order. */
-    auto recon_y = [&](int r, R lo[4], R hi[4]) {
-        const int u = tid + 1;
-        const int sb = (r + 2) % 3, sc = r % 3, st = (r + 1) % 3;
-        const R rho = ring[sc][0][u], vx = ring[sc][1][u], vy = ring[sc][2][u];
-        const R p = ring[sc][3][u], as = ring[sc][4][u];
-        if (FIRST_ORDER) {
-            lo[0] = hi[0] = rho; lo[1] = hi[1] = vy; lo[2] = hi[2] = vx; lo[3] = hi[3] = p;
-            return;
-        }
-        R d[4];
-        d[0] = limit_slope<LIM>(rho - ring[sb][0][u], ring[st][0][u] - rho);
-        const R dvx = limit_slope<LIM>(vx - ring[sb][1][u], ring[st][1][u] - vx);
-        d[1] = limit_slope<LIM>(vy - ring[sb][2][u], ring[st][2][u] - vy);
-        d[2] = dvx;
-        d[3] = limit_slope<LIM>(p - ring[sb][3][u], ring[st][3][u] - p);
-        hancock_2d(dtA_y, dtA_y / rho, rho, vy, vx, p, as, d, dvx, lo, hi);
-    };
-
-    /* x reconstruction of slot tid in ring row s, (rho, u, v, p) order. */
-    auto recon_x = [&](int s, R lo[4], R hi[4]) {
-        const int u = tid + 1;
-        const R rho = ring[s][0][u], vx = ring[s][1][u], vy = ring[s][2][u];
-        const R p = ring[s][3][u], as = ring[s][4][u];
-        if (FIRST_ORDER) {
-            lo[0] = hi[0] = rho; lo[1] = hi[1] = vx; lo[2] = hi[2] = vy; lo[3] = hi[3] = p;
-            return;
-        }
-        R d[4];
-        d[0] = limit_slope<LIM>(rho - ring[s][0][u - 1], ring[s][0][u + 1] - rho);
-        d[1] = limit_slope<LIM>(vx - ring[s][1][u - 1], ring[s][1][u + 1] - vx);
-        d[2] = limit_slope<LIM>(vy - ring[s][2][u - 1], ring[s][2][u + 1] - vy);
-        d[3] = limit_slope<LIM>(p - ring[s][3][u - 1], ring[s][3][u + 1] - p);
-        hancock_2d(dtA_x, dtA_x / rho, rho, vx, vy, p, as, d, d[1], lo, hi);
-    };
-
-    /* ---- prologue: the face below r_begin ---- */
-    load_row(r_begin - 2);
-    load_row(r_begin - 1);
-    load_row(r_begin);
-    __syncthreads();
-    R ytop[4], gbot[4];
-    R tmp_lo[4], prev_hi[4];
-    if (inner) recon_y(r_begin - 1, tmp_lo, prev_hi);
-    __syncthreads();
-    load_row(r_begin + 1);
-    __syncthreads();
-    if (inner) {
-        recon_y(r_begin, tmp_lo, ytop);
-        const int rc = hllc_flux_2d(a.gas, prev_hi[0], prev_hi[1], prev_hi[2], prev_hi[3],
-                                    tmp_lo[0], tmp_lo[1], tmp_lo[2], tmp_lo[3], gbot);
-        if (rc) err = rc;
-    }
-    __syncthreads();
-
-    /* ---- march up the rows ---- */
-    for (int r = r_begin; r < r_end; r++) {
-        load_row(r + 2);
+    for (;;) {
+        if (tid == 0) sm.item = atomicAdd(&ctrl->work_next, 1);
         __syncthreads();
+        const int item = sm.item;
+        __syncthreads();
+        if (item >= n_items) break;
 
-        R gtop[4], nlo[4], nhi[4];
+        const int strip = item % n_strips;
+        const int c0 = g + strip * a.strip_w;
+        const int sw = min(a.strip_w, nx - strip * a.strip_w);
+        const int r_begin = g + (item / n_strips) * a.chunk_h;
+        const int r_end = min(r_begin + a.chunk_h, g + ny);
+        const int col = c0 - 1 + tid;
+        const bool x_slot = tid <= sw + 1;
+        const bool inner = tid >= 1 && tid <= sw;
+        const bool ghost_xmin = (c0 == g) && tid == 0;
+        const bool ghost_xmax = (c0 + sw == g + nx) && tid == sw + 1;
+        const int nX = sw + 1;
+
+        /* Rows inside [r_begin, r_end) need the strip plus two halo columns per
+         * side (x work); rows outside need only the strip's own columns.  Cells
+         * outside the padded grid (first order with one ghost layer) are never
+         * read and are not loaded. */
+        auto load_row = [&](int r) {
+            if (r < 0 || r >= ty) return;
+            const bool full = (r >= r_begin && r < r_end);
+            const int lo = full ? 0 : 2;
+            const int hi = full ? sw + 3 : sw + 1;
+            const int s = r % 3;
+            for (int u = tid; u < NT + 2; u += NT) {
+                const int c = c0 - 2 + u;
+                if (u >= lo && u <= hi && c >= 0 && c < tx) {
+                    R w[5];
+                    fetch_w(a, Win, Uin, raw, r, c, w);
+#pragma unroll
+                    for (int q = 0; q < 5; q++) sm.ring[s][q][u] = w[q];
+                }
+            }
+        };
+
+        /* y reconstruction of this thread's cell in row r, (rho, v, u, p) order */
+        auto recon_y = [&](int r, R lo[4], R hi[4]) {
+            const int u = tid + 1;
+            const int sb = (r + 2) % 3, sc = r % 3, st = (r + 1) % 3;
+            const R rho = sm.ring[sc][0][u], vx = sm.ring[sc][1][u], vy = sm.ring[sc][2][u];
+            const R p = sm.ring[sc][3][u], as = sm.ring[sc][4][u];
+            if (FIRST_ORDER) {
+                lo[0] = hi[0] = rho; lo[1] = hi[1] = vy; lo[2] = hi[2] = vx; lo[3] = hi[3] = p;
+                return;
+            }
+            R d[4];
+            d[0] = limit_slope<LIM>(rho - sm.ring[sb][0][u], sm.ring[st][0][u] - rho);
+            const R dvx = limit_slope<LIM>(vx - sm.ring[sb][1][u], sm.ring[st][1][u] - vx);
+            d[1] = limit_slope<LIM>(vy - sm.ring[sb][2][u], sm.ring[st][2][u] - vy);
+            d[2] = dvx;
+            d[3] = limit_slope<LIM>(p - sm.ring[sb][3][u], sm.ring[st][3][u] - p);
+            hancock_2d(dtA_y, dtA_y / rho, rho, vy, vx, p, as, d, dvx, lo, hi);
+        };
+
+        /* x reconstruction of slot tid in ring row s, (rho, u, v, p) order */
+        auto recon_x = [&](int s, R lo[4], R hi[4]) {
+            const int u = tid + 1;
+            const R rho = sm.ring[s][0][u], vx = sm.ring[s][1][u], vy = sm.ring[s][2][u];
+            const R p = sm.ring[s][3][u], as = sm.ring[s][4][u];
+            if (FIRST_ORDER) {
+                lo[0] = hi[0] = rho; lo[1] = hi[1] = vx; lo[2] = hi[2] = vy; lo[3] = hi[3] = p;
+                return;
+            }
+            R d[4];
+            d[0] = limit_slope<LIM>(rho - sm.ring[s][0][u - 1], sm.ring[s][0][u + 1] - rho);
+            d[1] = limit_slope<LIM>(vx - sm.ring[s][1][u - 1], sm.ring[s][1][u + 1] - vx);
+            d[2] = limit_slope<LIM>(vy - sm.ring[s][2][u - 1], sm.ring[s][2][u + 1] - vy);
+            d[3] = limit_slope<LIM>(p - sm.ring[s][3][u - 1], sm.ring[s][3][u + 1] - p);
+            hancock_2d(dtA_x, dtA_x / rho, rho, vx, vy, p, as, d, d[1], lo, hi);
+        };
+
+        /* ---- prologue: the faces below r_begin ---- */
+        load_row(r_begin - 2);
+        load_row(r_begin - 1);
+        load_row(r_begin);
+        __syncthreads();
+        R ytop[4], gbot[4];
+        R tmp_lo[4], prev_hi[4];
+        if (inner) recon_y(r_begin - 1, tmp_lo, prev_hi);
+        __syncthreads();
+        load_row(r_begin + 1);
+        if (tid == 0) { sm.nT = 0; sm.nS = 0; }
+        __syncthreads();
         if (inner) {
-            recon_y(r + 1, nlo, nhi);
-            const int rc = hllc_flux_2d(a.gas, ytop[0], ytop[1], ytop[2], ytop[3],
-                                        nlo[0], nlo[1], nlo[2], nlo[3], gtop);
+            recon_y(r_begin, tmp_lo, ytop);
+#pragma unroll
+            for (int q = 0; q < 4; q++) { sm.FL[q][tid - 1] = prev_hi[q]; sm.FR[q][tid - 1] = tmp_lo[q]; }
+        }
+        __syncthreads();
+        {
+            const int rc = solve_faces<R, NT>(sm, a.gas, sw);
             if (rc) err = rc;
         }
-        R xl[4], xh[4];
-        if (x_slot) {
-            recon_x(r % 3, xl, xh);
+        if (inner) {
 #pragma unroll
-            for (int q = 0; q < 4; q++) xlo[q][tid] = xl[q];
+            for (int q = 0; q < 4; q++) gbot[q] = sm.FL[q][tid - 1];
         }
         __syncthreads();
 
-        R fx[4];
-        if (x_face) {
-            const int rc = hllc_flux_2d(a.gas, xh[0], xh[1], xh[2], xh[3],
-                                        xlo[0][tid + 1], xlo[1][tid + 1], xlo[2][tid + 1],
-                                        xlo[3][tid + 1], fx);
-            if (rc) err = rc;
-#pragma unroll
-            for (int q = 0; q < 4; q++) xfl[q][tid] = fx[q];
-        }
-        __syncthreads();
+        /* ---- march up the rows ---- */
+        for (int r = r_begin; r < r_end; r++) {
+            load_row(r + 2);
+            if (tid == 0) { sm.nT = 0; sm.nS = 0; }
+            __syncthreads();
 
-        const long long rowbase = (long long) r * a.pitch;
-        if (inner) {
-            const long long idx = rowbase + col;
-            /* y fluxes come back as (mass, mom_y, mom_x, energy) */
-            const int ymap[4] = { 0, 2, 1, 3 };
-            R Un[4];
+            R nhi[4];
+            if (inner) {
+                R nlo[4];
+                recon_y(r + 1, nlo, nhi);
+                const int f = nX + tid - 1;
 #pragma unroll
-            for (int q = 0; q < 4; q++) {
-                R v = Uin[q][idx];
-                v = v + (xfl[q][tid - 1] * dtr) * Ax;
-                v = v - (fx[q] * dtr) * Ax;
-                v = v + (gbot[ymap[q]] * dtr) * Ay;
-                v = v - (gtop[ymap[q]] * dtr) * Ay;
-                Un[q] = v;
-                Uout[q][idx] = v;
+                for (int q = 0; q < 4; q++) { sm.FL[q][f] = ytop[q]; sm.FR[q][f] = nlo[q]; }
             }
-            R w[4];
-            cons_to_prim_2d(a.gas, (R) a.vol, Un[0], Un[1], Un[2], Un[3], w);
-            const R as = sound_speed(a.gas, w[0], w[3]);
+            if (x_slot) {
+                R xl[4], xh[4];
+                recon_x(r % 3, xl, xh);
+                if (tid <= sw) {
 #pragma unroll
-            for (int q = 0; q < 4; q++) Wout[q][idx] = w[q];
-            Wout[4][idx] = as;
-            const double sx = (double) (as + fabs(w[1]));
-            const double sy = (double) (as + fabs(w[2]));
-            if (sx > mx_x) mx_x = sx;
-            if (sy > mx_y) mx_y = sy;
+                    for (int q = 0; q < 4; q++) sm.FL[q][tid] = xh[q];
+                }
+                if (tid >= 1) {
+#pragma unroll
+                    for (int q = 0; q < 4; q++) sm.FR[q][tid - 1] = xl[q];
+                }
+            }
+            __syncthreads();
+            {
+                const int rc = solve_faces<R, NT>(sm, a.gas, nX + sw);
+                if (rc) err = rc;
+            }
 
-            /* first ghost row below / above the domain: one-sided update */
-            if (r == g) {
-                const long long gi = idx - a.pitch;
+            const long long rowbase = (long long) r * a.pitch;
+            if (inner) {
+                const long long idx = rowbase + col;
+                R gtop[4];
 #pragma unroll
-                for (int q = 0; q < 4; q++)
-                    Uout[q][gi] = Uin[q][gi] - (gbot[ymap[q]] * dtr) * Ay;
-            }
-            if (r == g + ny - 1) {
-                const long long gi = idx + a.pitch;
+                for (int q = 0; q < 4; q++) gtop[q] = sm.FL[q][nX + tid - 1];
+                R Un[4];
 #pragma unroll
-                for (int q = 0; q < 4; q++)
-                    Uout[q][gi] = Uin[q][gi] + (gtop[ymap[q]] * dtr) * Ay;
-            }
-        }
-        /* first ghost column left / right of the domain */
-        if (ghost_xmin) {
-            const long long gi = rowbase + col;
+                for (int q = 0; q < 4; q++) {
+                    R v = Uin[q][idx];
+                    v = v + (sm.FL[q][tid - 1] * dtr) * Ax;
+                    v = v - (sm.FL[q][tid] * dtr) * Ax;
+                    v = v + (gbot[ymap[q]] * dtr) * Ay;
+                    v = v - (gtop[ymap[q]] * dtr) * Ay;
+                    Un[q] = v;
+                    Uout[q][idx] = v;
+                }
+                R w[4];
+                cons_to_prim_2d(a.gas, (R) a.vol, Un[0], Un[1], Un[2], Un[3], w);
+                const R as = sound_speed(a.gas, w[0], w[3]);
 #pragma unroll
-            for (int q = 0; q < 4; q++) Uout[q][gi] = Uin[q][gi] - (fx[q] * dtr) * Ax;
-        }
-        if (ghost_xmax) {
-            const long long gi = rowbase + col;
-#pragma unroll
-            for (int q = 0; q < 4; q++) Uout[q][gi] = Uin[q][gi] + (xfl[q][tid - 1] * dtr) * Ax;
-        }
+                for (int q = 0; q < 4; q++) Wout[q][idx] = w[q];
+                Wout[4][idx] = as;
+                const double sx = (double) (as + fabs(w[1]));
+                const double sy = (double) (as + fabs(w[2]));
+                if (sx > mx_x) mx_x = sx;
+                if (sy > mx_y) mx_y = sy;
 
-        if (inner) {
+                /* first ghost row below / above the domain: one-sided update */
+                if (r == g) {
+                    const long long gi = idx - a.pitch;
 #pragma unroll
-            for (int q = 0; q < 4; q++) { ytop[q] = nhi[q]; gbot[q] = gtop[q]; }
+                    for (int q = 0; q < 4; q++)
+                        Uout[q][gi] = Uin[q][gi] - (gbot[ymap[q]] * dtr) * Ay;
+                }
+                if (r == g + ny - 1) {
+                    const long long gi = idx + a.pitch;
+#pragma unroll
+                    for (int q = 0; q < 4; q++)
+                        Uout[q][gi] = Uin[q][gi] + (gtop[ymap[q]] * dtr) * Ay;
+                }
+#pragma unroll
+                for (int q = 0; q < 4; q++) { ytop[q] = nhi[q]; gbot[q] = gtop[q]; }
+            }
+            /* first ghost column left / right of the domain */
+            if (ghost_xmin) {
+                const long long gi = rowbase + col;
+#pragma unroll
+                for (int q = 0; q < 4; q++) Uout[q][gi] = Uin[q][gi] - (sm.FL[q][0] * dtr) * Ax;
+            }
+            if (ghost_xmax) {
+                const long long gi = rowbase + col;
+#pragma unroll
+                for (int q = 0; q < 4; q++) Uout[q][gi] = Uin[q][gi] + (sm.FL[q][sw] * dtr) * Ax;
+            }
+            __syncthreads();
         }
     }
 
-    if (err) record_error(ctrl, err, c0 + (int) blockIdx.y);
+    if (err) record_error(ctrl, err, (int) blockIdx.x);
 
     /* ---- CTA maxima -> device maxima for the next step's dt ---- */
 #pragma unroll
@@ -351,30 +449,30 @@ __global__ void __launch_bounds__(NT) mh2d_step_kernel(const Mh2dArgs<R> a)
         if (oy > mx_y) mx_y = oy;
     }
     if ((tid & 31) == 0) {
-        red[0][tid >> 5] = mx_x;
-        red[1][tid >> 5] = mx_y;
+        sm.red[0][tid >> 5] = mx_x;
+        sm.red[1][tid >> 5] = mx_y;
     }
     __syncthreads();
     if (tid == 0) {
-        double bx = red[0][0], by = red[1][0];
+        double bx = sm.red[0][0], by = sm.red[1][0];
         for (int w = 1; w < NT / 32; w++) {
-            if (red[0][w] > bx) bx = red[0][w];
-            if (red[1][w] > by) by = red[1][w];
+            if (sm.red[0][w] > bx) bx = sm.red[0][w];
+            if (sm.red[1][w] > by) by = sm.red[1][w];
         }
         const int nxt = (int) ((n + 1) % 3);
         atomicMax(&ctrl->smax[nxt][0], ordered_bits(bx));
         atomicMax(&ctrl->smax[nxt][1], ordered_bits(by));
         __threadfence();
-        const unsigned total = gridDim.x * gridDim.y;
-        am_last = (atomicAdd(&ctrl->blocks_done, 1u) == total - 1);
+        sm.am_last = (atomicAdd(&ctrl->blocks_done, 1u) == gridDim.x - 1);
     }
     __syncthreads();
 
     /* ---- last CTA: advance the clock (src/integrator_muscl_hancock.c:1143-1154) ---- */
-    if (am_last && tid == 0) {
+    if (sm.am_last && tid == 0) {
         __threadfence();
         volatile HydroStepControl *vc = ctrl;
         ctrl->dt = dt;
+        ctrl->work_next = 0;
         if (vc->error_code != 0) {
             ctrl->active = 0;
         } else {

@@ -226,6 +226,119 @@ HD R hllc_q(const GasConst<R> &c, R p_X, R p_star)
 }
 
 /*
+ * HLLC flux, 2D form, in three phases so a caller can batch faces by regime:
+ *
+ *   hllc_classify   sound speeds, the vacuum / vacuum-generation test and the
+ *                   star-pressure guess regime (PVRS, two-rarefaction or
+ *                   two-shock), src/riemann_solver_hllc.c:218-287 and
+ *                   src/riemann_solver.c:154-183;
+ *   guess_p_trrs /
+ *   guess_p_tsrs    the two expensive guesses (src/riemann_solver.c:184-215);
+ *   hllc_finish     the guess floor, wave speeds, S*, and the flux of the
+ *                   region that contains x/t = 0 (src/riemann_solver_hllc.c:289-375).
+ *
+ * The region flux is written once for the selected side K (L for 0 <= S_L
+ * and the left star region, R otherwise): the supersonic fluxes
+ * rho*u*u + p, rho*u*v, u*(E + p) are the same operations as the star
+ * branch's F_K terms, so only the star correction is conditional.
+ * hllc_flux_2d chains the phases and is operation-for-operation the
+ * reference's solve_flux_hllc_2d.
+ */
+enum : int {
+    PREG_VACUUM = 0,
+    PREG_PVRS = 1,
+    PREG_TRRS = 2,
+    PREG_TSRS = 3,
+};
+
+template <class R>
+HD int hllc_classify(const GasConst<R> &c, R rho_L, R u_L, R p_L, R rho_R, R u_R, R p_R,
+                     R &a_L, R &a_R, R &ppv)
+{
+    a_L = (rho_L > R(0)) ? sound_speed(c, rho_L, p_L) : R(0);
+    a_R = (rho_R > R(0)) ? sound_speed(c, rho_R, p_R) : R(0);
+    ppv = R(0);
+    if (rho_L <= R(0) || rho_R <= R(0) || ((a_L + a_R) * R(2) / c.gp1) <= (u_R - u_L))
+        return PREG_VACUUM;
+    const R p_min = (p_L > p_R) ? p_R : p_L;
+    const R p_max = (p_L > p_R) ? p_L : p_R;
+    ppv = R(0.5) * (p_L + p_R) - R(0.125) * (u_R - u_L) * (rho_L + rho_R) * (a_L + a_R);
+    if (p_max / p_min <= R(2) && (p_min <= ppv && ppv <= p_max)) return PREG_PVRS;
+    if (ppv < p_min) return PREG_TRRS;
+    return PREG_TSRS;
+}
+
+template <class R>
+HD R guess_p_trrs(const GasConst<R> &c, R u_L, R p_L, R a_L, R u_R, R p_R, R a_R)
+{
+    const R pg = (a_L + a_R - c.half_gm1 * (u_R - u_L))
+               / (a_L / pow(p_L, c.half_gm1_g) + a_R / pow(p_R, c.half_gm1_g));
+    return pow(pg, c.g_half_gm1);
+}
+
+template <class R>
+HD R guess_p_tsrs(const GasConst<R> &c, R rho_L, R u_L, R p_L, R rho_R, R u_R, R p_R, R ppv)
+{
+    const R gL = sqrt((R(2) / (c.gp1 * rho_L)) / (ppv + p_L * c.gm1_gp1));
+    const R gR = sqrt((R(2) / (c.gp1 * rho_R)) / (ppv + p_R * c.gm1_gp1));
+    return (gL * p_L + gR * p_R - (u_R - u_L)) / (gL + gR);
+}
+
+/* Flux of the vacuum / vacuum-generation case (src/riemann_solver_hllc.c:249-287). */
+template <class R>
+HD void hllc_vacuum_flux(const GasConst<R> &c, R rho_L, R u_L, R v_L, R p_L, R a_L,
+                         R rho_R, R u_R, R v_R, R p_R, R a_R, R F[4])
+{
+    R s[4];
+    solve_vacuum(c, rho_L, u_L, v_L, p_L, a_L, rho_R, u_R, v_R, p_R, a_R, R(0), s);
+    const R E = s[0] * (R(0.5) * (s[1] * s[1] + s[2] * s[2]) + s[3] / (s[0] * c.gm1));
+    F[0] = s[0] * s[1];
+    F[1] = s[0] * s[1] * s[1] + s[3];
+    F[2] = s[0] * s[1] * s[2];
+    F[3] = s[1] * (E + s[3]);
+}
+
+/* From the (unfloored) star-pressure guess to the flux.  Returns DEV_OK or
+ * DEV_ERR_HLLC_WAVE_SPEED. */
+template <class R>
+HD int hllc_finish(const GasConst<R> &c, R rho_L, R u_L, R v_L, R p_L, R a_L,
+                   R rho_R, R u_R, R v_R, R p_R, R a_R, R pg, R F[4])
+{
+    const R ps = (pg < c.tol) ? c.tol : pg;
+    const R S_L = u_L - a_L * hllc_q(c, p_L, ps);
+    const R S_R = u_R + a_R * hllc_q(c, p_R, ps);
+    const R S_s = (p_R - p_L + rho_L * u_L * (S_L - u_L) - rho_R * u_R * (S_R - u_R))
+                / (rho_L * (S_L - u_L) - rho_R * (S_R - u_R));
+    int region;
+    if (R(0) <= S_L) region = 0;
+    else if (S_L <= R(0) && R(0) <= S_s) region = 1;
+    else if (S_s <= R(0) && R(0) <= S_R) region = 2;
+    else if (S_R <= R(0)) region = 3;
+    else return DEV_ERR_HLLC_WAVE_SPEED;
+    const bool left = region <= 1;
+    const R rho = left ? rho_L : rho_R;
+    const R u = left ? u_L : u_R;
+    const R v = left ? v_L : v_R;
+    const R p = left ? p_L : p_R;
+    const R E = rho * (R(0.5) * (u * u + v * v) + p / (rho * c.gm1));
+    const R fm = rho * u;
+    F[0] = fm;
+    F[1] = fm * u + p;
+    F[2] = fm * v;
+    F[3] = u * (E + p);
+    if (region == 1 || region == 2) {
+        const R S = left ? S_L : S_R;
+        const R rs = rho * (S - u) / (S - S_s);
+        const R es = rs * (E / rho + (S_s - u) * (S_s + p / (rho * (S - u))));
+        F[0] = fm + S * (rs - rho);
+        F[1] = F[1] + S * (rs * S_s - rho * u);
+        F[2] = F[2] + S * (rs * v - rho * v);
+        F[3] = F[3] + S * (es - E);
+    }
+    return DEV_OK;
+}
+
+/*
  * HLLC flux, 2D form.  (u = normal velocity, v = tangential.)  F receives
  * (mass, normal momentum, tangential momentum, energy).  Returns DEV_OK or
  * DEV_ERR_HLLC_WAVE_SPEED (no branch matched, i.e. a NaN wave speed).
@@ -234,62 +347,16 @@ template <class R>
 HD int hllc_flux_2d(const GasConst<R> &c, R rho_L, R u_L, R v_L, R p_L,
                     R rho_R, R u_R, R v_R, R p_R, R F[4])
 {
-    const R a_L = (rho_L > R(0)) ? sound_speed(c, rho_L, p_L) : R(0);
-    const R a_R = (rho_R > R(0)) ? sound_speed(c, rho_R, p_R) : R(0);
-    if (rho_L <= R(0) || rho_R <= R(0) || ((a_L + a_R) * R(2) / c.gp1) <= (u_R - u_L)) {
-        R s[4];
-        solve_vacuum(c, rho_L, u_L, v_L, p_L, a_L, rho_R, u_R, v_R, p_R, a_R, R(0), s);
-        const R E = s[0] * (R(0.5) * (s[1] * s[1] + s[2] * s[2]) + s[3] / (s[0] * c.gm1));
-        F[0] = s[0] * s[1];
-        F[1] = s[0] * s[1] * s[1] + s[3];
-        F[2] = s[0] * s[1] * s[2];
-        F[3] = s[1] * (E + s[3]);
+    R a_L, a_R, ppv;
+    const int reg = hllc_classify(c, rho_L, u_L, p_L, rho_R, u_R, p_R, a_L, a_R, ppv);
+    if (reg == PREG_VACUUM) {
+        hllc_vacuum_flux(c, rho_L, u_L, v_L, p_L, a_L, rho_R, u_R, v_R, p_R, a_R, F);
         return DEV_OK;
     }
-    const R ps = guess_p(c, rho_L, u_L, p_L, a_L, rho_R, u_R, p_R, a_R);
-    const R S_L = u_L - a_L * hllc_q(c, p_L, ps);
-    const R S_R = u_R + a_R * hllc_q(c, p_R, ps);
-    const R S_s = (p_R - p_L + rho_L * u_L * (S_L - u_L) - rho_R * u_R * (S_R - u_R))
-                / (rho_L * (S_L - u_L) - rho_R * (S_R - u_R));
-    if (R(0) <= S_L) {
-        const R E = rho_L * (R(0.5) * (u_L * u_L + v_L * v_L) + p_L / (rho_L * c.gm1));
-        F[0] = rho_L * u_L;
-        F[1] = rho_L * u_L * u_L + p_L;
-        F[2] = rho_L * u_L * v_L;
-        F[3] = u_L * (E + p_L);
-        return DEV_OK;
-    }
-    if (S_L <= R(0) && R(0) <= S_s) {
-        const R E = rho_L * (R(0.5) * (u_L * u_L + v_L * v_L) + p_L / (rho_L * c.gm1));
-        const R fm = rho_L * u_L;
-        const R rs = rho_L * (S_L - u_L) / (S_L - S_s);
-        const R es = rs * (E / rho_L + (S_s - u_L) * (S_s + p_L / (rho_L * (S_L - u_L))));
-        F[0] = fm + S_L * (rs - rho_L);
-        F[1] = (fm * u_L + p_L) + S_L * (rs * S_s - rho_L * u_L);
-        F[2] = fm * v_L + S_L * (rs * v_L - rho_L * v_L);
-        F[3] = u_L * (E + p_L) + S_L * (es - E);
-        return DEV_OK;
-    }
-    if (S_s <= R(0) && R(0) <= S_R) {
-        const R E = rho_R * (R(0.5) * (u_R * u_R + v_R * v_R) + p_R / (rho_R * c.gm1));
-        const R fm = rho_R * u_R;
-        const R rs = rho_R * (S_R - u_R) / (S_R - S_s);
-        const R es = rs * (E / rho_R + (S_s - u_R) * (S_s + p_R / (rho_R * (S_R - u_R))));
-        F[0] = fm + S_R * (rs - rho_R);
-        F[1] = (fm * u_R + p_R) + S_R * (rs * S_s - rho_R * u_R);
-        F[2] = fm * v_R + S_R * (rs * v_R - rho_R * v_R);
-        F[3] = u_R * (E + p_R) + S_R * (es - E);
-        return DEV_OK;
-    }
-    if (S_R <= R(0)) {
-        const R E = rho_R * (R(0.5) * (u_R * u_R + v_R * v_R) + p_R / (rho_R * c.gm1));
-        F[0] = rho_R * u_R;
-        F[1] = rho_R * u_R * u_R + p_R;
-        F[2] = rho_R * u_R * v_R;
-        F[3] = u_R * (E + p_R);
-        return DEV_OK;
-    }
-    return DEV_ERR_HLLC_WAVE_SPEED;
+    R pg = ppv;
+    if (reg == PREG_TRRS) pg = guess_p_trrs(c, u_L, p_L, a_L, u_R, p_R, a_R);
+    else if (reg == PREG_TSRS) pg = guess_p_tsrs(c, rho_L, u_L, p_L, rho_R, u_R, p_R, ppv);
+    return hllc_finish(c, rho_L, u_L, v_L, p_L, a_L, rho_R, u_R, v_R, p_R, a_R, pg, F);
 }
 
 /* HLLC flux, 1D form (energy density groups 0.5*u*u as (0.5*u)*u). */

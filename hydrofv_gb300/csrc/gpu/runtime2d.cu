@@ -152,7 +152,7 @@ extern "C" int hydro_run2d_create(const HydroGrid2D *grid, const HydroGpuOptions
     a.g = grid->g;
     a.pitch = run->tx;
     a.strip_w = MH2D_THREADS - 2;
-    a.chunk_h = opt->chunk_rows > 0 ? opt->chunk_rows : 64;
+    a.chunk_h = opt->chunk_rows > 0 ? opt->chunk_rows : 32;
     for (int s = 0; s < 4; s++) a.bc[s] = grid->bc[s];
     a.dx = grid->dx;
     a.dy = grid->dy;
@@ -160,6 +160,7 @@ extern "C" int hydro_run2d_create(const HydroGrid2D *grid, const HydroGpuOptions
     a.area_y = grid->area_y;
     a.vol = grid->vol;
     a.first_order = (grid->integrator == INTEGRATOR_GODUNOV_FIRST_ORDER_2D) ? 1 : 0;
+    a.grid_ctas = mh2d_resident_ctas<double>(grid->limiter, a.first_order, run->device);
     return 0;
 }
 

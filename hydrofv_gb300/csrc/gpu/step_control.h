@@ -26,6 +26,7 @@ typedef struct HydroStepControl {
     int error_code;                /* first device error (hydro::DEV_ERR_*) */
     int error_cell;                /* padded index (or face) where it happened */
     unsigned int blocks_done;      /* last-CTA-done counter, reset every step */
+    int work_next;                 /* next (strip, row chunk) item of the step, reset every step */
     int store_count;               /* snapshots stored so far (StoringParam.store_count_) */
     double tf;                     /* stop once t >= tf (the dt is clipped to it) */
     long long max_steps;           /* stop once num_steps reaches it; < 0: no limit */
