@@ -35,6 +35,8 @@ import subprocess
 import sys
 import time
 
+import numpy as np
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
@@ -73,6 +75,7 @@ class ClockSampler:
     def __init__(self, device: int):
         self.device = device
         self.proc = None
+        self.fh = None
         self.path = os.path.join(ROOT, "gpurun_out", f"clocks_bench_{os.getpid()}.csv")
 
     def __enter__(self):
@@ -210,6 +213,13 @@ def main() -> None:
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--size", type=int, default=N_SIDE,
                     help="grid side (the headline workload is 2048; smaller sizes are for profiling)")
+    ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"],
+                    help="state precision of the timed path (fp64 is the drop-in)")
+    ap.add_argument("--workload", default="shear_layer", choices=["shear_layer", "point_blast"],
+                    help="shear_layer: MC, periodic, CFL 0.8; point_blast: Van Leer, reflective, CFL 0.4")
+    ap.add_argument("--compare", action="store_true",
+                    help="also run the other precision on the same steps and report the relative "
+                         "L1 error per field and the conserved-total drift of both")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.size != N_SIDE:
@@ -228,35 +238,62 @@ def main() -> None:
     if not os.path.exists(H.LIB_PATH):
         from hydrofv_gb300 import build as B
         B.build()
-    from hydrofv_gb300.problems import shear_layer
+    from hydrofv_gb300.problems import point_blast, shear_layer
 
     device = local
-    opts = H.default_options(device=device)
-    p = shear_layer(N_SIDE, steps=args.steps)
+    prec = H.PRECISION_FP32 if args.precision == "fp32" else H.PRECISION_FP64
+    make = shear_layer if args.workload == "shear_layer" else point_blast
+    p = make(N_SIDE, steps=args.steps)
     bounds = (p.x_min, p.x_max, p.y_min, p.y_max)
     cells = p.nx * p.ny
+    bytes_per_cell = BYTES_PER_CELL_FP64 if prec == H.PRECISION_FP64 else BYTES_PER_CELL_FP64 // 2
+
+    def session(precision):
+        return H.Solver2D(p.nx, p.ny, p.g, bounds, p.gamma, p.W, p.U, bc=p.bc,
+                          slope_limiter=p.slope_limiter, cfl=p.cfl,
+                          options=H.default_options(device=device, precision=precision))
+
+    def timed_run(precision, sampler=None):
+        """W warm-up steps, rewind, K timed steps; returns (ms, launches, W, U, drift)."""
+        with session(precision) as s:
+            s.advance(args.warmup)
+            s.restart()
+            tot0 = s.conserved_totals()
+            l0 = s.kernel_launches()
+            barrier(ws)
+            if sampler is not None:
+                with sampler:
+                    st, ms = s.advance(args.steps)
+            else:
+                st, ms = s.advance(args.steps)
+            launches = s.kernel_launches() - l0
+            assert st.num_steps == args.steps, st.num_steps
+            tot1 = s.conserved_totals()
+            W, U = s.download()
+        drift = ((tot1 - tot0) / np.where(tot0 != 0, np.abs(tot0), 1.0)).tolist()
+        return ms, launches, W, U, {"mass": drift[0], "energy": drift[3]}
 
     # ---- device-resident value ----
-    solver = H.Solver2D(p.nx, p.ny, p.g, bounds, p.gamma, p.W, p.U, bc=p.bc,
-                        slope_limiter=p.slope_limiter, cfl=p.cfl, options=opts)
-    solver.advance(args.warmup)
-    solver.restart()
-    launches0 = solver.kernel_launches()
-    barrier(ws)
-    with ClockSampler(device) as clk:
-        st, step_ms = solver.advance(args.steps)
-    launches = solver.kernel_launches() - launches0
-    solver.close()
-    assert st.num_steps == args.steps, st.num_steps
+    clk = ClockSampler(device)
+    step_ms, launches, W_main, U_main, drift_main = timed_run(prec, clk)
     step_ms = max_over_ranks(step_ms, ws)
     value = ws * cells * args.steps / (step_ms * 1e-3)
+
+    # ---- the other precision on the same steps: L1 error of the FP32 form ----
+    other = H.PRECISION_FP32 if prec == H.PRECISION_FP64 else H.PRECISION_FP64
+    ms_o, _, W_o, U_o, drift_o = timed_run(other)
+    W64, W32 = (W_main, W_o) if prec == H.PRECISION_FP64 else (W_o, W_main)
+    g = p.g
+    l1 = (np.abs(W32[:, g:-g, g:-g] - W64[:, g:-g, g:-g]).sum(axis=(1, 2))
+          / np.abs(W64[:, g:-g, g:-g]).sum(axis=(1, 2)))
+    del W_main, U_main, W_o, U_o
 
     # ---- end to end through the drop-in call (host arrays in and out) ----
     barrier(ws)
     t0 = time.perf_counter()
     r = H.run_2d(p.nx, p.ny, p.g, bounds, p.gamma, p.W, p.U, bc=p.bc,
                  slope_limiter=p.slope_limiter, cfl=p.cfl, tf=p.tf, max_steps=args.steps,
-                 options=H.default_options(device=device))
+                 options=H.default_options(device=device, precision=prec))
     e2e_s = time.perf_counter() - t0
     assert r.code == 0, r.message
     e2e_s = max_over_ranks(e2e_s, ws)
@@ -267,26 +304,43 @@ def main() -> None:
 
     pk = peaks()
     per_launch_s = step_ms * 1e-3 / args.steps
-    achieved_gbs = BYTES_PER_CELL_FP64 * cells / per_launch_s / 1e9
+    achieved_gbs = bytes_per_cell * cells / per_launch_s / 1e9
     fp64_tflops, fp32_tflops = H.calibrate(device)
-    traffic = profile_traffic()
+    traffic = profile_traffic() if (prec == H.PRECISION_FP64 and args.workload == "shear_layer"
+                                    and N_SIDE == 2048) else None
+    fp32_ms = step_ms if prec == H.PRECISION_FP32 else ms_o
+    fp64_ms = step_ms if prec == H.PRECISION_FP64 else ms_o
     line = {
         "metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms / args.steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic (seeded shear layer)",
-        "config": {"workload": WORKLOAD, "grid": [N_SIDE, N_SIDE], "ghost_cells": 2,
-                   "limiter": "monotonized_central", "cfl": 0.8, "steps_per_run": args.steps,
-                   "l2": "state 0.74 GB > 129 MB L2 (no flush needed)",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if prec == H.PRECISION_FP64 else "f32",
+        "data": f"synthetic (seeded {args.workload})",
+        "config": {"workload": WORKLOAD if args.workload == "shear_layer" and prec == H.PRECISION_FP64
+                   else f"{args.workload}_{N_SIDE}x{N_SIDE}_{args.precision}",
+                   "grid": [N_SIDE, N_SIDE], "ghost_cells": 2,
+                   "limiter": p.slope_limiter, "cfl": p.cfl, "boundaries": p.bc[0],
+                   "steps_per_run": args.steps,
+                   "l2": "state larger than the 129 MB L2 (no flush needed)" if cells >= 1 << 20
+                         else "state fits in L2 (profiling size)",
                    "parallelism": "replicas" if ws > 1 else "single"},
         "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": pk["hbm_gbs"],
                      "unit": "GB/s", "frac": achieved_gbs / pk["hbm_gbs"],
                      "traffic": traffic, "peak_source": pk["source"],
-                     "bytes_per_cell_update": BYTES_PER_CELL_FP64},
-        "fp_roofline": {"bound": "fp64_pipe", "peak_tflops_fp64": fp64_tflops,
-                        "peak_tflops_fp32": fp32_tflops,
+                     "bytes_per_cell_update": bytes_per_cell},
+        "fp_roofline": {"bound": "fp64_pipe" if prec == H.PRECISION_FP64 else "fp32_pipe",
+                        "peak_tflops_fp64": fp64_tflops, "peak_tflops_fp32": fp32_tflops,
                         "note": "peaks measured by hydro_gpu_calibrate (FMA chains); "
                                 "FP64 instruction counts per launch are in profiles/"},
+        "forms": {
+            "fp64": {"value": cells * args.steps / (fp64_ms * 1e-3), "ms_per_step": fp64_ms / args.steps,
+                     "conserved_drift": drift_main if prec == H.PRECISION_FP64 else drift_o},
+            "fp32": {"value": cells * args.steps / (fp32_ms * 1e-3), "ms_per_step": fp32_ms / args.steps,
+                     "speedup_vs_fp64": fp64_ms / fp32_ms,
+                     "rel_l1_vs_fp64": {"density": l1[0], "velocity_x": l1[1],
+                                        "velocity_y": l1[2], "pressure": l1[3]},
+                     "conserved_drift": drift_main if prec == H.PRECISION_FP32 else drift_o},
+        },
         "e2e": {"value": e2e_value, "unit": "cell-updates/s",
                 "h2d_bytes_per_step": r.stats["h2d_bytes"] / args.steps,
                 "d2h_bytes_per_step": r.stats["d2h_bytes"] / args.steps,

@@ -143,6 +143,7 @@ _SIGNATURES = {
                                                _P(SimulationStatus), _P(C.c_double)]),
     "hydro_gpu_solver_download": (ErrorStatus, [C.c_void_p, _P(System)]),
     "hydro_gpu_solver_kernel_launches": (C.c_int64, [C.c_void_p]),
+    "hydro_gpu_solver_conserved_totals": (ErrorStatus, [C.c_void_p, _dp]),
     "hydro_gpu_solver_destroy": (None, [C.c_void_p]),
     "hydro_gpu_device_count": (C.c_int, []),
     "hydro_gpu_calibrate": (C.c_int, [C.c_int, _dp, _dp]),
@@ -409,6 +410,15 @@ class Solver2D:
         W = np.stack([f.copy() for f in self._h.fields(W2)]).reshape((4,) + self._h.shape)
         U = np.stack([f.copy() for f in self._h.fields(U2)]).reshape((4,) + self._h.shape)
         return W, U
+
+    def conserved_totals(self) -> np.ndarray:
+        """(mass, mom_x, mom_y, energy) over the interior, FP64 compensated sums."""
+        out = np.zeros(4)
+        code, msg = _consume(self.lib, self.lib.hydro_gpu_solver_conserved_totals(
+            self.handle, out.ctypes.data_as(_dp)))
+        if code != 0:
+            raise HydroError(code, msg)
+        return out
 
     def kernel_launches(self) -> int:
         return int(self.lib.hydro_gpu_solver_kernel_launches(self.handle))

@@ -30,6 +30,7 @@ INCLUDES = ["-I" + os.path.join(ROOT, "include"), "-I" + os.path.join(CSRC, "gpu
 # (source, extra nvcc flags)
 CUDA_SOURCES = [
     ("gpu/mh2d.cu", ["--fmad=false"]),
+    ("gpu/mh2d_fp32.cu", []),
     ("gpu/runtime2d.cu", []),
     ("gpu/host_numerics.cu", ["--fmad=false"]),
     ("gpu/calibrate.cu", []),

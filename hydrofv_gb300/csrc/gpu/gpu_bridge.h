@@ -72,6 +72,9 @@ int hydro_run2d_advance(HydroRun2D *run, HydroSnapshotFn snap, void *ctx,
 /* Full padded W (ghosts filled) and U of the current state into host arrays. */
 int hydro_run2d_download(HydroRun2D *run, double *const W[4], double *const U[4],
                          HydroRunOutcome *oc);
+/* Conserved totals (mass, mom_x, mom_y, energy) over the interior of the
+ * current state, summed in FP64 with Neumaier compensation. */
+int hydro_run2d_totals(HydroRun2D *run, double totals[4], HydroRunOutcome *oc);
 void hydro_run2d_stats(const HydroRun2D *run, HydroGpuStats *stats);
 void hydro_run2d_destroy(HydroRun2D *run);
 

@@ -1,144 +1,18 @@
 /*
- * mh2d.cu -- instantiations and launchers of the 2D MUSCL-Hancock step, plus
- * the two helper kernels around a run:
- *
- *   mh2d_prepare_kernel     sound speed of the caller's primitives and the
- *                           first step's CFL maxima (src/utils.c:55-95 on the
- *                           W arrays as handed to launch_simulation);
- *   mh2d_materialize_kernel full padded W (interior, ghost fill, corners) for
- *                           snapshots and for the arrays handed back to the
- *                           caller (src/system.c:763-802 then
- *                           src/boundary.c:513-777).
+ * mh2d.cu -- FP64 instantiations of the 2D step and its helper kernels.
  *
  * Compiled with --fmad=false: the FP64 path must issue the same IEEE
  * operations as the reference CPU code, which never contracts a*b+c.
  */
-#include <cuda_runtime.h>
-
-#include "gpu_internal.h"
-#include "mh2d_kernel.cuh"
+#include "mh2d_launch.cuh"
 
 namespace hydro {
-
-template <class R>
-__global__ void mh2d_prepare_kernel(const Mh2dArgs<R> a)
-{
-    const int tx = a.nx + 2 * a.g, ty = a.ny + 2 * a.g;
-    const long long total = (long long) tx * ty;
-    double mx = -CUDART_INF, my = -CUDART_INF;
-    R *const *W = a.W[0];
-    for (long long k = blockIdx.x * (long long) blockDim.x + threadIdx.x; k < total;
-         k += (long long) gridDim.x * blockDim.x) {
-        const int r = (int) (k / tx), c = (int) (k % tx);
-        const long long idx = (long long) r * a.pitch + c;
-        const R as = sound_speed(a.gas, W[0][idx], W[3][idx]);
-        W[4][idx] = as;
-        if (r >= a.g && r < a.g + a.ny && c >= a.g && c < a.g + a.nx) {
-            const double sx = (double) (as + fabs(W[1][idx]));
-            const double sy = (double) (as + fabs(W[2][idx]));
-            if (sx > mx) mx = sx;
-            if (sy > my) my = sy;
-        }
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        const double ox = __shfl_xor_sync(0xffffffffu, mx, o);
-        const double oy = __shfl_xor_sync(0xffffffffu, my, o);
-        if (ox > mx) mx = ox;
-        if (oy > my) my = oy;
-    }
-    if ((threadIdx.x & 31) == 0) {
-        atomicMax(&a.ctrl->smax[0][0], ordered_bits(mx));
-        atomicMax(&a.ctrl->smax[0][1], ordered_bits(my));
-    }
-}
-
-template <class R>
-__global__ void mh2d_materialize_kernel(const Mh2dArgs<R> a, int buf, R *out0, R *out1,
-                                        R *out2, R *out3)
-{
-    const int tx = a.nx + 2 * a.g, ty = a.ny + 2 * a.g;
-    const long long total = (long long) tx * ty;
-    const R *const *U = a.U[buf];
-    const R *const *W = a.W[buf];
-    R *out[4] = { out0, out1, out2, out3 };
-    for (long long k = blockIdx.x * (long long) blockDim.x + threadIdx.x; k < total;
-         k += (long long) gridDim.x * blockDim.x) {
-        const int r = (int) (k / tx), c = (int) (k % tx);
-        const long long idx = (long long) r * a.pitch + c;
-        const bool in_x = c >= a.g && c < a.g + a.nx;
-        const bool in_y = r >= a.g && r < a.g + a.ny;
-        R w[5];
-        if (!in_x && !in_y) {
-            /* corners: converted, never overwritten by a boundary routine */
-            cons_to_prim_2d(a.gas, (R) a.vol, U[0][idx], U[1][idx], U[2][idx], U[3][idx], w);
-        } else {
-            fetch_w(a, W, U, false, r, c, w);
-        }
-#pragma unroll
-        for (int q = 0; q < 4; q++) out[q][k] = w[q];
-    }
-}
-
-/* ------------------------------------------------------------- launchers */
-
-template <class R, int LIM, int FIRST_ORDER>
-static cudaError_t launch_step_lim(const Mh2dArgs<R> &a, int grid, cudaStream_t s)
-{
-    mh2d_step_kernel<R, LIM, MH2D_THREADS, FIRST_ORDER><<<grid, MH2D_THREADS, 0, s>>>(a);
-    return cudaGetLastError();
-}
-
-template <class R>
-cudaError_t mh2d_launch_step(const Mh2dArgs<R> &a, int limiter, cudaStream_t s)
-{
-    const int n_items = ((a.nx + a.strip_w - 1) / a.strip_w) * ((a.ny + a.chunk_h - 1) / a.chunk_h);
-    const int grid = (a.grid_ctas > 0 && a.grid_ctas < n_items) ? a.grid_ctas : n_items;
-    if (a.first_order) return launch_step_lim<R, LIM_MINMOD, 1>(a, grid, s);
-    switch (limiter) {
-    case LIM_MINMOD: return launch_step_lim<R, LIM_MINMOD, 0>(a, grid, s);
-    case LIM_VAN_LEER: return launch_step_lim<R, LIM_VAN_LEER, 0>(a, grid, s);
-    default: return launch_step_lim<R, LIM_MC, 0>(a, grid, s);
-    }
-}
-
-template <class R>
-cudaError_t mh2d_launch_prepare(const Mh2dArgs<R> &a, cudaStream_t s)
-{
-    mh2d_prepare_kernel<R><<<1024, 256, 0, s>>>(a);
-    return cudaGetLastError();
-}
-
-template <class R>
-cudaError_t mh2d_launch_materialize(const Mh2dArgs<R> &a, int buf, R *const out[4], cudaStream_t s)
-{
-    mh2d_materialize_kernel<R><<<1024, 256, 0, s>>>(a, buf, out[0], out[1], out[2], out[3]);
-    return cudaGetLastError();
-}
-
-/* CTAs of the step kernel that fit on the device at once. */
-template <class R>
-int mh2d_resident_ctas(int limiter, int first_order, int device)
-{
-    int per_sm = 0, sms = 0;
-    cudaError_t e;
-    if (first_order)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mh2d_step_kernel<R, LIM_MINMOD, MH2D_THREADS, 1>, MH2D_THREADS, 0);
-    else if (limiter == LIM_MINMOD)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mh2d_step_kernel<R, LIM_MINMOD, MH2D_THREADS, 0>, MH2D_THREADS, 0);
-    else if (limiter == LIM_VAN_LEER)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mh2d_step_kernel<R, LIM_VAN_LEER, MH2D_THREADS, 0>, MH2D_THREADS, 0);
-    else
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mh2d_step_kernel<R, LIM_MC, MH2D_THREADS, 0>, MH2D_THREADS, 0);
-    if (e != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess)
-        return 0;
-    return per_sm * sms;
-}
 
 template int mh2d_resident_ctas<double>(int, int, int);
 template cudaError_t mh2d_launch_step<double>(const Mh2dArgs<double> &, int, cudaStream_t);
 template cudaError_t mh2d_launch_prepare<double>(const Mh2dArgs<double> &, cudaStream_t);
 template cudaError_t mh2d_launch_materialize<double>(const Mh2dArgs<double> &, int,
                                                      double *const[4], cudaStream_t);
+template cudaError_t mh2d_launch_totals<double>(const Mh2dArgs<double> &, int, double *, cudaStream_t);
 
 }  // namespace hydro

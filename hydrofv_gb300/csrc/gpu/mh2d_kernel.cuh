@@ -100,7 +100,7 @@ __device__ __forceinline__ void fetch_w(const Mh2dArgs<R> &a, const R *const *Wi
     }
     const long long idx = (long long) rr * a.pitch + cc;
     if (cons) {
-        cons_to_prim_2d(a.gas, (R) a.vol, Uin[0][idx], Uin[1][idx], Uin[2][idx], Uin[3][idx], w);
+        cons_to_prim_2d_guarded(a.gas, (R) a.vol, Uin[0][idx], Uin[1][idx], Uin[2][idx], Uin[3][idx], w);
         w[4] = sound_speed(a.gas, w[0], w[3]);
         return;
     }
@@ -397,7 +397,7 @@ __global__ void __launch_bounds__(NT, 4) mh2d_step_kernel(const Mh2dArgs<R> a)
                     Uout[q][idx] = v;
                 }
                 R w[4];
-                cons_to_prim_2d(a.gas, (R) a.vol, Un[0], Un[1], Un[2], Un[3], w);
+                cons_to_prim_2d_guarded(a.gas, (R) a.vol, Un[0], Un[1], Un[2], Un[3], w);
                 const R as = sound_speed(a.gas, w[0], w[3]);
 #pragma unroll
                 for (int q = 0; q < 4; q++) Wout[q][idx] = w[q];

@@ -654,6 +654,24 @@ HD void cons_to_prim_2d(const GasConst<R> &c, R vol, R m, R mx, R my, R E, R w[4
     w[3] = c.gm1 * (E - R(0.5) * m * (w[1] * w[1] + w[2] * w[2])) / vol;
 }
 
+/* FP32 state: the same conversion, except that where the kinetic energy is
+ * more than half of the total energy (E - KE loses at least one bit to
+ * cancellation, more as KE -> E) the pressure is recovered in FP64 from the
+ * stored conserved values.  For FP64 state this is cons_to_prim_2d. */
+template <class R>
+HD void cons_to_prim_2d_guarded(const GasConst<R> &c, R vol, R m, R mx, R my, R E, R w[4])
+{
+    cons_to_prim_2d(c, vol, m, mx, my, E, w);
+    if (sizeof(R) == 4) {
+        const R ke = R(0.5) * m * (w[1] * w[1] + w[2] * w[2]);
+        if (ke > R(0.5) * E) {
+            const double md = (double) m, ud = (double) mx / md, vd = (double) my / md;
+            const double pd = ((double) c.gm1) * ((double) E - 0.5 * md * (ud * ud + vd * vd)) / (double) vol;
+            w[3] = (R) pd;
+        }
+    }
+}
+
 /* Ordered-bits encoding of a double, monotone for every non-NaN value, so a
  * device-wide maximum is one unsigned 64-bit atomicMax. */
 HD unsigned long long ordered_bits(double x)

@@ -64,18 +64,23 @@ struct HydroRun2D {
     HydroGrid2D grid{};
     HydroGpuOptions opt{};
     int device = 0;
+    int fp32 = 0;                   /* state precision: 0 FP64 (drop-in), 1 FP32 */
+    size_t elem = sizeof(double);   /* bytes per state value */
     cudaStream_t stream = nullptr;
     int tx = 0, ty = 0;
     size_t ncell = 0;
-    double *slab = nullptr;
-    double *init_slab = nullptr;    /* initial U and W, kept for rewinding */
-    double *init_U[4] = {};
-    double *init_W[4] = {};
-    double *snap_d[4] = {};
+    void *slab = nullptr;
+    void *init_slab = nullptr;      /* initial U and W, kept for rewinding */
+    void *init_U[4] = {};
+    void *init_W[4] = {};
+    void *snap_d[4] = {};           /* materialized W (state precision) */
+    double *stage_d = nullptr;      /* FP32 form: FP64 staging for transfers (4 fields) */
+    double *totals_d = nullptr;     /* conserved totals (4 doubles) */
     double *snap_h = nullptr;       /* pinned, 4 * ncell */
     HydroStepControl *ctrl_d = nullptr;
     HydroStepControl *ctrl_h = nullptr;   /* pinned */
     Mh2dArgs<double> args{};
+    Mh2dArgs<float> args32{};
     cudaGraphExec_t graph = nullptr;
     cudaEvent_t ev[6] = {};
     bool begun = false;
@@ -92,6 +97,45 @@ static void fill_outcome(const HydroRun2D *run, HydroRunOutcome *oc)
     oc->t = run->ctrl_h->t;
     oc->dt = run->ctrl_h->dt;
     oc->store_count = run->ctrl_h->store_count;
+}
+
+/* Point the per-field arrays of `a` into the slab. */
+template <class R>
+static void carve(HydroRun2D *run, Mh2dArgs<R> &a)
+{
+    R *p = static_cast<R *>(run->slab);
+    for (int b = 0; b < 2; b++)
+        for (int q = 0; q < 4; q++) { a.U[b][q] = p; p += run->ncell; }
+    for (int b = 0; b < 2; b++)
+        for (int q = 0; q < 5; q++) { a.W[b][q] = p; p += run->ncell; }
+    for (int q = 0; q < 4; q++) { run->snap_d[q] = p; p += run->ncell; }
+}
+
+template <class R>
+static void setup_args(HydroRun2D *run, Mh2dArgs<R> &a, const HydroGrid2D *grid, const HydroGpuOptions *opt)
+{
+    a.ctrl = run->ctrl_d;
+    a.gas = make_gas_const<R>(grid->gamma, grid->tol);
+    a.nx = grid->nx;
+    a.ny = grid->ny;
+    a.g = grid->g;
+    a.pitch = run->tx;
+    a.strip_w = MH2D_THREADS - 2;
+    a.chunk_h = opt->chunk_rows > 0 ? opt->chunk_rows : 32;
+    for (int s = 0; s < 4; s++) a.bc[s] = grid->bc[s];
+    a.dx = grid->dx;
+    a.dy = grid->dy;
+    a.area_x = grid->area_x;
+    a.area_y = grid->area_y;
+    a.vol = grid->vol;
+    a.first_order = (grid->integrator == INTEGRATOR_GODUNOV_FIRST_ORDER_2D) ? 1 : 0;
+    a.grid_ctas = mh2d_resident_ctas<R>(grid->limiter, a.first_order, run->device);
+}
+
+static cudaError_t launch_step(HydroRun2D *run)
+{
+    return run->fp32 ? mh2d_launch_step<float>(run->args32, run->grid.limiter, run->stream)
+                     : mh2d_launch_step<double>(run->args, run->grid.limiter, run->stream);
 }
 
 extern "C" int hydro_run2d_create(const HydroGrid2D *grid, const HydroGpuOptions *opt,
@@ -113,6 +157,11 @@ extern "C" int hydro_run2d_create(const HydroGrid2D *grid, const HydroGpuOptions
                  "direction (got %d x %d, G = %d).", grid->nx, grid->ny, grid->g);
         return -1;
     }
+    if (opt->precision != HYDRO_GPU_PRECISION_FP64 && opt->precision != HYDRO_GPU_PRECISION_FP32) {
+        oc->kind = HYDRO_RUN_UNSUPPORTED;
+        snprintf(oc->message, sizeof oc->message, "Unknown precision %d.", opt->precision);
+        return -1;
+    }
     HydroRun2D *run = new (std::nothrow) HydroRun2D();
     if (!run) {
         oc->kind = HYDRO_RUN_CUDA_ERROR;
@@ -122,6 +171,8 @@ extern "C" int hydro_run2d_create(const HydroGrid2D *grid, const HydroGpuOptions
     run->grid = *grid;
     run->opt = *opt;
     run->device = opt->device;
+    run->fp32 = (opt->precision == HYDRO_GPU_PRECISION_FP32);
+    run->elem = run->fp32 ? sizeof(float) : sizeof(double);
     run->tx = grid->nx + 2 * grid->g;
     run->ty = grid->ny + 2 * grid->g;
     run->ncell = (size_t) run->tx * (size_t) run->ty;
@@ -133,34 +184,66 @@ extern "C" int hydro_run2d_create(const HydroGrid2D *grid, const HydroGpuOptions
 
     /* 8 (U) + 10 (W) + 4 (snapshot) fields; the initial copy is separate */
     const size_t nfield = 22;
-    CK(cudaMalloc(&run->slab, nfield * run->ncell * sizeof(double)), "cudaMalloc(state)");
-    double *p = run->slab;
-    Mh2dArgs<double> &a = run->args;
-    for (int b = 0; b < 2; b++)
-        for (int q = 0; q < 4; q++) { a.U[b][q] = p; p += run->ncell; }
-    for (int b = 0; b < 2; b++)
-        for (int q = 0; q < 5; q++) { a.W[b][q] = p; p += run->ncell; }
-    for (int q = 0; q < 4; q++) { run->snap_d[q] = p; p += run->ncell; }
+    CK(cudaMalloc(&run->slab, nfield * run->ncell * run->elem), "cudaMalloc(state)");
+    if (run->fp32) CK(cudaMalloc(&run->stage_d, 4 * run->ncell * sizeof(double)), "cudaMalloc(staging)");
+    CK(cudaMalloc(&run->totals_d, 4 * sizeof(double)), "cudaMalloc(totals)");
     CK(cudaMalloc(&run->ctrl_d, sizeof(HydroStepControl)), "cudaMalloc(control)");
     CK(cudaMallocHost(&run->ctrl_h, sizeof(HydroStepControl)), "cudaMallocHost(control)");
     memset(run->ctrl_h, 0, sizeof(HydroStepControl));
+    if (run->fp32) {
+        carve<float>(run, run->args32);
+        setup_args<float>(run, run->args32, grid, opt);
+    } else {
+        carve<double>(run, run->args);
+        setup_args<double>(run, run->args, grid, opt);
+    }
+    return 0;
+}
 
-    a.ctrl = run->ctrl_d;
-    a.gas = make_gas_const<double>(grid->gamma, grid->tol);
-    a.nx = grid->nx;
-    a.ny = grid->ny;
-    a.g = grid->g;
-    a.pitch = run->tx;
-    a.strip_w = MH2D_THREADS - 2;
-    a.chunk_h = opt->chunk_rows > 0 ? opt->chunk_rows : 32;
-    for (int s = 0; s < 4; s++) a.bc[s] = grid->bc[s];
-    a.dx = grid->dx;
-    a.dy = grid->dy;
-    a.area_x = grid->area_x;
-    a.area_y = grid->area_y;
-    a.vol = grid->vol;
-    a.first_order = (grid->integrator == INTEGRATOR_GODUNOV_FIRST_ORDER_2D) ? 1 : 0;
-    a.grid_ctas = mh2d_resident_ctas<double>(grid->limiter, a.first_order, run->device);
+/* Device field pointers of the active precision, as untyped pointers. */
+static void *fieldU(HydroRun2D *run, int b, int q)
+{
+    return run->fp32 ? (void *) run->args32.U[b][q] : (void *) run->args.U[b][q];
+}
+
+static void *fieldW(HydroRun2D *run, int b, int q)
+{
+    return run->fp32 ? (void *) run->args32.W[b][q] : (void *) run->args.W[b][q];
+}
+
+/* Host FP64 arrays -> device fields (converted to FP32 for the FP32 form). */
+static int upload_fields(HydroRun2D *run, double *const host[4], void *const dev[4], HydroRunOutcome *oc)
+{
+    const size_t bytes = run->ncell * sizeof(double);
+    for (int q = 0; q < 4; q++) {
+        if (!run->fp32) {
+            CK(cudaMemcpyAsync(dev[q], host[q], bytes, cudaMemcpyHostToDevice, run->stream), "H2D");
+        } else {
+            double *st = run->stage_d + q * run->ncell;
+            CK(cudaMemcpyAsync(st, host[q], bytes, cudaMemcpyHostToDevice, run->stream), "H2D");
+            CK(convert_f64_to_f32(st, static_cast<float *>(dev[q]), (long long) run->ncell, run->stream),
+               "convert");
+            run->kernel_launches++;
+        }
+    }
+    return 0;
+}
+
+/* Device fields -> host FP64 arrays. */
+static int download_fields(HydroRun2D *run, void *const dev[4], double *const host[4], HydroRunOutcome *oc)
+{
+    const size_t bytes = run->ncell * sizeof(double);
+    for (int q = 0; q < 4; q++) {
+        if (!run->fp32) {
+            CK(cudaMemcpyAsync(host[q], dev[q], bytes, cudaMemcpyDeviceToHost, run->stream), "D2H");
+        } else {
+            double *st = run->stage_d + q * run->ncell;
+            CK(convert_f32_to_f64(static_cast<const float *>(dev[q]), st, (long long) run->ncell, run->stream),
+               "convert");
+            run->kernel_launches++;
+            CK(cudaMemcpyAsync(host[q], st, bytes, cudaMemcpyDeviceToHost, run->stream), "D2H");
+        }
+    }
     return 0;
 }
 
@@ -169,26 +252,25 @@ extern "C" int hydro_run2d_upload(HydroRun2D *run, double *const W[4], double *c
 {
     memset(oc, 0, sizeof *oc);
     CK(cudaSetDevice(run->device), "cudaSetDevice");
-    const size_t bytes = run->ncell * sizeof(double);
-    Mh2dArgs<double> &a = run->args;
+    const size_t fbytes = run->ncell * run->elem;
     CK(cudaEventRecord(run->ev[0], run->stream), "cudaEventRecord");
-    for (int q = 0; q < 4; q++) {
-        CK(cudaMemcpyAsync(a.U[0][q], U[q], bytes, cudaMemcpyHostToDevice, run->stream), "H2D U");
-        CK(cudaMemcpyAsync(a.W[0][q], W[q], bytes, cudaMemcpyHostToDevice, run->stream), "H2D W");
-    }
+    void *u0[4], *w0[4];
+    for (int q = 0; q < 4; q++) { u0[q] = fieldU(run, 0, q); w0[q] = fieldW(run, 0, q); }
+    if (upload_fields(run, U, u0, oc)) return -1;
+    if (upload_fields(run, W, w0, oc)) return -1;
     for (int q = 0; q < 4; q++)
-        CK(cudaMemcpyAsync(a.U[1][q], a.U[0][q], bytes, cudaMemcpyDeviceToDevice, run->stream), "D2D U");
+        CK(cudaMemcpyAsync(fieldU(run, 1, q), u0[q], fbytes, cudaMemcpyDeviceToDevice, run->stream), "D2D U");
     if (keep_initial) {
         if (!run->init_slab) {
-            CK(cudaMalloc(&run->init_slab, 8 * bytes), "cudaMalloc(initial state)");
+            CK(cudaMalloc(&run->init_slab, 8 * fbytes), "cudaMalloc(initial state)");
             for (int q = 0; q < 4; q++) {
-                run->init_U[q] = run->init_slab + q * run->ncell;
-                run->init_W[q] = run->init_slab + (4 + q) * run->ncell;
+                run->init_U[q] = static_cast<char *>(run->init_slab) + q * fbytes;
+                run->init_W[q] = static_cast<char *>(run->init_slab) + (4 + q) * fbytes;
             }
         }
         for (int q = 0; q < 4; q++) {
-            CK(cudaMemcpyAsync(run->init_U[q], a.U[0][q], bytes, cudaMemcpyDeviceToDevice, run->stream), "D2D");
-            CK(cudaMemcpyAsync(run->init_W[q], a.W[0][q], bytes, cudaMemcpyDeviceToDevice, run->stream), "D2D");
+            CK(cudaMemcpyAsync(run->init_U[q], u0[q], fbytes, cudaMemcpyDeviceToDevice, run->stream), "D2D");
+            CK(cudaMemcpyAsync(run->init_W[q], w0[q], fbytes, cudaMemcpyDeviceToDevice, run->stream), "D2D");
         }
         run->have_initial = true;
     }
@@ -197,7 +279,7 @@ extern "C" int hydro_run2d_upload(HydroRun2D *run, double *const W[4], double *c
     float ms = 0;
     CK(cudaEventElapsedTime(&ms, run->ev[0], run->ev[1]), "cudaEventElapsedTime");
     run->h2d_ms += ms;
-    run->h2d_bytes += (long long) (8 * bytes);
+    run->h2d_bytes += (long long) (8 * run->ncell * sizeof(double));
     run->begun = false;
     return 0;
 }
@@ -211,12 +293,11 @@ extern "C" int hydro_run2d_restore(HydroRun2D *run, HydroRunOutcome *oc)
         return -1;
     }
     CK(cudaSetDevice(run->device), "cudaSetDevice");
-    const size_t bytes = run->ncell * sizeof(double);
-    Mh2dArgs<double> &a = run->args;
+    const size_t fbytes = run->ncell * run->elem;
     for (int q = 0; q < 4; q++) {
-        CK(cudaMemcpyAsync(a.U[0][q], run->init_U[q], bytes, cudaMemcpyDeviceToDevice, run->stream), "D2D");
-        CK(cudaMemcpyAsync(a.U[1][q], run->init_U[q], bytes, cudaMemcpyDeviceToDevice, run->stream), "D2D");
-        CK(cudaMemcpyAsync(a.W[0][q], run->init_W[q], bytes, cudaMemcpyDeviceToDevice, run->stream), "D2D");
+        CK(cudaMemcpyAsync(fieldU(run, 0, q), run->init_U[q], fbytes, cudaMemcpyDeviceToDevice, run->stream), "D2D");
+        CK(cudaMemcpyAsync(fieldU(run, 1, q), run->init_U[q], fbytes, cudaMemcpyDeviceToDevice, run->stream), "D2D");
+        CK(cudaMemcpyAsync(fieldW(run, 0, q), run->init_W[q], fbytes, cudaMemcpyDeviceToDevice, run->stream), "D2D");
     }
     CK(cudaStreamSynchronize(run->stream), "restore");
     run->begun = false;
@@ -250,6 +331,7 @@ extern "C" int hydro_run2d_begin(HydroRun2D *run, const HydroStepParams *sp, dou
     memset(oc, 0, sizeof *oc);
     CK(cudaSetDevice(run->device), "cudaSetDevice");
     run->args.sp = *sp;
+    run->args32.sp = *sp;
     HydroStepControl *c = run->ctrl_h;
     memset(c, 0, sizeof *c);
     c->tf = tf;
@@ -259,7 +341,8 @@ extern "C" int hydro_run2d_begin(HydroRun2D *run, const HydroStepParams *sp, dou
     for (int k = 0; k < 3; k++) c->smax[k][0] = c->smax[k][1] = ninf;
     c->active = recompute_active(c);
     if (push_control(run, oc)) return -1;
-    CK(mh2d_launch_prepare<double>(run->args, run->stream), "prepare kernel");
+    CK(run->fp32 ? mh2d_launch_prepare<float>(run->args32, run->stream)
+                 : mh2d_launch_prepare<double>(run->args, run->stream), "prepare kernel");
     run->kernel_launches++;
     CK(cudaStreamSynchronize(run->stream), "prepare");
     /* The kernel arguments changed: any recorded graph is stale. */
@@ -302,7 +385,7 @@ static int record_graph(HydroRun2D *run, HydroRunOutcome *oc)
     CK(cudaStreamBeginCapture(run->stream, cudaStreamCaptureModeThreadLocal), "begin capture");
     cudaError_t le = cudaSuccess;
     for (int k = 0; k < kGraphSteps && le == cudaSuccess; k++)
-        le = mh2d_launch_step<double>(run->args, run->grid.limiter, run->stream);
+        le = launch_step(run);
     cudaError_t ce = cudaStreamEndCapture(run->stream, &g);
     if (le != cudaSuccess) { set_cuda_error(oc, le, "step kernel (capture)"); if (g) cudaGraphDestroy(g); return -1; }
     if (ce != cudaSuccess) { set_cuda_error(oc, ce, "end capture"); return -1; }
@@ -324,7 +407,7 @@ static int enqueue_steps(HydroRun2D *run, long long k, HydroRunOutcome *oc)
             run->step_launches += kGraphSteps;
             run->kernel_launches += kGraphSteps;
         } else {
-            CK(mh2d_launch_step<double>(run->args, run->grid.limiter, run->stream), "step kernel");
+            CK(launch_step(run), "step kernel");
             k -= 1;
             run->step_launches += 1;
             run->kernel_launches += 1;
@@ -336,12 +419,17 @@ static int enqueue_steps(HydroRun2D *run, long long k, HydroRunOutcome *oc)
 static int materialize_to_host(HydroRun2D *run, double *const W[4], HydroRunOutcome *oc)
 {
     const int buf = (int) (run->ctrl_h->num_steps & 1);
-    CK(mh2d_launch_materialize<double>(run->args, buf, run->snap_d, run->stream), "materialize kernel");
+    if (run->fp32) {
+        float *out[4];
+        for (int q = 0; q < 4; q++) out[q] = static_cast<float *>(run->snap_d[q]);
+        CK(mh2d_launch_materialize<float>(run->args32, buf, out, run->stream), "materialize kernel");
+    } else {
+        double *out[4];
+        for (int q = 0; q < 4; q++) out[q] = static_cast<double *>(run->snap_d[q]);
+        CK(mh2d_launch_materialize<double>(run->args, buf, out, run->stream), "materialize kernel");
+    }
     run->kernel_launches++;
-    const size_t bytes = run->ncell * sizeof(double);
-    for (int q = 0; q < 4; q++)
-        CK(cudaMemcpyAsync(W[q], run->snap_d[q], bytes, cudaMemcpyDeviceToHost, run->stream), "D2H W");
-    return 0;
+    return download_fields(run, run->snap_d, W, oc);
 }
 
 extern "C" int hydro_run2d_advance(HydroRun2D *run, HydroSnapshotFn snap, void *ctx,
@@ -437,14 +525,30 @@ extern "C" int hydro_run2d_download(HydroRun2D *run, double *const W[4], double 
     const size_t bytes = run->ncell * sizeof(double);
     CK(cudaEventRecord(run->ev[4], run->stream), "cudaEventRecord");
     if (materialize_to_host(run, W, oc)) return -1;
-    for (int q = 0; q < 4; q++)
-        CK(cudaMemcpyAsync(U[q], run->args.U[buf][q], bytes, cudaMemcpyDeviceToHost, run->stream), "D2H U");
+    void *ub[4];
+    for (int q = 0; q < 4; q++) ub[q] = fieldU(run, buf, q);
+    if (download_fields(run, ub, U, oc)) return -1;
     CK(cudaEventRecord(run->ev[5], run->stream), "cudaEventRecord");
     CK(cudaEventSynchronize(run->ev[5]), "download");
     float ms = 0;
     CK(cudaEventElapsedTime(&ms, run->ev[4], run->ev[5]), "cudaEventElapsedTime");
     run->d2h_ms += ms;
     run->d2h_bytes += (long long) (8 * bytes);
+    fill_outcome(run, oc);
+    return 0;
+}
+
+extern "C" int hydro_run2d_totals(HydroRun2D *run, double totals[4], HydroRunOutcome *oc)
+{
+    memset(oc, 0, sizeof *oc);
+    CK(cudaSetDevice(run->device), "cudaSetDevice");
+    if (pull_control(run, oc)) return -1;
+    const int buf = (int) (run->ctrl_h->num_steps & 1);
+    CK(run->fp32 ? mh2d_launch_totals<float>(run->args32, buf, run->totals_d, run->stream)
+                 : mh2d_launch_totals<double>(run->args, buf, run->totals_d, run->stream), "totals kernel");
+    run->kernel_launches++;
+    CK(cudaMemcpyAsync(totals, run->totals_d, 4 * sizeof(double), cudaMemcpyDeviceToHost, run->stream), "D2H totals");
+    CK(cudaStreamSynchronize(run->stream), "totals");
     fill_outcome(run, oc);
     return 0;
 }
@@ -472,6 +576,8 @@ extern "C" void hydro_run2d_destroy(HydroRun2D *run)
         if (e) cudaEventDestroy(e);
     cudaFree(run->slab);
     cudaFree(run->init_slab);
+    cudaFree(run->stage_d);
+    cudaFree(run->totals_d);
     cudaFree(run->ctrl_d);
     if (run->ctrl_h) cudaFreeHost(run->ctrl_h);
     if (run->snap_h) cudaFreeHost(run->snap_h);

@@ -213,9 +213,9 @@ static ErrorStatus run_2d(
     memset(&grid, 0, sizeof grid);
     ErrorStatus e = setup_grid2d(bcp, s, ip, &grid);
     if (e.return_code != SUCCESS) return e;
-    if (opt->precision != HYDRO_GPU_PRECISION_FP64)
+    if (opt->precision != HYDRO_GPU_PRECISION_FP64 && opt->precision != HYDRO_GPU_PRECISION_FP32)
     {
-        return WRAP_RAISE_ERROR(NOT_IMPLEMENTED_ERROR, "Requested precision is not available for this integrator.");
+        return WRAP_RAISE_ERROR(VALUE_ERROR, "Unknown precision.");
     }
 
     status->num_steps = 0;
@@ -597,6 +597,13 @@ ErrorStatus hydro_gpu_solver_download(HydroGpuSolver *sv, System *__restrict sys
     double *W[4] = { system->density_, system->velocity_x_, system->velocity_y_, system->pressure_ };
     double *U[4] = { system->mass_, system->momentum_x_, system->momentum_y_, system->energy_ };
     if (hydro_run2d_download(sv->run, W, U, &oc) != 0) return outcome_error(&oc);
+    return make_success_error_status();
+}
+
+ErrorStatus hydro_gpu_solver_conserved_totals(HydroGpuSolver *sv, double totals[4])
+{
+    HydroRunOutcome oc;
+    if (hydro_run2d_totals(sv->run, totals, &oc) != 0) return outcome_error(&oc);
     return make_success_error_status();
 }
 

@@ -112,6 +112,11 @@ ErrorStatus hydro_gpu_solver_advance(
  * System's host arrays. */
 ErrorStatus hydro_gpu_solver_download(HydroGpuSolver *solver, System *__restrict system);
 
+/* Conserved totals (mass, momentum_x, momentum_y, energy) over the interior
+ * of the current state, summed on the device in FP64 with Neumaier
+ * compensation (drift diagnostics for either precision). */
+ErrorStatus hydro_gpu_solver_conserved_totals(HydroGpuSolver *solver, double totals[4]);
+
 /* Kernels launched by this solver so far. */
 int64 hydro_gpu_solver_kernel_launches(const HydroGpuSolver *solver);
 
