@@ -145,6 +145,14 @@ _SIGNATURES = {
     "hydro_gpu_solver_kernel_launches": (C.c_int64, [C.c_void_p]),
     "hydro_gpu_solver_conserved_totals": (ErrorStatus, [C.c_void_p, _dp]),
     "hydro_gpu_solver_destroy": (None, [C.c_void_p]),
+    "hydro_gpu_batch_create": (ErrorStatus, [_P(C.c_void_p), C.c_int, C.c_void_p, C.c_void_p,
+                                             _P(IntegratorParam), _P(HydroGpuOptions)]),
+    "hydro_gpu_batch_restart": (ErrorStatus, [C.c_void_p]),
+    "hydro_gpu_batch_advance": (ErrorStatus, [C.c_void_p, C.c_int64, C.c_double, C.c_void_p,
+                                              _P(C.c_double)]),
+    "hydro_gpu_batch_download": (ErrorStatus, [C.c_void_p, C.c_void_p]),
+    "hydro_gpu_batch_kernel_launches": (C.c_int64, [C.c_void_p]),
+    "hydro_gpu_batch_destroy": (None, [C.c_void_p]),
     "hydro_gpu_device_count": (C.c_int, []),
     "hydro_gpu_calibrate": (C.c_int, [C.c_int, _dp, _dp]),
     "hydro_gpu_version": (C.c_char_p, []),
@@ -428,6 +436,92 @@ class Solver2D:
             self.lib.hydro_gpu_solver_destroy(self.handle)
             self.handle = C.c_void_p()
         self._h.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+class Batch2D:
+    """Ensemble of independent 2D problems (hydro_gpu_batch_*): one launch per
+    step for all instances, each with its own dt.  `problems` are objects with
+    the fields of hydrofv_gb300.problems.Problem2D; integrator, limiter and CFL
+    are taken from the first one."""
+
+    def __init__(self, problems, options: HydroGpuOptions | None = None):
+        self.lib = lib = library()
+        self.n = len(problems)
+        self._handles = []
+        self._keep: list = []
+        systems = (System * self.n)()
+        bcps = (BoundaryConditionParam * self.n)()
+        p0 = problems[0]
+        for i, p in enumerate(problems):
+            h = _SystemHandle(lib, "cartesian_2d", p.nx, p.ny, p.g,
+                              (p.x_min, p.x_max, p.y_min, p.y_max), p.gamma)
+            for dst, src in zip(h.fields(W2), p.W):
+                dst[:] = np.ascontiguousarray(src).reshape(-1)
+            for dst, src in zip(h.fields(U2), p.U):
+                dst[:] = np.ascontiguousarray(src).reshape(-1)
+            self._handles.append(h)
+            systems[i] = h.s
+            bcp, _ = _params(lib, p.bc, p0.integrator, p0.riemann_solver, p0.slope_limiter,
+                             p0.cfl, self._keep)
+            bcps[i] = bcp
+        self._systems, self._bcps = systems, bcps
+        _, ip = _params(lib, p0.bc, p0.integrator, p0.riemann_solver, p0.slope_limiter, p0.cfl,
+                        self._keep)
+        self._ip = ip
+        opt = options if options is not None else lib.hydro_gpu_default_options()
+        self.handle = C.c_void_p()
+        code, msg = _consume(lib, lib.hydro_gpu_batch_create(
+            C.byref(self.handle), self.n, C.cast(bcps, C.c_void_p),
+            C.cast(systems, C.c_void_p), C.byref(ip), C.byref(opt)))
+        if code != 0:
+            raise HydroError(code, msg)
+        self.cells = sum(p.nx * p.ny for p in problems)
+        self.shapes = [h.shape for h in self._handles]
+
+    def restart(self):
+        code, msg = _consume(self.lib, self.lib.hydro_gpu_batch_restart(self.handle))
+        if code != 0:
+            raise HydroError(code, msg)
+
+    def advance(self, steps: int, tf: float = 1e300):
+        st = (SimulationStatus * self.n)()
+        ms = C.c_double(0.0)
+        code, msg = _consume(self.lib, self.lib.hydro_gpu_batch_advance(
+            self.handle, steps, tf, C.cast(st, C.c_void_p), C.byref(ms)))
+        if code != 0:
+            raise HydroError(code, msg)
+        return [(s.num_steps, s.t, s.dt) for s in st], ms.value
+
+    def download(self):
+        code, msg = _consume(self.lib, self.lib.hydro_gpu_batch_download(
+            self.handle, C.cast(self._systems, C.c_void_p)))
+        if code != 0:
+            raise HydroError(code, msg)
+        out = []
+        for i, h in enumerate(self._handles):
+            h.s = self._systems[i]
+            W = np.stack([f.copy() for f in h.fields(W2)]).reshape((4,) + h.shape)
+            U = np.stack([f.copy() for f in h.fields(U2)]).reshape((4,) + h.shape)
+            out.append((W, U))
+        return out
+
+    def kernel_launches(self) -> int:
+        return int(self.lib.hydro_gpu_batch_kernel_launches(self.handle))
+
+    def close(self):
+        if self.handle:
+            self.lib.hydro_gpu_batch_destroy(self.handle)
+            self.handle = C.c_void_p()
+        for i, h in enumerate(self._handles):
+            h.s = self._systems[i]
+            h.close()
+        self._handles = []
 
     def __enter__(self):
         return self

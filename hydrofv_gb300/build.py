@@ -32,6 +32,7 @@ CUDA_SOURCES = [
     ("gpu/mh2d.cu", ["--fmad=false"]),
     ("gpu/mh2d_fp32.cu", []),
     ("gpu/runtime2d.cu", []),
+    ("gpu/runtime_batch.cu", []),
     ("gpu/host_numerics.cu", ["--fmad=false"]),
     ("gpu/calibrate.cu", []),
     ("gpu/noalloc2d.cu", []),

@@ -78,6 +78,24 @@ int hydro_run2d_totals(HydroRun2D *run, double totals[4], HydroRunOutcome *oc);
 void hydro_run2d_stats(const HydroRun2D *run, HydroGpuStats *stats);
 void hydro_run2d_destroy(HydroRun2D *run);
 
+/* Ensembles of independent 2D grids stepped by one launch per step. */
+typedef struct HydroBatch2D HydroBatch2D;
+int hydro_batch2d_create(const HydroGrid2D *grids, int n, const HydroGpuOptions *opt,
+                         HydroBatch2D **out, HydroRunOutcome *oc);
+int hydro_batch2d_upload(HydroBatch2D *b, int i, double *const W[4], double *const U[4],
+                         HydroRunOutcome *oc);
+int hydro_batch2d_restore(HydroBatch2D *b, HydroRunOutcome *oc);
+int hydro_batch2d_begin(HydroBatch2D *b, const HydroStepParams *sp, double tf, int64 max_steps,
+                        HydroRunOutcome *oc);
+/* Every instance: stop at tf or after max_steps_more further steps. */
+int hydro_batch2d_set_limits(HydroBatch2D *b, double tf, int64 max_steps_more, HydroRunOutcome *oc);
+int hydro_batch2d_advance(HydroBatch2D *b, HydroRunOutcome *oc, double *step_ms);
+int hydro_batch2d_status(HydroBatch2D *b, int i, HydroRunOutcome *oc);
+int hydro_batch2d_download(HydroBatch2D *b, int i, double *const W[4], double *const U[4],
+                           HydroRunOutcome *oc);
+void hydro_batch2d_stats(const HydroBatch2D *b, HydroGpuStats *stats);
+void hydro_batch2d_destroy(HydroBatch2D *b);
+
 /* 1D Cartesian problem (Godunov first order or MUSCL-Hancock). */
 typedef struct HydroGrid1D
 {

@@ -18,6 +18,9 @@ cudaError_t mh2d_launch_step(const Mh2dArgs<R> &a, int limiter, cudaStream_t s);
 template <class R>
 int mh2d_resident_ctas(int limiter, int first_order, int device);
 template <class R>
+cudaError_t mh2d_launch_batch_step(const Mh2dBatchArgs<R> &b, int limiter, int first_order, int grid,
+                                   cudaStream_t s);
+template <class R>
 cudaError_t mh2d_launch_prepare(const Mh2dArgs<R> &a, cudaStream_t s);
 template <class R>
 cudaError_t mh2d_launch_materialize(const Mh2dArgs<R> &a, int buf, R *const out[4], cudaStream_t s);

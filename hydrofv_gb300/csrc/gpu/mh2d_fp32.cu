@@ -14,6 +14,7 @@
 namespace hydro {
 
 template int mh2d_resident_ctas<float>(int, int, int);
+template cudaError_t mh2d_launch_batch_step<float>(const Mh2dBatchArgs<float> &, int, int, int, cudaStream_t);
 template cudaError_t mh2d_launch_step<float>(const Mh2dArgs<float> &, int, cudaStream_t);
 template cudaError_t mh2d_launch_prepare<float>(const Mh2dArgs<float> &, cudaStream_t);
 template cudaError_t mh2d_launch_materialize<float>(const Mh2dArgs<float> &, int,

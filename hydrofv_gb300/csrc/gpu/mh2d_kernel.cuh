@@ -191,9 +191,224 @@ __device__ __forceinline__ int solve_faces(Mh2dShared<R, NT> &sm, const GasConst
 }
 
 /*
- * One time step.  The grid is persistent: each CTA takes (strip, row chunk)
- * items from a device counter until none are left, so SMs that finish early
- * take more work (the FP64 pipe of an SM is shared by its CTAs).
+ * Process one work item (one strip of NT-2 columns x one chunk of chunk_h
+ * rows) of step n with time step dt.  Shared by the single-grid and the
+ * batched kernels; the caller reduces mx_x / mx_y and handles errors.
+ */
+template <class R, int LIM, int NT, int FIRST_ORDER>
+__device__ __forceinline__ void mh2d_item(const Mh2dArgs<R> &a, Mh2dShared<R, NT> &sm, int item,
+                                          long long n, double dt, double &mx_x, double &mx_y,
+                                          int &err)
+{
+    const R dtr = (R) dt;
+    const R dtA_x = (R) (dt * a.area_x / a.vol);
+    const R dtA_y = (R) (dt * a.area_y / a.vol);
+    const R Ax = (R) a.area_x, Ay = (R) a.area_y;
+    const int buf = (int) (n & 1);
+    const bool raw = (n == 0);
+    const R *const *Uin = a.U[buf];
+    R *const *Uout = a.U[buf ^ 1];
+    const R *const *Win = a.W[buf];
+    R *const *Wout = a.W[buf ^ 1];
+    const int tid = threadIdx.x;
+    const int g = a.g, nx = a.nx, ny = a.ny;
+    const int tx = nx + 2 * g, ty = ny + 2 * g;
+    const int n_strips = (nx + a.strip_w - 1) / a.strip_w;
+    const int ymap[4] = { 0, 2, 1, 3 };   /* y fluxes come back as (mass, mom_y, mom_x, energy) */
+
+    const int strip = item % n_strips;
+    const int c0 = g + strip * a.strip_w;
+    const int sw = min(a.strip_w, nx - strip * a.strip_w);
+    const int r_begin = g + (item / n_strips) * a.chunk_h;
+    const int r_end = min(r_begin + a.chunk_h, g + ny);
+    const int col = c0 - 1 + tid;
+    const bool x_slot = tid <= sw + 1;
+    const bool inner = tid >= 1 && tid <= sw;
+    const bool ghost_xmin = (c0 == g) && tid == 0;
+    const bool ghost_xmax = (c0 + sw == g + nx) && tid == sw + 1;
+    const int nX = sw + 1;
+
+    /* Rows inside [r_begin, r_end) need the strip plus two halo columns per
+     * side (x work); rows outside need only the strip's own columns.  Cells
+     * outside the padded grid (first order with one ghost layer) are never
+     * read and are not loaded. */
+    auto load_row = [&](int r) {
+        if (r < 0 || r >= ty) return;
+        const bool full = (r >= r_begin && r < r_end);
+        const int lo = full ? 0 : 2;
+        const int hi = full ? sw + 3 : sw + 1;
+        const int s = r % 3;
+        for (int u = tid; u < NT + 2; u += NT) {
+            const int c = c0 - 2 + u;
+            if (u >= lo && u <= hi && c >= 0 && c < tx) {
+                R w[5];
+                fetch_w(a, Win, Uin, raw, r, c, w);
+#pragma unroll
+                for (int q = 0; q < 5; q++) sm.ring[s][q][u] = w[q];
+            }
+        }
+    };
+
+    /* y reconstruction of this thread's cell in row r, (rho, v, u, p) order */
+    auto recon_y = [&](int r, R lo[4], R hi[4]) {
+        const int u = tid + 1;
+        const int sb = (r + 2) % 3, sc = r % 3, st = (r + 1) % 3;
+        const R rho = sm.ring[sc][0][u], vx = sm.ring[sc][1][u], vy = sm.ring[sc][2][u];
+        const R p = sm.ring[sc][3][u], as = sm.ring[sc][4][u];
+        if (FIRST_ORDER) {
+            lo[0] = hi[0] = rho; lo[1] = hi[1] = vy; lo[2] = hi[2] = vx; lo[3] = hi[3] = p;
+            return;
+        }
+        R d[4];
+        d[0] = limit_slope<LIM>(rho - sm.ring[sb][0][u], sm.ring[st][0][u] - rho);
+        const R dvx = limit_slope<LIM>(vx - sm.ring[sb][1][u], sm.ring[st][1][u] - vx);
+        d[1] = limit_slope<LIM>(vy - sm.ring[sb][2][u], sm.ring[st][2][u] - vy);
+        d[2] = dvx;
+        d[3] = limit_slope<LIM>(p - sm.ring[sb][3][u], sm.ring[st][3][u] - p);
+        hancock_2d(dtA_y, dtA_y / rho, rho, vy, vx, p, as, d, dvx, lo, hi);
+    };
+
+    /* x reconstruction of slot tid in ring row s, (rho, u, v, p) order */
+    auto recon_x = [&](int s, R lo[4], R hi[4]) {
+        const int u = tid + 1;
+        const R rho = sm.ring[s][0][u], vx = sm.ring[s][1][u], vy = sm.ring[s][2][u];
+        const R p = sm.ring[s][3][u], as = sm.ring[s][4][u];
+        if (FIRST_ORDER) {
+            lo[0] = hi[0] = rho; lo[1] = hi[1] = vx; lo[2] = hi[2] = vy; lo[3] = hi[3] = p;
+            return;
+        }
+        R d[4];
+        d[0] = limit_slope<LIM>(rho - sm.ring[s][0][u - 1], sm.ring[s][0][u + 1] - rho);
+        d[1] = limit_slope<LIM>(vx - sm.ring[s][1][u - 1], sm.ring[s][1][u + 1] - vx);
+        d[2] = limit_slope<LIM>(vy - sm.ring[s][2][u - 1], sm.ring[s][2][u + 1] - vy);
+        d[3] = limit_slope<LIM>(p - sm.ring[s][3][u - 1], sm.ring[s][3][u + 1] - p);
+        hancock_2d(dtA_x, dtA_x / rho, rho, vx, vy, p, as, d, d[1], lo, hi);
+    };
+
+    /* ---- prologue: the faces below r_begin ---- */
+    load_row(r_begin - 2);
+    load_row(r_begin - 1);
+    load_row(r_begin);
+    __syncthreads();
+    R ytop[4], gbot[4];
+    R tmp_lo[4], prev_hi[4];
+    if (inner) recon_y(r_begin - 1, tmp_lo, prev_hi);
+    __syncthreads();
+    load_row(r_begin + 1);
+    if (tid == 0) { sm.nT = 0; sm.nS = 0; }
+    __syncthreads();
+    if (inner) {
+        recon_y(r_begin, tmp_lo, ytop);
+#pragma unroll
+        for (int q = 0; q < 4; q++) { sm.FL[q][tid - 1] = prev_hi[q]; sm.FR[q][tid - 1] = tmp_lo[q]; }
+    }
+    __syncthreads();
+    {
+        const int rc = solve_faces<R, NT>(sm, a.gas, sw);
+        if (rc) err = rc;
+    }
+    if (inner) {
+#pragma unroll
+        for (int q = 0; q < 4; q++) gbot[q] = sm.FL[q][tid - 1];
+    }
+    __syncthreads();
+
+    /* ---- march up the rows ---- */
+    for (int r = r_begin; r < r_end; r++) {
+        load_row(r + 2);
+        if (tid == 0) { sm.nT = 0; sm.nS = 0; }
+        __syncthreads();
+
+        R nhi[4];
+        if (inner) {
+            R nlo[4];
+            recon_y(r + 1, nlo, nhi);
+            const int f = nX + tid - 1;
+#pragma unroll
+            for (int q = 0; q < 4; q++) { sm.FL[q][f] = ytop[q]; sm.FR[q][f] = nlo[q]; }
+        }
+        if (x_slot) {
+            R xl[4], xh[4];
+            recon_x(r % 3, xl, xh);
+            if (tid <= sw) {
+#pragma unroll
+                for (int q = 0; q < 4; q++) sm.FL[q][tid] = xh[q];
+            }
+            if (tid >= 1) {
+#pragma unroll
+                for (int q = 0; q < 4; q++) sm.FR[q][tid - 1] = xl[q];
+            }
+        }
+        __syncthreads();
+        {
+            const int rc = solve_faces<R, NT>(sm, a.gas, nX + sw);
+            if (rc) err = rc;
+        }
+
+        const long long rowbase = (long long) r * a.pitch;
+        if (inner) {
+            const long long idx = rowbase + col;
+            R gtop[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) gtop[q] = sm.FL[q][nX + tid - 1];
+            R Un[4];
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                R v = Uin[q][idx];
+                v = v + (sm.FL[q][tid - 1] * dtr) * Ax;
+                v = v - (sm.FL[q][tid] * dtr) * Ax;
+                v = v + (gbot[ymap[q]] * dtr) * Ay;
+                v = v - (gtop[ymap[q]] * dtr) * Ay;
+                Un[q] = v;
+                Uout[q][idx] = v;
+            }
+            R w[4];
+            cons_to_prim_2d_guarded(a.gas, (R) a.vol, Un[0], Un[1], Un[2], Un[3], w);
+            const R as = sound_speed(a.gas, w[0], w[3]);
+#pragma unroll
+            for (int q = 0; q < 4; q++) Wout[q][idx] = w[q];
+            Wout[4][idx] = as;
+            const double sx = (double) (as + fabs(w[1]));
+            const double sy = (double) (as + fabs(w[2]));
+            if (sx > mx_x) mx_x = sx;
+            if (sy > mx_y) mx_y = sy;
+
+            /* first ghost row below / above the domain: one-sided update */
+            if (r == g) {
+                const long long gi = idx - a.pitch;
+#pragma unroll
+                for (int q = 0; q < 4; q++)
+                    Uout[q][gi] = Uin[q][gi] - (gbot[ymap[q]] * dtr) * Ay;
+            }
+            if (r == g + ny - 1) {
+                const long long gi = idx + a.pitch;
+#pragma unroll
+                for (int q = 0; q < 4; q++)
+                    Uout[q][gi] = Uin[q][gi] + (gtop[ymap[q]] * dtr) * Ay;
+            }
+#pragma unroll
+            for (int q = 0; q < 4; q++) { ytop[q] = nhi[q]; gbot[q] = gtop[q]; }
+        }
+        /* first ghost column left / right of the domain */
+        if (ghost_xmin) {
+            const long long gi = rowbase + col;
+#pragma unroll
+            for (int q = 0; q < 4; q++) Uout[q][gi] = Uin[q][gi] - (sm.FL[q][0] * dtr) * Ax;
+        }
+        if (ghost_xmax) {
+            const long long gi = rowbase + col;
+#pragma unroll
+            for (int q = 0; q < 4; q++) Uout[q][gi] = Uin[q][gi] + (sm.FL[q][sw] * dtr) * Ax;
+        }
+        __syncthreads();
+    }
+}
+
+/*
+ * One time step of one grid.  The grid is persistent: each CTA takes
+ * (strip, row chunk) items from a device counter until none are left, so
+ * SMs that finish early take more work (the FP64 pipe of an SM is shared by
+ * its CTAs).
  */
 template <class R, int LIM, int NT, int FIRST_ORDER>
 __global__ void __launch_bounds__(NT, 4) mh2d_step_kernel(const Mh2dArgs<R> a)
@@ -219,27 +434,10 @@ __global__ void __launch_bounds__(NT, 4) mh2d_step_kernel(const Mh2dArgs<R> a)
         }
         return;
     }
-    const R dtr = (R) dt;
-    const R dtA_x = (R) (dt * a.area_x / a.vol);
-    const R dtA_y = (R) (dt * a.area_y / a.vol);
-    const R Ax = (R) a.area_x, Ay = (R) a.area_y;
-
-    const int buf = (int) (n & 1);
-    const bool raw = (n == 0);
-    const R *const *Uin = a.U[buf];
-    R *const *Uout = a.U[buf ^ 1];
-    const R *const *Win = a.W[buf];
-    R *const *Wout = a.W[buf ^ 1];
 
     __shared__ Mh2dShared<R, NT> sm;
-
     const int tid = threadIdx.x;
-    const int g = a.g, nx = a.nx, ny = a.ny;
-    const int tx = nx + 2 * g, ty = ny + 2 * g;
-    const int n_strips = (nx + a.strip_w - 1) / a.strip_w;
-    const int n_items = n_strips * ((ny + a.chunk_h - 1) / a.chunk_h);
-    const int ymap[4] = { 0, 2, 1, 3 };   /* y fluxes come back as (mass, mom_y, mom_x, energy) */
-
+    const int n_items = ((a.nx + a.strip_w - 1) / a.strip_w) * ((a.ny + a.chunk_h - 1) / a.chunk_h);
     double mx_x = -CUDART_INF, mx_y = -CUDART_INF;
     int err = DEV_OK;
 
@@ -249,193 +447,7 @@ __global__ void __launch_bounds__(NT, 4) mh2d_step_kernel(const Mh2dArgs<R> a)
         const int item = sm.item;
         __syncthreads();
         if (item >= n_items) break;
-
-        const int strip = item % n_strips;
-        const int c0 = g + strip * a.strip_w;
-        const int sw = min(a.strip_w, nx - strip * a.strip_w);
-        const int r_begin = g + (item / n_strips) * a.chunk_h;
-        const int r_end = min(r_begin + a.chunk_h, g + ny);
-        const int col = c0 - 1 + tid;
-        const bool x_slot = tid <= sw + 1;
-        const bool inner = tid >= 1 && tid <= sw;
-        const bool ghost_xmin = (c0 == g) && tid == 0;
-        const bool ghost_xmax = (c0 + sw == g + nx) && tid == sw + 1;
-        const int nX = sw + 1;
-
-        /* Rows inside [r_begin, r_end) need the strip plus two halo columns per
-         * side (x work); rows outside need only the strip's own columns.  Cells
-         * outside the padded grid (first order with one ghost layer) are never
-         * read and are not loaded. */
-        auto load_row = [&](int r) {
-            if (r < 0 || r >= ty) return;
-            const bool full = (r >= r_begin && r < r_end);
-            const int lo = full ? 0 : 2;
-            const int hi = full ? sw + 3 : sw + 1;
-            const int s = r % 3;
-            for (int u = tid; u < NT + 2; u += NT) {
-                const int c = c0 - 2 + u;
-                if (u >= lo && u <= hi && c >= 0 && c < tx) {
-                    R w[5];
-                    fetch_w(a, Win, Uin, raw, r, c, w);
-#pragma unroll
-                    for (int q = 0; q < 5; q++) sm.ring[s][q][u] = w[q];
-                }
-            }
-        };
-
-        /* y reconstruction of this thread's cell in row r, (rho, v, u, p) order */
-        auto recon_y = [&](int r, R lo[4], R hi[4]) {
-            const int u = tid + 1;
-            const int sb = (r + 2) % 3, sc = r % 3, st = (r + 1) % 3;
-            const R rho = sm.ring[sc][0][u], vx = sm.ring[sc][1][u], vy = sm.ring[sc][2][u];
-            const R p = sm.ring[sc][3][u], as = sm.ring[sc][4][u];
-            if (FIRST_ORDER) {
-                lo[0] = hi[0] = rho; lo[1] = hi[1] = vy; lo[2] = hi[2] = vx; lo[3] = hi[3] = p;
-                return;
-            }
-            R d[4];
-            d[0] = limit_slope<LIM>(rho - sm.ring[sb][0][u], sm.ring[st][0][u] - rho);
-            const R dvx = limit_slope<LIM>(vx - sm.ring[sb][1][u], sm.ring[st][1][u] - vx);
-            d[1] = limit_slope<LIM>(vy - sm.ring[sb][2][u], sm.ring[st][2][u] - vy);
-            d[2] = dvx;
-            d[3] = limit_slope<LIM>(p - sm.ring[sb][3][u], sm.ring[st][3][u] - p);
-            hancock_2d(dtA_y, dtA_y / rho, rho, vy, vx, p, as, d, dvx, lo, hi);
-        };
-
-        /* x reconstruction of slot tid in ring row s, (rho, u, v, p) order */
-        auto recon_x = [&](int s, R lo[4], R hi[4]) {
-            const int u = tid + 1;
-            const R rho = sm.ring[s][0][u], vx = sm.ring[s][1][u], vy = sm.ring[s][2][u];
-            const R p = sm.ring[s][3][u], as = sm.ring[s][4][u];
-            if (FIRST_ORDER) {
-                lo[0] = hi[0] = rho; lo[1] = hi[1] = vx; lo[2] = hi[2] = vy; lo[3] = hi[3] = p;
-                return;
-            }
-            R d[4];
-            d[0] = limit_slope<LIM>(rho - sm.ring[s][0][u - 1], sm.ring[s][0][u + 1] - rho);
-            d[1] = limit_slope<LIM>(vx - sm.ring[s][1][u - 1], sm.ring[s][1][u + 1] - vx);
-            d[2] = limit_slope<LIM>(vy - sm.ring[s][2][u - 1], sm.ring[s][2][u + 1] - vy);
-            d[3] = limit_slope<LIM>(p - sm.ring[s][3][u - 1], sm.ring[s][3][u + 1] - p);
-            hancock_2d(dtA_x, dtA_x / rho, rho, vx, vy, p, as, d, d[1], lo, hi);
-        };
-
-        /* ---- prologue: the faces below r_begin ---- */
-        load_row(r_begin - 2);
-        load_row(r_begin - 1);
-        load_row(r_begin);
-        __syncthreads();
-        R ytop[4], gbot[4];
-        R tmp_lo[4], prev_hi[4];
-        if (inner) recon_y(r_begin - 1, tmp_lo, prev_hi);
-        __syncthreads();
-        load_row(r_begin + 1);
-        if (tid == 0) { sm.nT = 0; sm.nS = 0; }
-        __syncthreads();
-        if (inner) {
-            recon_y(r_begin, tmp_lo, ytop);
-#pragma unroll
-            for (int q = 0; q < 4; q++) { sm.FL[q][tid - 1] = prev_hi[q]; sm.FR[q][tid - 1] = tmp_lo[q]; }
-        }
-        __syncthreads();
-        {
-            const int rc = solve_faces<R, NT>(sm, a.gas, sw);
-            if (rc) err = rc;
-        }
-        if (inner) {
-#pragma unroll
-            for (int q = 0; q < 4; q++) gbot[q] = sm.FL[q][tid - 1];
-        }
-        __syncthreads();
-
-        /* ---- march up the rows ---- */
-        for (int r = r_begin; r < r_end; r++) {
-            load_row(r + 2);
-            if (tid == 0) { sm.nT = 0; sm.nS = 0; }
-            __syncthreads();
-
-            R nhi[4];
-            if (inner) {
-                R nlo[4];
-                recon_y(r + 1, nlo, nhi);
-                const int f = nX + tid - 1;
-#pragma unroll
-                for (int q = 0; q < 4; q++) { sm.FL[q][f] = ytop[q]; sm.FR[q][f] = nlo[q]; }
-            }
-            if (x_slot) {
-                R xl[4], xh[4];
-                recon_x(r % 3, xl, xh);
-                if (tid <= sw) {
-#pragma unroll
-                    for (int q = 0; q < 4; q++) sm.FL[q][tid] = xh[q];
-                }
-                if (tid >= 1) {
-#pragma unroll
-                    for (int q = 0; q < 4; q++) sm.FR[q][tid - 1] = xl[q];
-                }
-            }
-            __syncthreads();
-            {
-                const int rc = solve_faces<R, NT>(sm, a.gas, nX + sw);
-                if (rc) err = rc;
-            }
-
-            const long long rowbase = (long long) r * a.pitch;
-            if (inner) {
-                const long long idx = rowbase + col;
-                R gtop[4];
-#pragma unroll
-                for (int q = 0; q < 4; q++) gtop[q] = sm.FL[q][nX + tid - 1];
-                R Un[4];
-#pragma unroll
-                for (int q = 0; q < 4; q++) {
-                    R v = Uin[q][idx];
-                    v = v + (sm.FL[q][tid - 1] * dtr) * Ax;
-                    v = v - (sm.FL[q][tid] * dtr) * Ax;
-                    v = v + (gbot[ymap[q]] * dtr) * Ay;
-                    v = v - (gtop[ymap[q]] * dtr) * Ay;
-                    Un[q] = v;
-                    Uout[q][idx] = v;
-                }
-                R w[4];
-                cons_to_prim_2d_guarded(a.gas, (R) a.vol, Un[0], Un[1], Un[2], Un[3], w);
-                const R as = sound_speed(a.gas, w[0], w[3]);
-#pragma unroll
-                for (int q = 0; q < 4; q++) Wout[q][idx] = w[q];
-                Wout[4][idx] = as;
-                const double sx = (double) (as + fabs(w[1]));
-                const double sy = (double) (as + fabs(w[2]));
-                if (sx > mx_x) mx_x = sx;
-                if (sy > mx_y) mx_y = sy;
-
-                /* first ghost row below / above the domain: one-sided update */
-                if (r == g) {
-                    const long long gi = idx - a.pitch;
-#pragma unroll
-                    for (int q = 0; q < 4; q++)
-                        Uout[q][gi] = Uin[q][gi] - (gbot[ymap[q]] * dtr) * Ay;
-                }
-                if (r == g + ny - 1) {
-                    const long long gi = idx + a.pitch;
-#pragma unroll
-                    for (int q = 0; q < 4; q++)
-                        Uout[q][gi] = Uin[q][gi] + (gtop[ymap[q]] * dtr) * Ay;
-                }
-#pragma unroll
-                for (int q = 0; q < 4; q++) { ytop[q] = nhi[q]; gbot[q] = gtop[q]; }
-            }
-            /* first ghost column left / right of the domain */
-            if (ghost_xmin) {
-                const long long gi = rowbase + col;
-#pragma unroll
-                for (int q = 0; q < 4; q++) Uout[q][gi] = Uin[q][gi] - (sm.FL[q][0] * dtr) * Ax;
-            }
-            if (ghost_xmax) {
-                const long long gi = rowbase + col;
-#pragma unroll
-                for (int q = 0; q < 4; q++) Uout[q][gi] = Uin[q][gi] + (sm.FL[q][sw] * dtr) * Ax;
-            }
-            __syncthreads();
-        }
+        mh2d_item<R, LIM, NT, FIRST_ORDER>(a, sm, item, n, dt, mx_x, mx_y, err);
     }
 
     if (err) record_error(ctrl, err, (int) blockIdx.x);
@@ -493,6 +505,168 @@ __global__ void __launch_bounds__(NT, 4) mh2d_step_kernel(const Mh2dArgs<R> a)
             ctrl->active = act;
         }
         ctrl->blocks_done = 0;
+    }
+}
+
+/* ------------------------------------------------------------------ */
+/* Batched ensembles: many independent grids in one launch per step.   */
+/* ------------------------------------------------------------------ */
+
+/* Work queue of one batched step launch. */
+struct HydroBatchControl {
+    int work_next;           /* next global work item */
+    unsigned int ctas_done;  /* CTAs that left the queue (last one resets both) */
+};
+
+template <class R>
+struct Mh2dBatchArgs {
+    const Mh2dArgs<R> *inst;  /* per-instance arguments (device memory), each with its own control */
+    const int *item_off;      /* n_inst + 1 prefix offsets of the instances' work items */
+    int n_inst;
+    int total_items;
+    HydroBatchControl *bctrl;
+};
+
+/* dt of instance `a` for its current step, or 0 when it must not step
+ * (inactive; on dt == 0 the error is recorded as the single-grid kernel does). */
+template <class R>
+__device__ double instance_dt(const Mh2dArgs<R> &a, long long &n)
+{
+    HydroStepControl *ctrl = a.ctrl;
+    if (!*(volatile int *) &ctrl->active) return 0.0;
+    n = ctrl->num_steps;
+    const double t_now = ctrl->t;
+    const double Sx = from_ordered_bits(ctrl->smax[n % 3][0]);
+    const double Sy = from_ordered_bits(ctrl->smax[n % 3][1]);
+    const double cfl = (n < a.sp.shrink_steps) ? a.sp.cfl_shrunk : a.sp.cfl;
+    double dt = cfl / (Sx / a.dx + Sy / a.dy);
+    const double tf = ctrl->tf;
+    if (t_now + dt > tf) dt = tf - t_now;
+    if (dt == 0.0) {
+        ctrl->dt = dt;
+        record_error(ctrl, DEV_ERR_DT_ZERO, -1);
+        ctrl->active = 0;
+    }
+    return dt;
+}
+
+/* Clock advance of one instance by the last of its items (the single-grid
+ * kernel's last-CTA block, per instance). */
+__device__ __forceinline__ void instance_bookkeeping(HydroStepControl *ctrl, const HydroStepParams &sp,
+                                                     long long n, double dt)
+{
+    volatile HydroStepControl *vc = ctrl;
+    ctrl->dt = dt;
+    if (vc->error_code != 0) {
+        ctrl->active = 0;
+    } else {
+        const double tn = vc->t + dt;
+        const long long nn = n + 1;
+        ctrl->t = tn;
+        ctrl->num_steps = nn;
+        const int nn2 = (int) ((n + 2) % 3);
+        ctrl->smax[nn2][0] = ordered_bits(-CUDART_INF);
+        ctrl->smax[nn2][1] = ordered_bits(-CUDART_INF);
+        int act = (tn < vc->tf) && (vc->max_steps < 0 || nn < vc->max_steps);
+        if (sp.is_storing &&
+            tn >= sp.storing_interval * (double) (vc->store_count - sp.store_initial_offset + 1)) {
+            ctrl->snapshot_due = 1;
+            act = 0;
+        }
+        ctrl->active = act;
+    }
+    ctrl->blocks_done = 0;
+}
+
+/*
+ * One time step of every active instance of a batch.  Persistent CTAs take
+ * global items from one queue; an item belongs to one instance (found by
+ * binary search in the prefix offsets), whose dt the CTA derives from that
+ * instance's control block.  After each item the CTA folds its CFL maxima
+ * into the instance's next-step words, and the instance's last item
+ * advances that instance's clock.  Instances are laid out largest first,
+ * so the queue drains the big grids early and the tail is made of small
+ * items.
+ */
+template <class R, int LIM, int NT, int FIRST_ORDER>
+__global__ void __launch_bounds__(NT, 4) mh2d_batch_step_kernel(const Mh2dBatchArgs<R> b)
+{
+    __shared__ Mh2dShared<R, NT> sm;
+    __shared__ int s_inst, s_local, s_go, s_last;
+    __shared__ long long s_n;
+    __shared__ double s_dt;
+    const int tid = threadIdx.x;
+    for (;;) {
+        if (tid == 0) {
+            const int gi = atomicAdd(&b.bctrl->work_next, 1);
+            s_go = 0;
+            sm.item = gi;
+            if (gi < b.total_items) {
+                int lo = 0, hi = b.n_inst - 1;
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (b.item_off[mid] <= gi) lo = mid;
+                    else hi = mid - 1;
+                }
+                s_inst = lo;
+                s_local = gi - b.item_off[lo];
+                long long n = 0;
+                const double dt = instance_dt(b.inst[lo], n);
+                s_dt = dt;
+                s_n = n;
+                s_go = (dt != 0.0);
+            }
+        }
+        __syncthreads();
+        if (sm.item >= b.total_items) break;
+        const int go = s_go, inst = s_inst, local = s_local;
+        const long long n = s_n;
+        const double dt = s_dt;
+        __syncthreads();
+        if (!go) continue;
+        const Mh2dArgs<R> &a = b.inst[inst];
+        double mx_x = -CUDART_INF, mx_y = -CUDART_INF;
+        int err = DEV_OK;
+        mh2d_item<R, LIM, NT, FIRST_ORDER>(a, sm, local, n, dt, mx_x, mx_y, err);
+        if (err) record_error(a.ctrl, err, inst);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const double ox = __shfl_xor_sync(0xffffffffu, mx_x, o);
+            const double oy = __shfl_xor_sync(0xffffffffu, mx_y, o);
+            if (ox > mx_x) mx_x = ox;
+            if (oy > mx_y) mx_y = oy;
+        }
+        if ((tid & 31) == 0) {
+            sm.red[0][tid >> 5] = mx_x;
+            sm.red[1][tid >> 5] = mx_y;
+        }
+        __syncthreads();
+        if (tid == 0) {
+            double bx = sm.red[0][0], by = sm.red[1][0];
+            for (int w = 1; w < NT / 32; w++) {
+                if (sm.red[0][w] > bx) bx = sm.red[0][w];
+                if (sm.red[1][w] > by) by = sm.red[1][w];
+            }
+            HydroStepControl *ctrl = a.ctrl;
+            const int nxt = (int) ((n + 1) % 3);
+            atomicMax(&ctrl->smax[nxt][0], ordered_bits(bx));
+            atomicMax(&ctrl->smax[nxt][1], ordered_bits(by));
+            __threadfence();
+            const int n_items = b.item_off[inst + 1] - b.item_off[inst];
+            s_last = (atomicAdd(&ctrl->blocks_done, 1u) == (unsigned) (n_items - 1));
+            if (s_last) {
+                __threadfence();
+                instance_bookkeeping(ctrl, a.sp, n, dt);
+            }
+        }
+        __syncthreads();
+    }
+    if (tid == 0) {
+        __threadfence();
+        if (atomicAdd(&b.bctrl->ctas_done, 1u) == gridDim.x - 1) {
+            b.bctrl->work_next = 0;
+            b.bctrl->ctas_done = 0;
+        }
     }
 }
 

@@ -121,6 +121,25 @@ cudaError_t mh2d_launch_materialize(const Mh2dArgs<R> &a, int buf, R *const out[
     return cudaGetLastError();
 }
 
+template <class R, int LIM, int FIRST_ORDER>
+static cudaError_t launch_batch_lim(const Mh2dBatchArgs<R> &b, int grid, cudaStream_t s)
+{
+    mh2d_batch_step_kernel<R, LIM, MH2D_THREADS, FIRST_ORDER><<<grid, MH2D_THREADS, 0, s>>>(b);
+    return cudaGetLastError();
+}
+
+template <class R>
+cudaError_t mh2d_launch_batch_step(const Mh2dBatchArgs<R> &b, int limiter, int first_order, int grid,
+                                   cudaStream_t s)
+{
+    if (first_order) return launch_batch_lim<R, LIM_MINMOD, 1>(b, grid, s);
+    switch (limiter) {
+    case LIM_MINMOD: return launch_batch_lim<R, LIM_MINMOD, 0>(b, grid, s);
+    case LIM_VAN_LEER: return launch_batch_lim<R, LIM_VAN_LEER, 0>(b, grid, s);
+    default: return launch_batch_lim<R, LIM_MC, 0>(b, grid, s);
+    }
+}
+
 /* CTAs of the step kernel that fit on the device at once. */
 template <class R>
 int mh2d_resident_ctas(int limiter, int first_order, int device)

@@ -621,3 +621,141 @@ void hydro_gpu_solver_destroy(HydroGpuSolver *sv)
     hydro_run2d_destroy(sv->run);
     free(sv);
 }
+
+/* -------------------------------------------------------------- batches */
+
+struct HydroGpuBatch
+{
+    HydroBatch2D *b;
+    int n;
+    HydroStepParams params;
+    int begun;
+};
+
+ErrorStatus hydro_gpu_batch_create(
+    HydroGpuBatch **out,
+    int n,
+    BoundaryConditionParam *bcps,
+    System *systems,
+    IntegratorParam *__restrict ip,
+    const HydroGpuOptions *options
+)
+{
+    *out = NULL;
+    if (n < 1 || !bcps || !systems) return WRAP_RAISE_ERROR(POINTER_ERROR, "Empty batch.");
+    ErrorStatus e = WRAP_TRACEBACK(finalize_integrator_param(ip));
+    if (e.return_code != SUCCESS) return e;
+    if (ip->integrator_flag_ != INTEGRATOR_MUSCL_HANCOCK_2D && ip->integrator_flag_ != INTEGRATOR_GODUNOV_FIRST_ORDER_2D)
+        return WRAP_RAISE_ERROR(NOT_IMPLEMENTED_ERROR, "Batches run the 2D integrators.");
+    HydroGrid2D *grids = calloc((size_t) n, sizeof *grids);
+    HydroGpuBatch *bt = calloc(1, sizeof *bt);
+    if (!grids || !bt)
+    {
+        free(grids);
+        free(bt);
+        return WRAP_RAISE_ERROR(MEMORY_ERROR, "Failed to allocate the batch.");
+    }
+    for (int i = 0; i < n; i++)
+    {
+        e = WRAP_TRACEBACK(finalize_boundary_condition_param(&systems[i], &bcps[i]));
+        if (e.return_code == SUCCESS) e = WRAP_TRACEBACK(hydro_final_check(&systems[i], ip));
+        if (e.return_code == SUCCESS) e = setup_grid2d(&bcps[i], &systems[i], ip, &grids[i]);
+        if (e.return_code != SUCCESS)
+        {
+            free(grids);
+            free(bt);
+            return e;
+        }
+    }
+    const HydroGpuOptions opt = options ? *options : hydro_gpu_default_options();
+    StoringParam none = get_new_storing_param();
+    bt->params = step_params(ip, &none);
+    bt->n = n;
+    HydroRunOutcome oc;
+    int rc = hydro_batch2d_create(grids, n, &opt, &bt->b, &oc);
+    free(grids);
+    for (int i = 0; rc == 0 && i < n; i++)
+    {
+        System *s = &systems[i];
+        double *W[4] = { s->density_, s->velocity_x_, s->velocity_y_, s->pressure_ };
+        double *U[4] = { s->mass_, s->momentum_x_, s->momentum_y_, s->energy_ };
+        rc = hydro_batch2d_upload(bt->b, i, W, U, &oc);
+    }
+    if (rc != 0)
+    {
+        hydro_batch2d_destroy(bt->b);
+        free(bt);
+        return outcome_error(&oc);
+    }
+    *out = bt;
+    return make_success_error_status();
+}
+
+ErrorStatus hydro_gpu_batch_restart(HydroGpuBatch *bt)
+{
+    HydroRunOutcome oc;
+    if (hydro_batch2d_restore(bt->b, &oc) != 0) return outcome_error(&oc);
+    bt->begun = 0;
+    return make_success_error_status();
+}
+
+ErrorStatus hydro_gpu_batch_advance(
+    HydroGpuBatch *bt,
+    int64 num_steps,
+    double tf,
+    SimulationStatus *statuses,
+    double *step_ms
+)
+{
+    HydroRunOutcome oc;
+    if (!bt->begun)
+    {
+        if (hydro_batch2d_begin(bt->b, &bt->params, tf, num_steps, &oc) != 0) return outcome_error(&oc);
+        bt->begun = 1;
+    }
+    else if (hydro_batch2d_set_limits(bt->b, tf, num_steps, &oc) != 0)
+    {
+        return outcome_error(&oc);
+    }
+    const int rc = hydro_batch2d_advance(bt->b, &oc, step_ms);
+    if (statuses)
+    {
+        for (int i = 0; i < bt->n; i++)
+        {
+            HydroRunOutcome so;
+            hydro_batch2d_status(bt->b, i, &so);
+            statuses[i].num_steps = so.num_steps;
+            statuses[i].t = so.t;
+            statuses[i].dt = so.dt;
+        }
+    }
+    if (rc != 0) return outcome_error(&oc);
+    return make_success_error_status();
+}
+
+ErrorStatus hydro_gpu_batch_download(HydroGpuBatch *bt, System *systems)
+{
+    for (int i = 0; i < bt->n; i++)
+    {
+        HydroRunOutcome oc;
+        System *s = &systems[i];
+        double *W[4] = { s->density_, s->velocity_x_, s->velocity_y_, s->pressure_ };
+        double *U[4] = { s->mass_, s->momentum_x_, s->momentum_y_, s->energy_ };
+        if (hydro_batch2d_download(bt->b, i, W, U, &oc) != 0) return outcome_error(&oc);
+    }
+    return make_success_error_status();
+}
+
+int64 hydro_gpu_batch_kernel_launches(const HydroGpuBatch *bt)
+{
+    HydroGpuStats st;
+    hydro_batch2d_stats(bt->b, &st);
+    return st.kernel_launches;
+}
+
+void hydro_gpu_batch_destroy(HydroGpuBatch *bt)
+{
+    if (!bt) return;
+    hydro_batch2d_destroy(bt->b);
+    free(bt);
+}

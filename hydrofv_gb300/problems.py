@@ -295,3 +295,15 @@ def random_problem_1d(nx: int, seed: int, bc, integrator: str = "godunov_first_o
     U = primitive_to_conserved_1d(W, gamma, vol)
     return Problem1D(nx, g, 0.0, 1.0, gamma, W, U, tuple(bc), integrator, riemann_solver,
                      limiter, cfl=0.8, tf=1e300, max_steps=steps, name=f"random1d_{nx}_{seed}")
+
+
+def four_quadrant_ensemble(count: int = 256, seed: int = 4, steps: int = 500,
+                           side_range=(128, 1024), limiter: str = "minmod"):
+    """Batched ensemble of independent four-quadrant Riemann problems: grid side
+    drawn log-uniform in side_range per instance, quadrant states
+    rho, p ~ U[0.1, 2], u, v ~ U[-1, 1], gamma = 1.4, transmissive,
+    MUSCL-Hancock + HLLC + minmod, CFL 0.8, per-instance dt."""
+    rng = np.random.default_rng(seed)
+    lo, hi = math.log(side_range[0]), math.log(side_range[1])
+    sides = np.rint(np.exp(rng.uniform(lo, hi, size=count))).astype(int)
+    return [four_quadrant(int(s), rng, steps=steps, limiter=limiter) for s in sides]

@@ -122,6 +122,45 @@ int64 hydro_gpu_solver_kernel_launches(const HydroGpuSolver *solver);
 
 void hydro_gpu_solver_destroy(HydroGpuSolver *solver);
 
+/* ------------------------------------------------------------------ */
+/* Batched ensembles of independent 2D grids.                          */
+/* ------------------------------------------------------------------ */
+
+typedef struct HydroGpuBatch HydroGpuBatch;
+
+/* n independent 2D problems (systems[i] with boundary conditions bcps[i];
+ * one integrator / Riemann solver / limiter / CFL for all) uploaded into one
+ * device slab.  Each instance keeps its own time and CFL dt; every step is
+ * one launch over all instances, replayed from a CUDA graph.  The initial
+ * states are kept on the device for hydro_gpu_batch_restart. */
+ErrorStatus hydro_gpu_batch_create(
+    HydroGpuBatch **batch,
+    int n_instances,
+    BoundaryConditionParam *boundary_condition_params,
+    System *systems,
+    IntegratorParam *__restrict integrator_param,
+    const HydroGpuOptions *options
+);
+
+ErrorStatus hydro_gpu_batch_restart(HydroGpuBatch *batch);
+
+/* Advance every instance by up to num_steps steps (each stops at tf on its
+ * own clock); statuses[i] (may be NULL) receives each instance's status. */
+ErrorStatus hydro_gpu_batch_advance(
+    HydroGpuBatch *batch,
+    int64 num_steps,
+    double tf,
+    SimulationStatus *statuses,
+    double *step_ms
+);
+
+/* Copy every instance's state back into systems[i]'s host arrays. */
+ErrorStatus hydro_gpu_batch_download(HydroGpuBatch *batch, System *systems);
+
+int64 hydro_gpu_batch_kernel_launches(const HydroGpuBatch *batch);
+
+void hydro_gpu_batch_destroy(HydroGpuBatch *batch);
+
 /* Measure the device's FMA throughput (TFLOP/s, 1 FMA = 2 FLOP) in FP64 and
  * FP32 with a short calibration kernel; either pointer may be NULL.  Used
  * for roofline reporting.  Returns 0 on success. */
