@@ -203,6 +203,68 @@ def run_reference_arm(args) -> None:
     print(json.dumps(line))
 
 
+def run_ensemble(args, H, device, ws, rank) -> None:
+    """Batched ensemble: every instance steps args.steps times, one launch per
+    step for the whole batch, FP64 and FP32 on the same instances."""
+    from hydrofv_gb300.problems import four_quadrant_ensemble
+    probs = four_quadrant_ensemble(count=args.instances, steps=args.steps)
+    cells = sum(p.nx * p.ny for p in probs)
+    res = {}
+    finals = {}
+    for name, prec in (("fp64", H.PRECISION_FP64), ("fp32", H.PRECISION_FP32)):
+        opts = H.default_options(device=device, precision=prec, autotune=1 if args.autotune else 0)
+        with H.Batch2D(probs, options=opts) as b:
+            b.advance(args.warmup)
+            b.restart()
+            l0 = b.kernel_launches()
+            barrier(ws)
+            clk = ClockSampler(device)
+            with clk:
+                st, ms = b.advance(args.steps)
+            launches = b.kernel_launches() - l0
+            assert all(s[0] == args.steps for s in st)
+            finals[name] = b.download()
+        ms = max_over_ranks(ms, ws)
+        res[name] = {"value": ws * cells * args.steps / (ms * 1e-3), "ms_per_step": ms / args.steps,
+                     "gpu_launches": int(launches), "clocks": clk.summary()}
+    num = np.zeros(4)
+    den = np.zeros(4)
+    for (W64, _), (W32, _), p in zip(finals["fp64"], finals["fp32"], probs):
+        g = p.g
+        num += np.abs(W32[:, g:-g, g:-g] - W64[:, g:-g, g:-g]).sum(axis=(1, 2))
+        den += np.abs(W64[:, g:-g, g:-g]).sum(axis=(1, 2))
+    l1 = num / den
+    if rank != 0:
+        return
+    main_form = "fp32" if args.precision == "fp32" else "fp64"
+    r = res[main_form]
+    pk = peaks()
+    bpc = BYTES_PER_CELL_FP64 if main_form == "fp64" else BYTES_PER_CELL_FP64 // 2
+    achieved = bpc * r["value"] / ws / 1e9
+    line = {
+        "metric": METRIC, "value": r["value"], "unit": "cell-updates/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_per_step"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if main_form == "fp64" else "f32",
+        "data": "synthetic (seeded four-quadrant ensemble)",
+        "config": {"workload": f"ensemble_{args.instances}x_four_quadrant_{main_form}",
+                   "instances": args.instances, "interior_cells": cells,
+                   "sides": [int(p.nx) for p in probs][:8] + ["..."],
+                   "limiter": "minmod", "cfl": 0.8, "boundaries": "transmissive",
+                   "steps_per_instance": args.steps, "autotune": bool(args.autotune)},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
+                     "frac": achieved / pk["hbm_gbs"], "traffic": None, "peak_source": pk["source"],
+                     "bytes_per_cell_update": bpc},
+        "forms": {"fp64": res["fp64"],
+                  "fp32": dict(res["fp32"], speedup_vs_fp64=res["fp32"]["value"] / res["fp64"]["value"],
+                               rel_l1_vs_fp64={"density": l1[0], "velocity_x": l1[1],
+                                               "velocity_y": l1[2], "pressure": l1[3]})},
+        "gpu_launches": r["gpu_launches"],
+        "clocks": r["clocks"],
+    }
+    print(json.dumps(line))
+
+
 def main() -> None:
     global N_SIDE, WORKLOAD
     ap = argparse.ArgumentParser()
@@ -215,8 +277,14 @@ def main() -> None:
                     help="grid side (the headline workload is 2048; smaller sizes are for profiling)")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"],
                     help="state precision of the timed path (fp64 is the drop-in)")
-    ap.add_argument("--workload", default="shear_layer", choices=["shear_layer", "point_blast"],
-                    help="shear_layer: MC, periodic, CFL 0.8; point_blast: Van Leer, reflective, CFL 0.4")
+    ap.add_argument("--workload", default="shear_layer",
+                    choices=["shear_layer", "point_blast", "ensemble"],
+                    help="shear_layer: MC, periodic, CFL 0.8; point_blast: Van Leer, reflective, "
+                         "CFL 0.4; ensemble: 256 four-quadrant problems, side log-uniform in "
+                         "[128, 1024], minmod, transmissive, one launch per step for all")
+    ap.add_argument("--instances", type=int, default=256, help="ensemble size")
+    ap.add_argument("--autotune", action="store_true",
+                    help="let the library time work-item shapes before stepping")
     ap.add_argument("--compare", action="store_true",
                     help="also run the other precision on the same steps and report the relative "
                          "L1 error per field and the conserved-total drift of both")
@@ -239,6 +307,9 @@ def main() -> None:
         from hydrofv_gb300 import build as B
         B.build()
     from hydrofv_gb300.problems import point_blast, shear_layer
+    if args.workload == "ensemble":
+        run_ensemble(args, H, local, ws, rank)
+        return
 
     device = local
     prec = H.PRECISION_FP32 if args.precision == "fp32" else H.PRECISION_FP64

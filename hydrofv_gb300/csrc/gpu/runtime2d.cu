@@ -24,7 +24,10 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <new>
+#include <tuple>
 
 #include "gpu_bridge.h"
 #include "gpu_internal.h"
@@ -325,6 +328,111 @@ static int recompute_active(HydroStepControl *c)
            c->error_code == 0;
 }
 
+/* ------------------------------------------------------------ autotuner */
+
+/* Work-item shape (rows per item) and persistent grid size are tuned on the
+ * run's own state: each candidate runs one warm-up and two timed steps from
+ * the initial state (CUDA events), the fastest is kept, the state is rewound
+ * and the choice is cached for the process per (precision, limiter, order,
+ * grid shape). */
+namespace {
+std::mutex g_tune_mutex;
+std::map<std::tuple<int, int, int, int, int>, std::pair<int, int>> g_tune_cache;
+}
+
+static void set_shape(HydroRun2D *run, int chunk, int ctas)
+{
+    run->args.chunk_h = run->args32.chunk_h = chunk;
+    run->args.grid_ctas = run->args32.grid_ctas = ctas;
+    if (run->graph) {
+        cudaGraphExecDestroy(run->graph);
+        run->graph = nullptr;
+    }
+}
+
+static int ensure_initial_copy(HydroRun2D *run, HydroRunOutcome *oc)
+{
+    const size_t fbytes = run->ncell * run->elem;
+    if (!run->init_slab) {
+        CK(cudaMalloc(&run->init_slab, 8 * fbytes), "cudaMalloc(initial state)");
+        for (int q = 0; q < 4; q++) {
+            run->init_U[q] = static_cast<char *>(run->init_slab) + q * fbytes;
+            run->init_W[q] = static_cast<char *>(run->init_slab) + (4 + q) * fbytes;
+        }
+    }
+    if (!run->have_initial) {
+        for (int q = 0; q < 4; q++) {
+            CK(cudaMemcpyAsync(run->init_U[q], fieldU(run, 0, q), fbytes, cudaMemcpyDeviceToDevice, run->stream), "D2D");
+            CK(cudaMemcpyAsync(run->init_W[q], fieldW(run, 0, q), fbytes, cudaMemcpyDeviceToDevice, run->stream), "D2D");
+        }
+        run->have_initial = true;
+    }
+    return 0;
+}
+
+static int autotune(HydroRun2D *run, const HydroStepParams *sp, HydroRunOutcome *oc)
+{
+    const auto key = std::make_tuple(run->fp32, run->grid.limiter, run->args.first_order + 2 * run->args32.first_order,
+                                     run->grid.nx, run->grid.ny);
+    {
+        std::lock_guard<std::mutex> lock(g_tune_mutex);
+        auto it = g_tune_cache.find(key);
+        if (it != g_tune_cache.end()) {
+            set_shape(run, it->second.first, it->second.second);
+            return 0;
+        }
+    }
+    if (ensure_initial_copy(run, oc)) return -1;
+    const int resident = run->fp32 ? run->args32.grid_ctas : run->args.grid_ctas;
+    const int storing = run->args.sp.is_storing;
+    run->args.sp.is_storing = run->args32.sp.is_storing = 0;
+    const int chunks[] = { 8, 16, 32, 64 };
+    int best_chunk = 32, best_ctas = resident;
+    float best_ms = 1e30f;
+    HydroStepControl *c = run->ctrl_h;
+    const unsigned long long ninf = ordered_bits(-INFINITY);
+    for (int ci = 0; ci < 4; ci++) {
+        for (int half = 0; half < 2; half++) {
+            const int ctas = half ? (resident / 2 > 0 ? resident / 2 : 1) : resident;
+            set_shape(run, chunks[ci], ctas);
+            memset(c, 0, sizeof *c);
+            c->tf = 1e300;
+            c->max_steps = 3;
+            for (int k = 0; k < 3; k++) c->smax[k][0] = c->smax[k][1] = ninf;
+            c->active = 1;
+            CK(cudaMemcpyAsync(run->ctrl_d, c, sizeof *c, cudaMemcpyHostToDevice, run->stream), "H2D control");
+            CK(run->fp32 ? mh2d_launch_prepare<float>(run->args32, run->stream)
+                         : mh2d_launch_prepare<double>(run->args, run->stream), "prepare kernel");
+            CK(launch_step(run), "step kernel");
+            CK(cudaEventRecord(run->ev[2], run->stream), "cudaEventRecord");
+            CK(launch_step(run), "step kernel");
+            CK(launch_step(run), "step kernel");
+            CK(cudaEventRecord(run->ev[3], run->stream), "cudaEventRecord");
+            CK(cudaEventSynchronize(run->ev[3]), "autotune");
+            run->kernel_launches += 4;
+            float ms = 0;
+            CK(cudaEventElapsedTime(&ms, run->ev[2], run->ev[3]), "cudaEventElapsedTime");
+            if (ms < best_ms) {
+                best_ms = ms;
+                best_chunk = chunks[ci];
+                best_ctas = ctas;
+            }
+            /* rewind: the buffers the candidate wrote */
+            const size_t fbytes = run->ncell * run->elem;
+            for (int q = 0; q < 4; q++) {
+                CK(cudaMemcpyAsync(fieldU(run, 0, q), run->init_U[q], fbytes, cudaMemcpyDeviceToDevice, run->stream), "D2D");
+                CK(cudaMemcpyAsync(fieldU(run, 1, q), run->init_U[q], fbytes, cudaMemcpyDeviceToDevice, run->stream), "D2D");
+                CK(cudaMemcpyAsync(fieldW(run, 0, q), run->init_W[q], fbytes, cudaMemcpyDeviceToDevice, run->stream), "D2D");
+            }
+        }
+    }
+    set_shape(run, best_chunk, best_ctas);
+    run->args.sp.is_storing = run->args32.sp.is_storing = storing;
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    g_tune_cache[key] = std::make_pair(best_chunk, best_ctas);
+    return 0;
+}
+
 extern "C" int hydro_run2d_begin(HydroRun2D *run, const HydroStepParams *sp, double tf,
                                  int64 max_steps, int store_count, HydroRunOutcome *oc)
 {
@@ -332,6 +440,7 @@ extern "C" int hydro_run2d_begin(HydroRun2D *run, const HydroStepParams *sp, dou
     CK(cudaSetDevice(run->device), "cudaSetDevice");
     run->args.sp = *sp;
     run->args32.sp = *sp;
+    if (run->opt.autotune && autotune(run, sp, oc)) return -1;
     HydroStepControl *c = run->ctrl_h;
     memset(c, 0, sizeof *c);
     c->tf = tf;

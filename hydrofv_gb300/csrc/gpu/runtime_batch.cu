@@ -75,6 +75,7 @@ struct HydroBatch2D {
     std::vector<Mh2dArgs<double>> a64;
     std::vector<Mh2dArgs<float>> a32;
     int grid_ctas = 0;
+    bool tuned = false;
     cudaGraphExec_t graph = nullptr;
     cudaEvent_t ev[2] = {};
     double step_ms = 0;
@@ -291,55 +292,6 @@ static int active(const HydroStepControl &c)
     return (c.t < c.tf) && (c.max_steps < 0 || c.num_steps < c.max_steps) && !c.error_code;
 }
 
-extern "C" int hydro_batch2d_begin(HydroBatch2D *b, const HydroStepParams *sp, double tf, int64 max_steps,
-                                   HydroRunOutcome *oc)
-{
-    memset(oc, 0, sizeof *oc);
-    BK(cudaSetDevice(b->device), "cudaSetDevice");
-    HydroStepParams p = *sp;
-    p.is_storing = 0;
-    const unsigned long long ninf = ordered_bits(-INFINITY);
-    for (int k = 0; k < b->n; k++) {
-        HydroStepControl &c = b->ctrl_h[k];
-        memset(&c, 0, sizeof c);
-        c.tf = tf;
-        c.max_steps = max_steps;
-        for (int j = 0; j < 3; j++) c.smax[j][0] = c.smax[j][1] = ninf;
-        c.active = active(c);
-    }
-    if (push(b, oc)) return -1;
-    if (b->fp32) {
-        for (auto &a : b->a32) a.sp = p;
-        BK(cudaMemcpyAsync(b->args_d, b->a32.data(), b->n * sizeof(Mh2dArgs<float>), cudaMemcpyHostToDevice,
-                           b->stream), "H2D args");
-        for (auto &a : b->a32) BK(mh2d_launch_prepare<float>(a, b->stream), "prepare kernel");
-    } else {
-        for (auto &a : b->a64) a.sp = p;
-        BK(cudaMemcpyAsync(b->args_d, b->a64.data(), b->n * sizeof(Mh2dArgs<double>), cudaMemcpyHostToDevice,
-                           b->stream), "H2D args");
-        for (auto &a : b->a64) BK(mh2d_launch_prepare<double>(a, b->stream), "prepare kernel");
-    }
-    b->launches += b->n;
-    BK(cudaStreamSynchronize(b->stream), "prepare");
-    return 0;
-}
-
-extern "C" int hydro_batch2d_set_limits(HydroBatch2D *b, double tf, int64 max_steps_more, HydroRunOutcome *oc)
-{
-    memset(oc, 0, sizeof *oc);
-    BK(cudaSetDevice(b->device), "cudaSetDevice");
-    if (pull(b, oc)) return -1;
-    for (int k = 0; k < b->n; k++) {
-        HydroStepControl &c = b->ctrl_h[k];
-        c.tf = tf;
-        c.max_steps = c.num_steps + max_steps_more;
-        c.active = active(c);
-    }
-    if (push(b, oc)) return -1;
-    BK(cudaStreamSynchronize(b->stream), "set limits");
-    return 0;
-}
-
 static cudaError_t launch_batch(HydroBatch2D *b)
 {
     if (b->fp32) {
@@ -358,6 +310,132 @@ static cudaError_t launch_batch(HydroBatch2D *b)
     a.total_items = b->item_off[b->n];
     a.bctrl = b->bctrl_d;
     return mh2d_launch_batch_step<double>(a, b->limiter, b->first_order, b->grid_ctas, b->stream);
+}
+
+/* Rows per work item for every instance: item table and arguments. */
+static int set_chunk(HydroBatch2D *b, int chunk, int ctas, HydroRunOutcome *oc)
+{
+    b->item_off[0] = 0;
+    for (int k = 0; k < b->n; k++) {
+        const int nx = b->fp32 ? b->a32[k].nx : b->a64[k].nx;
+        const int ny = b->fp32 ? b->a32[k].ny : b->a64[k].ny;
+        b->item_off[k + 1] = b->item_off[k] + ((nx + MH2D_THREADS - 3) / (MH2D_THREADS - 2)) * ((ny + chunk - 1) / chunk);
+        if (b->fp32) b->a32[k].chunk_h = chunk;
+        else b->a64[k].chunk_h = chunk;
+    }
+    BK(cudaMemcpyAsync(b->item_off_d, b->item_off.data(), (b->n + 1) * sizeof(int), cudaMemcpyHostToDevice,
+                       b->stream), "H2D items");
+    if (b->fp32)
+        BK(cudaMemcpyAsync(b->args_d, b->a32.data(), b->n * sizeof(Mh2dArgs<float>), cudaMemcpyHostToDevice,
+                           b->stream), "H2D args");
+    else
+        BK(cudaMemcpyAsync(b->args_d, b->a64.data(), b->n * sizeof(Mh2dArgs<double>), cudaMemcpyHostToDevice,
+                           b->stream), "H2D args");
+    b->grid_ctas = std::min(ctas, b->item_off[b->n]);
+    if (b->graph) {
+        cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+    }
+    BK(cudaStreamSynchronize(b->stream), "set chunk");
+    return 0;
+}
+
+static int batch_prepare_all(HydroBatch2D *b, double tf, int64 max_steps, HydroRunOutcome *oc);
+
+/* Time candidate (rows per item, persistent CTAs) pairs on the batch's own
+ * initial state, keep the fastest, rewind (see runtime2d.cu). */
+static int batch_autotune(HydroBatch2D *b, HydroRunOutcome *oc)
+{
+    int resident = b->fp32 ? mh2d_resident_ctas<float>(b->limiter, b->first_order, b->device)
+                           : mh2d_resident_ctas<double>(b->limiter, b->first_order, b->device);
+    if (resident <= 0) resident = b->grid_ctas;
+    const int chunks[] = { 8, 16, 32, 64 };
+    int best_chunk = 32, best_ctas = resident;
+    float best_ms = 1e30f;
+    for (int ci = 0; ci < 4; ci++) {
+        for (int half = 0; half < 2; half++) {
+            const int ctas = half ? std::max(1, resident / 2) : resident;
+            if (set_chunk(b, chunks[ci], ctas, oc)) return -1;
+            if (batch_prepare_all(b, 1e300, 3, oc)) return -1;
+            BK(launch_batch(b), "batch step kernel");
+            BK(cudaEventRecord(b->ev[0], b->stream), "cudaEventRecord");
+            BK(launch_batch(b), "batch step kernel");
+            BK(launch_batch(b), "batch step kernel");
+            BK(cudaEventRecord(b->ev[1], b->stream), "cudaEventRecord");
+            BK(cudaEventSynchronize(b->ev[1]), "autotune");
+            b->launches += 3;
+            float ms = 0;
+            BK(cudaEventElapsedTime(&ms, b->ev[0], b->ev[1]), "cudaEventElapsedTime");
+            if (ms < best_ms) {
+                best_ms = ms;
+                best_chunk = chunks[ci];
+                best_ctas = ctas;
+            }
+            if (hydro_batch2d_restore(b, oc)) return -1;
+        }
+    }
+    return set_chunk(b, best_chunk, best_ctas, oc);
+}
+
+static int batch_prepare_all(HydroBatch2D *b, double tf, int64 max_steps, HydroRunOutcome *oc)
+{
+    const unsigned long long ninf = ordered_bits(-INFINITY);
+    for (int k = 0; k < b->n; k++) {
+        HydroStepControl &c = b->ctrl_h[k];
+        memset(&c, 0, sizeof c);
+        c.tf = tf;
+        c.max_steps = max_steps;
+        for (int j = 0; j < 3; j++) c.smax[j][0] = c.smax[j][1] = ninf;
+        c.active = active(c);
+    }
+    if (push(b, oc)) return -1;
+    if (b->fp32) {
+        for (auto &a : b->a32) BK(mh2d_launch_prepare<float>(a, b->stream), "prepare kernel");
+    } else {
+        for (auto &a : b->a64) BK(mh2d_launch_prepare<double>(a, b->stream), "prepare kernel");
+    }
+    b->launches += b->n;
+    BK(cudaStreamSynchronize(b->stream), "prepare");
+    return 0;
+}
+
+extern "C" int hydro_batch2d_begin(HydroBatch2D *b, const HydroStepParams *sp, double tf, int64 max_steps,
+                                   HydroRunOutcome *oc)
+{
+    memset(oc, 0, sizeof *oc);
+    BK(cudaSetDevice(b->device), "cudaSetDevice");
+    HydroStepParams p = *sp;
+    p.is_storing = 0;
+    if (b->fp32) {
+        for (auto &a : b->a32) a.sp = p;
+        BK(cudaMemcpyAsync(b->args_d, b->a32.data(), b->n * sizeof(Mh2dArgs<float>), cudaMemcpyHostToDevice,
+                           b->stream), "H2D args");
+    } else {
+        for (auto &a : b->a64) a.sp = p;
+        BK(cudaMemcpyAsync(b->args_d, b->a64.data(), b->n * sizeof(Mh2dArgs<double>), cudaMemcpyHostToDevice,
+                           b->stream), "H2D args");
+    }
+    if (b->opt.autotune && !b->tuned) {
+        if (batch_autotune(b, oc)) return -1;
+        b->tuned = true;
+    }
+    return batch_prepare_all(b, tf, max_steps, oc);
+}
+
+extern "C" int hydro_batch2d_set_limits(HydroBatch2D *b, double tf, int64 max_steps_more, HydroRunOutcome *oc)
+{
+    memset(oc, 0, sizeof *oc);
+    BK(cudaSetDevice(b->device), "cudaSetDevice");
+    if (pull(b, oc)) return -1;
+    for (int k = 0; k < b->n; k++) {
+        HydroStepControl &c = b->ctrl_h[k];
+        c.tf = tf;
+        c.max_steps = c.num_steps + max_steps_more;
+        c.active = active(c);
+    }
+    if (push(b, oc)) return -1;
+    BK(cudaStreamSynchronize(b->stream), "set limits");
+    return 0;
 }
 
 extern "C" int hydro_batch2d_advance(HydroBatch2D *b, HydroRunOutcome *oc, double *step_ms)

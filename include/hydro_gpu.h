@@ -37,7 +37,11 @@ typedef struct HydroGpuOptions
     int chunk_steps;        /* steps enqueued between host polls (0: auto) */
     int use_graph;          /* replay step chunks as CUDA graphs (default 1) */
     int block_threads;      /* threads per step CTA (0: tuned default) */
-    int chunk_rows;         /* grid rows per step CTA (0: tuned default) */
+    int chunk_rows;         /* grid rows per step work item (0: default 32) */
+    int autotune;           /* 1: before the first step, time candidate work-item
+                               shapes and persistent grid sizes on the actual
+                               state (then rewind) and keep the fastest; cached
+                               per shape for the process */
 } HydroGpuOptions;
 
 typedef struct HydroGpuStats
@@ -54,7 +58,7 @@ typedef struct HydroGpuStats
     int64 interior_cells;   /* cells updated per step */
 } HydroGpuStats;
 
-/* Defaults: device 0, no step limit, FP64, auto chunking, graphs on. */
+/* Defaults: device 0, no step limit, FP64, auto chunking, graphs on, no autotuning. */
 HydroGpuOptions hydro_gpu_default_options(void);
 
 /* Options used by plain launch_simulation() in this process.  Lets programs

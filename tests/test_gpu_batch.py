@@ -80,3 +80,22 @@ def test_batch_against_oracle_sample(gpu_available, oracle_mod):
         assert ref.rc == 0
         l1 = oracle_mod.rel_l1(outs[k][1], ref.U, probs[k].g)
         assert np.all(l1 <= 1e-12), l1
+
+
+def test_autotune_changes_schedule_not_results(gpu_available):
+    """The autotuner only picks work-item shapes and grid sizes."""
+    p = shear_layer(300, steps=12)
+    ref = single(p)
+    r = H.run_2d(p.nx, p.ny, p.g, (0, 1, 0, 1), p.gamma, p.W, p.U, bc=p.bc,
+                 slope_limiter=p.slope_limiter, cfl=p.cfl, tf=p.tf, max_steps=p.max_steps,
+                 options=H.default_options(autotune=1))
+    assert r.code == 0, r.message
+    assert np.array_equal(r.U, ref.U, equal_nan=True)
+    probs = four_quadrant_ensemble(count=6, steps=10, side_range=(40, 300))
+    outs = []
+    for tune in (0, 1):
+        with H.Batch2D(probs, options=H.default_options(autotune=tune)) as b:
+            b.advance(10)
+            outs.append(b.download())
+    for (W0, U0), (W1, U1) in zip(*outs):
+        assert np.array_equal(U0, U1, equal_nan=True)
