@@ -100,6 +100,16 @@ class HydroGpuOptions(C.Structure):
     ]
 
 
+class HydroGpuAdjointStats(C.Structure):
+    _fields_ = [
+        ("forward_ms", C.c_double), ("recompute_ms", C.c_double), ("vjp_ms", C.c_double),
+        ("tangent_ms", C.c_double), ("replay_ms", C.c_double), ("steps", C.c_int64),
+        ("checkpoint_every", C.c_int64), ("checkpoints", C.c_int64),
+        ("recompute_mismatches", C.c_int64), ("kernel_launches", C.c_int64),
+        ("device_bytes", C.c_int64), ("interior_cells", C.c_int64),
+    ]
+
+
 class HydroGpuStats(C.Structure):
     _fields_ = [
         ("total_ms", C.c_double), ("h2d_ms", C.c_double), ("step_ms", C.c_double),
@@ -153,6 +163,26 @@ _SIGNATURES = {
     "hydro_gpu_batch_download": (ErrorStatus, [C.c_void_p, C.c_void_p]),
     "hydro_gpu_batch_kernel_launches": (C.c_int64, [C.c_void_p]),
     "hydro_gpu_batch_destroy": (None, [C.c_void_p]),
+    "hydro_gpu_adjoint_create": (ErrorStatus, [_P(C.c_void_p), _P(BoundaryConditionParam), _P(System),
+                                               _P(IntegratorParam), C.c_int64, C.c_int,
+                                               _P(HydroGpuOptions)]),
+    "hydro_gpu_adjoint_forward": (ErrorStatus, [C.c_void_p, C.c_void_p]),
+    "hydro_gpu_adjoint_backward": (ErrorStatus, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "hydro_gpu_adjoint_tangent": (ErrorStatus, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                                C.c_void_p]),
+    "hydro_gpu_adjoint_replay": (ErrorStatus, [C.c_void_p, C.c_void_p, C.c_void_p,
+                                               _P(C.c_uint64)]),
+    "hydro_gpu_adjoint_replay_frozen": (ErrorStatus, [C.c_void_p, C.c_void_p, C.c_void_p]),
+    "hydro_gpu_adjoint_dt": (ErrorStatus, [C.c_void_p, _dp]),
+    "hydro_gpu_adjoint_stats": (None, [C.c_void_p, _P(HydroGpuAdjointStats)]),
+    "hydro_gpu_adjoint_destroy": (None, [C.c_void_p]),
+    "hydro_ad_hllc_jvp": (C.c_int, [C.c_double, C.c_double] + [_dp] * 6),
+    "hydro_ad_hllc_vjp": (C.c_int, [C.c_double, C.c_double] + [_dp] * 5 + [_P(C.c_int)]),
+    "hydro_ad_recon_jvp": (None, [C.c_int, C.c_int, C.c_double, C.c_double] + [_dp] * 10),
+    "hydro_ad_recon_vjp": (None, [C.c_int, C.c_int, C.c_double, C.c_double] + [_dp] * 8),
+    "hydro_ad_hllc_forced": (None, [C.c_double, C.c_double, _dp, _dp, C.c_int, _dp]),
+    "hydro_ad_recon_forced": (None, [C.c_int, C.c_int, C.c_double, C.c_double, _dp, _dp, _dp, C.c_int,
+                                     _dp, _dp, _P(C.c_int)]),
     "hydro_gpu_device_count": (C.c_int, []),
     "hydro_gpu_calibrate": (C.c_int, [C.c_int, _dp, _dp]),
     "hydro_gpu_version": (C.c_char_p, []),
@@ -528,3 +558,184 @@ class Batch2D:
 
     def __exit__(self, *exc):
         self.close()
+
+
+# ---------------------------------------------------------------- adjoint
+
+def _ptr4(arrs):
+    """(double*)[4] array of pointers to four contiguous float64 arrays."""
+    t = (_dp * 4)()
+    for k, a in enumerate(arrs):
+        t[k] = a.ctypes.data_as(_dp)
+    return t
+
+
+class Adjoint2D:
+    """Discrete adjoint / tangent-linear session (hydro_gpu_adjoint_*) of the
+    2D MUSCL-Hancock + HLLC step: forward pass with checkpoints every
+    `checkpoint_every` steps, reverse pass, tangent-linear model and frozen-dt
+    replay.  Field arrays are (4, ny + 2G, nx + 2G) float64 in the order
+    (rho, vx, vy, p); interior entries are read, ghost entries of outputs
+    are 0."""
+
+    def __init__(self, problem, steps: int, checkpoint_every: int,
+                 options: HydroGpuOptions | None = None):
+        self.lib = lib = library()
+        p = problem
+        self.shape = (4, p.ny + 2 * p.g, p.nx + 2 * p.g)
+        self.steps = int(steps)
+        self._h = _SystemHandle(lib, "cartesian_2d", p.nx, p.ny, p.g,
+                                (p.x_min, p.x_max, p.y_min, p.y_max), p.gamma)
+        for dst, src in zip(self._h.fields(W2), p.W):
+            dst[:] = np.ascontiguousarray(src).reshape(-1)
+        for dst, src in zip(self._h.fields(U2), p.U):
+            dst[:] = np.ascontiguousarray(src).reshape(-1)
+        self._keep: list = []
+        bcp, ip = _params(lib, p.bc, p.integrator, p.riemann_solver, p.slope_limiter, p.cfl,
+                          self._keep)
+        self._bcp, self._ip = bcp, ip
+        opt = options if options is not None else lib.hydro_gpu_default_options()
+        self.handle = C.c_void_p()
+        code, msg = _consume(lib, lib.hydro_gpu_adjoint_create(
+            C.byref(self.handle), C.byref(bcp), C.byref(self._h.s), C.byref(ip), self.steps,
+            int(checkpoint_every), C.byref(opt)))
+        if code != 0:
+            raise HydroError(code, msg)
+
+    def _check(self, e):
+        code, msg = _consume(self.lib, e)
+        if code != 0:
+            raise HydroError(code, msg)
+
+    def _empty(self):
+        return np.zeros(self.shape)
+
+    def _in(self, W):
+        W = np.ascontiguousarray(W, dtype=np.float64)
+        if W.shape != self.shape:
+            raise ValueError(f"expected shape {self.shape}, got {W.shape}")
+        return W
+
+    def forward(self) -> np.ndarray:
+        """Run the forward pass; returns W^N (interior)."""
+        out = self._empty()
+        self._check(self.lib.hydro_gpu_adjoint_forward(self.handle, _ptr4(out)))
+        return out
+
+    def backward(self, seed: np.ndarray) -> np.ndarray:
+        """dJ/dW0 for seed = dJ/dW^N."""
+        seed = self._in(seed)
+        grad = self._empty()
+        self._check(self.lib.hydro_gpu_adjoint_backward(self.handle, _ptr4(seed), _ptr4(grad)))
+        return grad
+
+    def tangent(self, dw0: np.ndarray, w0: np.ndarray | None = None):
+        """(W^N, dW^N) of the tangent-linear model in direction dw0."""
+        dw0 = self._in(dw0)
+        wN, dwN = self._empty(), self._empty()
+        w0p = _ptr4(self._in(w0)) if w0 is not None else None
+        self._keep_w0 = w0
+        self._check(self.lib.hydro_gpu_adjoint_tangent(self.handle, w0p, _ptr4(dw0), _ptr4(wN),
+                                                       _ptr4(dwN)))
+        return wN, dwN
+
+    def replay(self, w0: np.ndarray, signatures: bool = True):
+        """(W^N, per-step branch signatures) of the frozen-dt replay from w0."""
+        w0 = self._in(w0)
+        wN = self._empty()
+        sig = np.zeros(self.steps, dtype=np.uint64) if signatures else None
+        sp = sig.ctypes.data_as(C.POINTER(C.c_uint64)) if sig is not None else None
+        self._check(self.lib.hydro_gpu_adjoint_replay(self.handle, _ptr4(w0), _ptr4(wN), sp))
+        return wN, sig
+
+    def replay_frozen(self, w0: np.ndarray) -> np.ndarray:
+        """W^N of the replay from w0 with the forward pass's dt AND branch
+        decisions forced (the map the adjoint differentiates)."""
+        w0 = self._in(w0)
+        wN = self._empty()
+        self._check(self.lib.hydro_gpu_adjoint_replay_frozen(self.handle, _ptr4(w0), _ptr4(wN)))
+        return wN
+
+    def dt(self) -> np.ndarray:
+        out = np.zeros(self.steps)
+        self._check(self.lib.hydro_gpu_adjoint_dt(self.handle, out.ctypes.data_as(_dp)))
+        return out
+
+    def stats(self) -> dict:
+        st = HydroGpuAdjointStats()
+        self.lib.hydro_gpu_adjoint_stats(self.handle, C.byref(st))
+        return {name: getattr(st, name) for name, _ in HydroGpuAdjointStats._fields_}
+
+    def close(self):
+        if self.handle:
+            self.lib.hydro_gpu_adjoint_destroy(self.handle)
+            self.handle = C.c_void_p()
+        self._h.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+def _vec(x):
+    return np.ascontiguousarray(x, dtype=np.float64).reshape(4)
+
+
+def ad_hllc_jvp(gamma, tol, L, R, dL, dR):
+    """(F, dF, code) of the HLLC 2D flux in tangent mode (host build)."""
+    F, dF = np.zeros(4), np.zeros(4)
+    args = [_vec(a) for a in (L, R, dL, dR)]
+    rc = library().hydro_ad_hllc_jvp(gamma, tol, *[a.ctypes.data_as(_dp) for a in args],
+                                     F.ctypes.data_as(_dp), dF.ctypes.data_as(_dp))
+    return F, dF, rc
+
+
+def ad_hllc_vjp(gamma, tol, L, R, Fb):
+    """(Lb, Rb, rc, branch code) of the HLLC 2D flux in reverse mode (host build)."""
+    Lb, Rb = np.zeros(4), np.zeros(4)
+    code = C.c_int(0)
+    args = [_vec(a) for a in (L, R, Fb)]
+    rc = library().hydro_ad_hllc_vjp(gamma, tol, *[a.ctypes.data_as(_dp) for a in args],
+                                     Lb.ctypes.data_as(_dp), Rb.ctypes.data_as(_dp), C.byref(code))
+    return Lb, Rb, rc, code.value
+
+
+def ad_recon_jvp(limiter, direction, gamma, dtA, wm, w0, wp, dwm, dw0, dwp):
+    """(lo, hi, dlo, dhi) of one cell's reconstruction in tangent mode."""
+    outs = [np.zeros(4) for _ in range(4)]
+    args = [_vec(a) for a in (wm, w0, wp, dwm, dw0, dwp)]
+    library().hydro_ad_recon_jvp(limiter, direction, gamma, dtA,
+                                 *[a.ctypes.data_as(_dp) for a in args],
+                                 *[o.ctypes.data_as(_dp) for o in outs])
+    return tuple(outs)
+
+
+def ad_recon_vjp(limiter, direction, gamma, dtA, wm, w0, wp, lob, hib):
+    """(wmb, w0b, wpb) of one cell's reconstruction in reverse mode."""
+    outs = [np.zeros(4) for _ in range(3)]
+    args = [_vec(a) for a in (wm, w0, wp, lob, hib)]
+    library().hydro_ad_recon_vjp(limiter, direction, gamma, dtA,
+                                 *[a.ctypes.data_as(_dp) for a in args],
+                                 *[o.ctypes.data_as(_dp) for o in outs])
+    return tuple(outs)
+
+
+def ad_hllc_forced(gamma, tol, L, R, code):
+    """HLLC 2D flux with the branch code given (host build)."""
+    F = np.zeros(4)
+    L, R = _vec(L), _vec(R)
+    library().hydro_ad_hllc_forced(gamma, tol, L.ctypes.data_as(_dp), R.ctypes.data_as(_dp), int(code),
+                                   F.ctypes.data_as(_dp))
+    return F
+
+
+def ad_recon_forced(limiter, direction, gamma, dtA, wm, w0, wp, code):
+    """(lo, hi, natural code) of one cell's reconstruction with the limiter cases given."""
+    lo, hi = np.zeros(4), np.zeros(4)
+    nat = C.c_int(0)
+    args = [_vec(a) for a in (wm, w0, wp)]
+    library().hydro_ad_recon_forced(limiter, direction, gamma, dtA, *[a.ctypes.data_as(_dp) for a in args],
+                                    int(code), lo.ctypes.data_as(_dp), hi.ctypes.data_as(_dp), C.byref(nat))
+    return lo, hi, nat.value

@@ -37,6 +37,8 @@ CUDA_SOURCES = [
     ("gpu/calibrate.cu", []),
     ("gpu/noalloc2d.cu", []),
     ("gpu/run1d.cu", ["--fmad=false"]),
+    ("gpu/adjoint2d.cu", ["--fmad=false"]),
+    ("gpu/ad_pointwise.cu", ["--fmad=false"]),
 ]
 C_SOURCES = [
     "host/error.c",

@@ -96,6 +96,21 @@ int hydro_batch2d_download(HydroBatch2D *b, int i, double *const W[4], double *c
 void hydro_batch2d_stats(const HydroBatch2D *b, HydroGpuStats *stats);
 void hydro_batch2d_destroy(HydroBatch2D *b);
 
+/* Discrete adjoint / tangent-linear session of the 2D MUSCL-Hancock step. */
+typedef struct HydroAdj2D HydroAdj2D;
+int hydro_adj2d_create(const HydroGrid2D *grid, const HydroGpuOptions *opt, const HydroStepParams *sp,
+                       int64 num_steps, int checkpoint_every, double *const W0[4],
+                       HydroAdj2D **out, HydroRunOutcome *oc);
+int hydro_adj2d_forward(HydroAdj2D *a, double *const W[4], double *const U[4], HydroRunOutcome *oc);
+int hydro_adj2d_backward(HydroAdj2D *a, double *const seed[4], double *const grad[4], HydroRunOutcome *oc);
+int hydro_adj2d_tangent(HydroAdj2D *a, double *const w0[4], double *const dw0[4],
+                        double *const wN[4], double *const dwN[4], HydroRunOutcome *oc);
+int hydro_adj2d_replay(HydroAdj2D *a, double *const w0[4], double *const wN[4],
+                       unsigned long long *signatures, int frozen, HydroRunOutcome *oc);
+int hydro_adj2d_dt(const HydroAdj2D *a, double *dt);
+void hydro_adj2d_stats(const HydroAdj2D *a, HydroGpuAdjointStats *st);
+void hydro_adj2d_destroy(HydroAdj2D *a);
+
 /* 1D Cartesian problem (Godunov first order or MUSCL-Hancock). */
 typedef struct HydroGrid1D
 {

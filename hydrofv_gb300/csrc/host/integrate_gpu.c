@@ -759,3 +759,108 @@ void hydro_gpu_batch_destroy(HydroGpuBatch *bt)
     hydro_batch2d_destroy(bt->b);
     free(bt);
 }
+
+/* ------------------------------------------------------------- adjoint */
+
+struct HydroGpuAdjoint
+{
+    HydroAdj2D *adj;
+};
+
+ErrorStatus hydro_gpu_adjoint_create(
+    HydroGpuAdjoint **out,
+    BoundaryConditionParam *__restrict bcp,
+    System *__restrict system,
+    IntegratorParam *__restrict ip,
+    int64 num_steps,
+    int checkpoint_every,
+    const HydroGpuOptions *options
+)
+{
+    *out = NULL;
+    ErrorStatus e = WRAP_TRACEBACK(finalize_boundary_condition_param(system, bcp));
+    if (e.return_code != SUCCESS) return e;
+    e = WRAP_TRACEBACK(finalize_integrator_param(ip));
+    if (e.return_code != SUCCESS) return e;
+    if (ip->integrator_flag_ != INTEGRATOR_MUSCL_HANCOCK_2D)
+        return WRAP_RAISE_ERROR(NOT_IMPLEMENTED_ERROR, "The adjoint differentiates muscl_hancock_2d.");
+    if (system->num_ghost_cells_side < 2)
+        return WRAP_RAISE_ERROR(VALUE_ERROR, "Number of ghost cells must be at least 2.");
+    if (num_steps < 1 || checkpoint_every < 1)
+        return WRAP_RAISE_ERROR(VALUE_ERROR, "num_steps and checkpoint_every must be at least 1.");
+    HydroGrid2D grid;
+    memset(&grid, 0, sizeof grid);
+    e = setup_grid2d(bcp, system, ip, &grid);
+    if (e.return_code != SUCCESS) return e;
+    HydroGpuAdjoint *ad = calloc(1, sizeof *ad);
+    if (!ad) return WRAP_RAISE_ERROR(MEMORY_ERROR, "Failed to allocate the adjoint session.");
+    const HydroGpuOptions opt = options ? *options : hydro_gpu_default_options();
+    StoringParam none = get_new_storing_param();
+    const HydroStepParams params = step_params(ip, &none);
+    double *W[4] = { system->density_, system->velocity_x_, system->velocity_y_, system->pressure_ };
+    HydroRunOutcome oc;
+    if (hydro_adj2d_create(&grid, &opt, &params, num_steps, checkpoint_every, W, &ad->adj, &oc) != 0)
+    {
+        hydro_adj2d_destroy(ad->adj);
+        free(ad);
+        return outcome_error(&oc);
+    }
+    *out = ad;
+    return make_success_error_status();
+}
+
+ErrorStatus hydro_gpu_adjoint_forward(HydroGpuAdjoint *ad, double *const W_final[4])
+{
+    HydroRunOutcome oc;
+    if (hydro_adj2d_forward(ad->adj, W_final, NULL, &oc) != 0) return outcome_error(&oc);
+    return make_success_error_status();
+}
+
+ErrorStatus hydro_gpu_adjoint_backward(HydroGpuAdjoint *ad, double *const seed[4], double *const grad[4])
+{
+    HydroRunOutcome oc;
+    if (hydro_adj2d_backward(ad->adj, seed, grad, &oc) != 0) return outcome_error(&oc);
+    return make_success_error_status();
+}
+
+ErrorStatus hydro_gpu_adjoint_tangent(HydroGpuAdjoint *ad, double *const w0[4], double *const dw0[4],
+                                      double *const w_final[4], double *const dw_final[4])
+{
+    HydroRunOutcome oc;
+    if (hydro_adj2d_tangent(ad->adj, w0, dw0, w_final, dw_final, &oc) != 0) return outcome_error(&oc);
+    return make_success_error_status();
+}
+
+ErrorStatus hydro_gpu_adjoint_replay(HydroGpuAdjoint *ad, double *const w0[4], double *const w_final[4],
+                                     unsigned long long *signatures)
+{
+    HydroRunOutcome oc;
+    if (hydro_adj2d_replay(ad->adj, w0, w_final, signatures, 0, &oc) != 0) return outcome_error(&oc);
+    return make_success_error_status();
+}
+
+ErrorStatus hydro_gpu_adjoint_replay_frozen(HydroGpuAdjoint *ad, double *const w0[4], double *const w_final[4])
+{
+    HydroRunOutcome oc;
+    if (hydro_adj2d_replay(ad->adj, w0, w_final, NULL, 1, &oc) != 0) return outcome_error(&oc);
+    return make_success_error_status();
+}
+
+ErrorStatus hydro_gpu_adjoint_dt(const HydroGpuAdjoint *ad, double *dt)
+{
+    if (hydro_adj2d_dt(ad->adj, dt) != 0)
+        return WRAP_RAISE_ERROR(VALUE_ERROR, "Run the forward pass first.");
+    return make_success_error_status();
+}
+
+void hydro_gpu_adjoint_stats(const HydroGpuAdjoint *ad, HydroGpuAdjointStats *stats)
+{
+    hydro_adj2d_stats(ad->adj, stats);
+}
+
+void hydro_gpu_adjoint_destroy(HydroGpuAdjoint *ad)
+{
+    if (!ad) return;
+    hydro_adj2d_destroy(ad->adj);
+    free(ad);
+}

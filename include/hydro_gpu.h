@@ -211,6 +211,118 @@ int hydro_gpu_muscl_hancock_2d_noalloc(
     int error_message_size
 );
 
+/* ------------------------------------------------------------------ */
+/* Discrete adjoint and tangent-linear model of the 2D MUSCL-Hancock + */
+/* HLLC step.  No counterpart in the reference.                        */
+/* ------------------------------------------------------------------ */
+
+/* The differentiated map: interior primitives W0 = (rho, vx, vy, p) of the
+ * System handed to hydro_gpu_adjoint_create -> W^N after num_steps steps.
+ * Ghost cells are images of the interior under the built-in boundary rules
+ * (reflective, transmissive or periodic on every side), U0 is W0 converted
+ * to conserved form, and every step uses the dt the forward pass chose (dt
+ * is frozen: the CFL reduction is not differentiated; tf is ignored and the
+ * run is exactly num_steps steps).  Limiter, Riemann-regime and region
+ * decisions are those of the evaluation being differentiated.
+ *
+ * All field arguments are the padded host layout of the System arrays
+ * ((nx + 2G) * (ny + 2G) doubles, row-major), in the order rho, vx, vy, p;
+ * interior entries are read, ghost entries of outputs are written as 0. */
+typedef struct HydroGpuAdjoint HydroGpuAdjoint;
+
+typedef struct HydroGpuAdjointStats
+{
+    double forward_ms;            /* CUDA-event time of the forward pass */
+    double recompute_ms;          /* last backward pass: segment recomputation */
+    double vjp_ms;                /* last backward pass: reverse sweep */
+    double tangent_ms;            /* last tangent-linear run */
+    double replay_ms;             /* last replay */
+    int64 steps;
+    int64 checkpoint_every;
+    int64 checkpoints;
+    int64 recompute_mismatches;   /* recomputed dt or state differing from the forward pass (0 expected) */
+    int64 kernel_launches;        /* kernels of this library launched by the session */
+    int64 device_bytes;           /* device memory held by the session */
+    int64 interior_cells;
+} HydroGpuAdjointStats;
+
+/* Finalize the parameters (muscl_hancock_2d with the HLLC solver, FP64),
+ * allocate checkpoint and segment storage (state copies at steps 0, K, 2K,
+ * ... with K = checkpoint_every, plus K resident states for recomputation)
+ * and upload the System's W arrays as W0. */
+ErrorStatus hydro_gpu_adjoint_create(
+    HydroGpuAdjoint **adjoint,
+    BoundaryConditionParam *__restrict boundary_condition_param,
+    System *__restrict system,
+    IntegratorParam *__restrict integrator_param,
+    int64 num_steps,
+    int checkpoint_every,
+    const HydroGpuOptions *options
+);
+
+/* Run the forward pass (the production step kernel) from W0, logging dt and
+ * storing checkpoints.  W_final (may be NULL) receives W^N. */
+ErrorStatus hydro_gpu_adjoint_forward(HydroGpuAdjoint *adjoint, double *const W_final[4]);
+
+/* Reverse pass: given seed = dJ/dW^N, write grad = dJ/dW0.  Segments are
+ * recomputed from their checkpoints and swept in reverse. */
+ErrorStatus hydro_gpu_adjoint_backward(HydroGpuAdjoint *adjoint, double *const seed[4],
+                                       double *const grad[4]);
+
+/* Tangent-linear model from W0 (or from w0 when not NULL) in direction dw0:
+ * dw_final = (dW^N/dW0) dw0; w_final (may be NULL) receives the primal W^N,
+ * which equals the forward pass's bit for bit when w0 is NULL. */
+ErrorStatus hydro_gpu_adjoint_tangent(HydroGpuAdjoint *adjoint, double *const w0[4],
+                                      double *const dw0[4], double *const w_final[4],
+                                      double *const dw_final[4]);
+
+/* Replay the num_steps steps from w0 with the forward pass's dt sequence
+ * (finite-difference checks of the frozen-dt map).  signatures (may be
+ * NULL, else num_steps entries) receives per step a hash sum of every
+ * limiter / regime / region decision: equal signatures mean (up to hash
+ * collisions) that the replay took the same branches. */
+ErrorStatus hydro_gpu_adjoint_replay(HydroGpuAdjoint *adjoint, double *const w0[4],
+                                     double *const w_final[4], unsigned long long *signatures);
+
+/* Replay from w0 with the forward pass's dt sequence AND its branch
+ * decisions (every limiter case, Riemann regime, guess floor, wave-speed
+ * branch and flux region, recorded once from W0): the exact map the adjoint
+ * differentiates, smooth around W0, for finite-difference checks that must
+ * not cross kinks.  With w0 = W0 it returns W^N bit for bit. */
+ErrorStatus hydro_gpu_adjoint_replay_frozen(HydroGpuAdjoint *adjoint, double *const w0[4],
+                                            double *const w_final[4]);
+
+/* dt of each forward step (num_steps entries). */
+ErrorStatus hydro_gpu_adjoint_dt(const HydroGpuAdjoint *adjoint, double *dt);
+
+void hydro_gpu_adjoint_stats(const HydroGpuAdjoint *adjoint, HydroGpuAdjointStats *stats);
+
+void hydro_gpu_adjoint_destroy(HydroGpuAdjoint *adjoint);
+
+/* Pointwise derivative kernels, host builds of the device code (for tests):
+ * HLLC 2D flux (states rho, u_normal, u_tangential, p) in tangent and
+ * reverse mode, and the cell reconstruction of one sweep direction
+ * (dir 0: x, 1: y; cells wm, w0, wp in storage order rho, vx, vy, p;
+ * limiter = SLOPE_LIMITER_*; lo / hi in sweep order). */
+int hydro_ad_hllc_jvp(double gamma, double tol, const double L[4], const double R[4],
+                      const double dL[4], const double dR[4], double F[4], double dF[4]);
+int hydro_ad_hllc_vjp(double gamma, double tol, const double L[4], const double R[4],
+                      const double Fb[4], double Lb[4], double Rb[4], int *branch_code);
+void hydro_ad_recon_jvp(int limiter, int dir, double gamma, double dtA, const double wm[4],
+                        const double w0[4], const double wp[4], const double dwm[4],
+                        const double dw0[4], const double dwp[4], double lo[4], double hi[4],
+                        double dlo[4], double dhi[4]);
+void hydro_ad_recon_vjp(int limiter, int dir, double gamma, double dtA, const double wm[4],
+                        const double w0[4], const double wp[4], const double lob[4],
+                        const double hib[4], double wmb[4], double w0b[4], double wpb[4]);
+/* The same two pieces with their branch decisions given (branch_code of
+ * hydro_ad_hllc_vjp; natural_code receives the reconstruction's own code). */
+void hydro_ad_hllc_forced(double gamma, double tol, const double L[4], const double R[4], int code,
+                          double F[4]);
+void hydro_ad_recon_forced(int limiter, int dir, double gamma, double dtA, const double wm[4],
+                           const double w0[4], const double wp[4], int code, double lo[4],
+                           double hi[4], int *natural_code);
+
 /* Number of visible CUDA devices (0 when none; never fails). */
 int hydro_gpu_device_count(void);
 

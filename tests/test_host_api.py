@@ -224,3 +224,11 @@ def test_no_cpu_fallback_without_gpu(hydro_lib, oracle_mod):
     assert r.num_steps == 0
     # host arrays untouched
     assert np.array_equal(r.W, p.W) and np.array_equal(r.U, p.U)
+
+
+def test_adjoint_rejects_boundary_none():
+    """The adjoint session validates its inputs before touching a device."""
+    from hydrofv_gb300.problems import random_problem_2d
+    p = random_problem_2d(16, 16, seed=1, bc=("none",) * 4, limiter="minmod", steps=4, smooth=True)
+    with pytest.raises(H.HydroError):
+        H.Adjoint2D(p, steps=4, checkpoint_every=2)
