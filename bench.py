@@ -265,6 +265,97 @@ def run_ensemble(args, H, device, ws, rank) -> None:
     print(json.dumps(line))
 
 
+def run_adjoint(args, H, device, ws, rank) -> None:
+    """Discrete adjoint of the shear layer (MC, periodic, FP64): forward pass
+    with checkpoints, then the reverse pass (segment recomputation + reverse
+    sweep) for dJ/dW0, J = sum_{x > 0.5} rho^2 V at the last step.  Checks
+    on --fd-directions seeded random directions in (rho, p): the dot-product
+    test against the tangent-linear model, central differences (eps 1e-6)
+    of the branch-frozen replay, and of the free replay with its branch flips."""
+    import math
+    from hydrofv_gb300.problems import right_half_density_squared, shear_layer
+    side = args.size if args.size != 2048 else 1024
+    steps = args.steps
+    K = args.checkpoint_every
+    p = shear_layer(side, steps=steps)
+    cells = p.nx * p.ny
+    opts = H.default_options(device=device)
+    interior = np.zeros(p.W.shape[1:], dtype=bool)
+    interior[p.g:-p.g, p.g:-p.g] = True
+
+    def dot(a, b):
+        return math.fsum((a[:, interior] * b[:, interior]).ravel())
+
+    with H.Adjoint2D(p, steps=steps, checkpoint_every=K, options=opts) as ad:
+        for _ in range(max(1, args.warmup // 3)):
+            WN = ad.forward()
+            J, seed = right_half_density_squared(p, WN)
+            ad.backward(seed)
+        barrier(ws)
+        WN = ad.forward()
+        st_f = ad.stats()
+        J, seed = right_half_density_squared(p, WN)
+        l0 = st_f["kernel_launches"]
+        clk = ClockSampler(device)
+        with clk:
+            t0 = time.perf_counter()
+            grad = ad.backward(seed)
+            wall = time.perf_counter() - t0
+        st = ad.stats()
+        launches = st["kernel_launches"] - l0
+        back_ms = st["recompute_ms"] + st["vjp_ms"]
+        checks = {"dot_product_rel": [], "fd_frozen_rel": [], "fd_free_rel": [], "fd_free_flipped_steps": []}
+        rng = np.random.default_rng(2024)
+        _, base_sig = ad.replay(p.W) if args.fd_directions else (None, None)
+        eps = 1e-6
+        for _ in range(args.fd_directions):
+            d = np.zeros_like(p.W)
+            d[0] = rng.normal(size=d[0].shape) * np.abs(p.W[0])
+            d[3] = rng.normal(size=d[3].shape) * np.abs(p.W[3])
+            d[:, ~interior] = 0.0
+            an = dot(grad, d)
+            _, dwN = ad.tangent(d)
+            checks["dot_product_rel"].append(abs(dot(seed, dwN) - an) / abs(an))
+            jp = right_half_density_squared(p, ad.replay_frozen(p.W + eps * d))[0]
+            jm = right_half_density_squared(p, ad.replay_frozen(p.W - eps * d))[0]
+            checks["fd_frozen_rel"].append(abs((jp - jm) / (2 * eps) - an) / abs(an))
+            Wp, sp = ad.replay(p.W + eps * d)
+            Wm, sm = ad.replay(p.W - eps * d)
+            fd = (right_half_density_squared(p, Wp)[0] - right_half_density_squared(p, Wm)[0]) / (2 * eps)
+            checks["fd_free_rel"].append(abs(fd - an) / abs(an))
+            checks["fd_free_flipped_steps"].append(int(((sp != base_sig) | (sm != base_sig)).sum()))
+        st_all = ad.stats()
+    if rank != 0:
+        return
+    line = {
+        "metric": "discrete adjoint of the 2D MUSCL-HLLC step: cell-steps/s of the reverse pass",
+        "value": ws * cells * steps / (back_ms * 1e-3), "unit": "cell-steps/s", "n_gpus": ws,
+        "steps": steps, "warmup": args.warmup, "ms_per_step": back_ms / steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded shear layer)",
+        "config": {"workload": f"adjoint_shear_layer_{side}x{side}_mc_fp64", "grid": [side, side],
+                   "steps": steps, "checkpoint_every": K, "objective": "sum_{x>0.5} rho^2 V at step N",
+                   "gradient_of": "initial rho and p (all four primitives returned)",
+                   "l2": "state larger than the 129 MB L2" if cells >= 1 << 20 else "fits in L2"},
+        "forward": {"ms": st_f["forward_ms"], "ms_per_step": st_f["forward_ms"] / steps,
+                    "cell_updates_per_s": cells * steps / (st_f["forward_ms"] * 1e-3)},
+        "backward": {"ms": back_ms, "recompute_ms": st["recompute_ms"], "reverse_sweep_ms": st["vjp_ms"],
+                     "cost_vs_forward": back_ms / st_f["forward_ms"],
+                     "reverse_sweep_vs_forward": st["vjp_ms"] / st_f["forward_ms"],
+                     "recompute_mismatches": st["recompute_mismatches"],
+                     "device_bytes": st_all["device_bytes"]},
+        "checks": dict(checks, eps=eps, directions=args.fd_directions,
+                       tangent_ms=st_all["tangent_ms"], replay_ms=st_all["replay_ms"]),
+        "e2e": {"value": ws * cells * steps / wall, "unit": "cell-steps/s",
+                "h2d_bytes_per_step": 4 * p.W[0].size * 8 / steps,
+                "d2h_bytes_per_step": 4 * p.W[0].size * 8 / steps,
+                "note": "hydro_gpu_adjoint_backward with host seed in and host gradient out"},
+        "gpu_launches": int(launches),
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line))
+
+
 def main() -> None:
     global N_SIDE, WORKLOAD
     ap = argparse.ArgumentParser()
@@ -278,11 +369,14 @@ def main() -> None:
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"],
                     help="state precision of the timed path (fp64 is the drop-in)")
     ap.add_argument("--workload", default="shear_layer",
-                    choices=["shear_layer", "point_blast", "ensemble"],
+                    choices=["shear_layer", "point_blast", "ensemble", "adjoint"],
                     help="shear_layer: MC, periodic, CFL 0.8; point_blast: Van Leer, reflective, "
                          "CFL 0.4; ensemble: 256 four-quadrant problems, side log-uniform in "
                          "[128, 1024], minmod, transmissive, one launch per step for all")
     ap.add_argument("--instances", type=int, default=256, help="ensemble size")
+    ap.add_argument("--checkpoint-every", type=int, default=50, help="adjoint checkpoint interval")
+    ap.add_argument("--fd-directions", type=int, default=2,
+                    help="adjoint: random directions checked by dot product and finite differences")
     ap.add_argument("--autotune", action="store_true",
                     help="let the library time work-item shapes before stepping")
     ap.add_argument("--compare", action="store_true",
@@ -309,6 +403,9 @@ def main() -> None:
     from hydrofv_gb300.problems import point_blast, shear_layer
     if args.workload == "ensemble":
         run_ensemble(args, H, local, ws, rank)
+        return
+    if args.workload == "adjoint":
+        run_adjoint(args, H, local, ws, rank)
         return
 
     device = local

@@ -174,6 +174,7 @@ _SIGNATURES = {
                                                _P(C.c_uint64)]),
     "hydro_gpu_adjoint_replay_frozen": (ErrorStatus, [C.c_void_p, C.c_void_p, C.c_void_p]),
     "hydro_gpu_adjoint_dt": (ErrorStatus, [C.c_void_p, _dp]),
+    "hydro_gpu_adjoint_set_tape": (None, [C.c_void_p, C.c_int]),
     "hydro_gpu_adjoint_stats": (None, [C.c_void_p, _P(HydroGpuAdjointStats)]),
     "hydro_gpu_adjoint_destroy": (None, [C.c_void_p]),
     "hydro_ad_hllc_jvp": (C.c_int, [C.c_double, C.c_double] + [_dp] * 6),
@@ -655,6 +656,10 @@ class Adjoint2D:
         wN = self._empty()
         self._check(self.lib.hydro_gpu_adjoint_replay_frozen(self.handle, _ptr4(w0), _ptr4(wN)))
         return wN
+
+    def set_tape(self, enabled: bool):
+        """Tape the segment recomputation (default) or recompute in the sweep."""
+        self.lib.hydro_gpu_adjoint_set_tape(self.handle, 1 if enabled else 0)
 
     def dt(self) -> np.ndarray:
         out = np.zeros(self.steps)

@@ -499,6 +499,62 @@ __global__ void __launch_bounds__(kThreads) ad_flux_vjp_kernel(const AdGeom q, c
     }
 }
 
+/* The same from the tape the recomputation wrote (face states and the HLLC
+ * guess with its factors), so neither the reconstruction nor the guesses
+ * are evaluated again. */
+__global__ void __launch_bounds__(kThreads) ad_flux_vjp_tape_kernel(const AdGeom q, const GasConst<double> gas,
+                                                                    const double *tape, long long plane,
+                                                                    FacesP<double> fb, F4<double> Ub,
+                                                                    double cx, double cy, int *err)
+{
+    const int g = q.g;
+    GRID_STRIDE(k, (long long) q.tx * q.ty) {
+        const int r = (int) (k / q.tx), c = (int) (k % q.tx);
+#pragma unroll
+        for (int dir = 0; dir < 2; dir++) {
+            const bool on = dir == 0 ? (r >= g && r < g + q.ny && c >= g - 1 && c <= g + q.nx - 1)
+                                     : (c >= g && c < g + q.nx && r >= g - 1 && r <= g + q.ny - 1);
+            if (!on) continue;
+            const double *T = tape + (long long) (dir * MH2D_TAPE_FIELDS) * plane + k;
+            const long long kn = dir == 0 ? k + 1 : k + q.tx;
+            double L[4], Rs[4], Fb[4], Lb[4], Rb[4];
+#pragma unroll
+            for (int e = 0; e < 4; e++) {
+                L[e] = T[(TAPE_L + e) * plane];
+                Rs[e] = T[(TAPE_R + e) * plane];
+            }
+            if (dir == 0) {
+#pragma unroll
+                for (int e = 0; e < 4; e++) Fb[e] = cx * (Ub.p[e][kn] - Ub.p[e][k]);
+            } else {
+                /* y flux components are (mass, mom_y, mom_x, energy) */
+                Fb[0] = cy * (Ub.p[0][kn] - Ub.p[0][k]);
+                Fb[1] = cy * (Ub.p[2][kn] - Ub.p[2][k]);
+                Fb[2] = cy * (Ub.p[1][kn] - Ub.p[1][k]);
+                Fb[3] = cy * (Ub.p[3][kn] - Ub.p[3][k]);
+            }
+            HllcFwd st;
+            const int rc = hllc_fwd_from_guess(gas, L[0], L[1], L[3], Rs[0], Rs[1], Rs[3], T[TAPE_AL * plane],
+                                               T[TAPE_AR * plane], T[TAPE_PG * plane], (int) T[TAPE_REG * plane],
+                                               st);
+            if (rc) {
+                record(err, rc);
+#pragma unroll
+                for (int e = 0; e < 4; e++) { Lb[e] = 0.0; Rb[e] = 0.0; }
+            } else {
+                hllc_vjp_core(gas, L, Rs, st, true, T[TAPE_Z0 * plane], T[TAPE_Z1 * plane], Fb, Lb, Rb);
+            }
+            if (dir == 0) {
+#pragma unroll
+                for (int e = 0; e < 4; e++) { fb.xhi[e][k] = Lb[e]; fb.xlo[e][kn] = Rb[e]; }
+            } else {
+#pragma unroll
+                for (int e = 0; e < 4; e++) { fb.yhi[e][k] = Lb[e]; fb.ylo[e][kn] = Rb[e]; }
+            }
+        }
+    }
+}
+
 /* Shares of the reverse reconstruction (storage order rho, vx, vy, p). */
 struct SharesP {
     double *own[4];
@@ -664,6 +720,10 @@ struct HydroAdj2D {
     FacesP<Dual> tfaces{};
     FluxP<Dual> tflux{};
     bool forward_done = false;
+    /* tape of a segment (K steps x 2 x MH2D_TAPE_FIELDS fields), written by the
+     * recomputation and read by the reverse sweep */
+    bool use_tape = true;
+    double *tape_d = nullptr;
     /* statistics */
     double forward_ms = 0, recompute_ms = 0, vjp_ms = 0, tangent_ms = 0, replay_ms = 0;
     long long launches = 0;
@@ -753,13 +813,19 @@ int copy_state(HydroAdj2D *a, const StateP<double> &src, const StateP<double> &d
 
 /* One production step n from `in` to `out`. */
 int prod_step(HydroAdj2D *a, long long n, const StateP<double> &in, const StateP<double> &out,
-              HydroRunOutcome *oc)
+              double *tape, HydroRunOutcome *oc)
 {
     Mh2dArgs<double> args = a->pargs;
     const int b = (int) (n & 1);
     for (int i = 0; i < 4; i++) { args.U[b][i] = in.U[i]; args.U[b ^ 1][i] = out.U[i]; }
     for (int i = 0; i < 5; i++) { args.W[b][i] = in.W[i]; args.W[b ^ 1][i] = out.W[i]; }
-    CK(mh2d_launch_step<double>(args, a->grid.limiter, a->stream), "step kernel");
+    if (tape) {
+        args.tape = tape;
+        args.tape_plane = (long long) a->ncell;
+        CK(mh2d_launch_step_tape<double>(args, a->grid.limiter, a->stream), "step kernel (tape)");
+    } else {
+        CK(mh2d_launch_step<double>(args, a->grid.limiter, a->stream), "step kernel");
+    }
     a->launches++;
     return 0;
 }
@@ -1008,7 +1074,7 @@ extern "C" int hydro_adj2d_forward(HydroAdj2D *a, double *const W[4], double *co
     const StateP<double> *in = &a->ckpt[0];
     for (long long n = 0; n < a->nsteps; n++) {
         const StateP<double> &o = a->fwd[(n + 1) & 1];
-        if (prod_step(a, n, *in, o, oc)) return -1;
+        if (prod_step(a, n, *in, o, nullptr, oc)) return -1;
         ad_log_dt_kernel<<<1, 1, 0, a->stream>>>(a->ctrl_d, a->dt_log_d, n);
         CK(cudaGetLastError(), "dt log kernel");
         a->launches++;
@@ -1091,6 +1157,15 @@ extern "C" int hydro_adj2d_backward(HydroAdj2D *a, double *const seed[4], double
     a->launches++;
     a->recompute_ms = 0;
     a->vjp_ms = 0;
+    double *tape_base = nullptr;
+    if (a->use_tape) {
+        if (!a->tape_d) {
+            void *p;
+            if (dalloc(a, (size_t) a->K * 2 * MH2D_TAPE_FIELDS * a->ncell * sizeof(double), &p, oc)) return -1;
+            a->tape_d = static_cast<double *>(p);
+        }
+        tape_base = a->tape_d;
+    }
     for (int s = a->n_ckpt - 1; s >= 0; s--) {
         const long long k0 = (long long) s * a->K;
         const long long k1 = (k0 + a->K < a->nsteps) ? k0 + a->K : a->nsteps;
@@ -1101,8 +1176,11 @@ extern "C" int hydro_adj2d_backward(HydroAdj2D *a, double *const seed[4], double
         CK(cudaEventRecord(a->ev[0], a->stream), "cudaEventRecord");
         CK(cudaMemcpyAsync(a->ctrl_d, &a->ckpt_ctrl_d[s], sizeof(HydroStepControl), cudaMemcpyDeviceToDevice,
                            a->stream), "D2D control");
+        auto tape_of = [&](long long k) -> double * {
+            return tape_base ? tape_base + (size_t) (k - k0) * 2 * MH2D_TAPE_FIELDS * a->ncell : nullptr;
+        };
         for (long long n = k0; n < k1; n++) {
-            if (prod_step(a, n, slab(n), slab(n + 1), oc)) return -1;
+            if (prod_step(a, n, slab(n), slab(n + 1), tape_of(n), oc)) return -1;
             ad_check_dt_kernel<<<1, 1, 0, a->stream>>>(a->ctrl_d, a->dt_log_d, n, a->counters_d + 1);
             CK(cudaGetLastError(), "dt check kernel");
             a->launches++;
@@ -1116,10 +1194,18 @@ extern "C" int hydro_adj2d_backward(HydroAdj2D *a, double *const seed[4], double
         for (long long k = k1 - 1; k >= k0; k--) {
             const StateP<double> &st = slab(k);
             const double dt = a->dt_h[(size_t) k];
-            if (launch_recon<double>(a, st, a->faces, dt, nullptr, BranchP{}, oc)) return -1;
-            ad_flux_vjp_kernel<<<nb, kThreads, 0, a->stream>>>(q, gas, a->faces, a->faces_b, f4(a->Ub),
-                                                               dt * a->grid.area_x, dt * a->grid.area_y, a->err_d);
-            CK(cudaGetLastError(), "flux vjp kernel");
+            if (tape_base) {
+                ad_flux_vjp_tape_kernel<<<nb, kThreads, 0, a->stream>>>(q, gas, tape_of(k), (long long) a->ncell,
+                                                                        a->faces_b, f4(a->Ub), dt * a->grid.area_x,
+                                                                        dt * a->grid.area_y, a->err_d);
+                CK(cudaGetLastError(), "flux vjp kernel");
+            } else {
+                if (launch_recon<double>(a, st, a->faces, dt, nullptr, BranchP{}, oc)) return -1;
+                ad_flux_vjp_kernel<<<nb, kThreads, 0, a->stream>>>(q, gas, a->faces, a->faces_b, f4(a->Ub),
+                                                                   dt * a->grid.area_x, dt * a->grid.area_y,
+                                                                   a->err_d);
+                CK(cudaGetLastError(), "flux vjp kernel");
+            }
             const double dtA_x = dt * a->grid.area_x / vol, dtA_y = dt * a->grid.area_y / vol;
             switch (a->grid.limiter) {
             case LIM_MINMOD:
@@ -1270,6 +1356,11 @@ extern "C" int hydro_adj2d_replay(HydroAdj2D *a, double *const w0[4], double *co
                            a->stream), "D2H signatures");
     CK(cudaStreamSynchronize(a->stream), "adjoint replay");
     return 0;
+}
+
+extern "C" void hydro_adj2d_set_tape(HydroAdj2D *a, int enabled)
+{
+    a->use_tape = enabled != 0;
 }
 
 extern "C" int hydro_adj2d_dt(const HydroAdj2D *a, double *dt)

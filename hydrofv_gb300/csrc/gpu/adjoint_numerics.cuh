@@ -209,54 +209,92 @@ HD void vacuum_fan_vjp(const GasConst<double> &c, bool right, double rho, double
     ab += -kb * k / a;
 }
 
-/*
- * Reverse of hllc_flux_2d.  L, Rs = (rho, u_normal, u_tangential, p) of the
- * left / right face states, Fb = adjoint of the flux (mass, normal momentum,
- * tangential momentum, energy).  Writes Lb, Rb.  Returns DEV_OK or
- * DEV_ERR_HLLC_WAVE_SPEED.
- */
-HD int hllc_vjp(const GasConst<double> &c, const double L[4], const double Rs[4], const double Fb[4],
-                double Lb[4], double Rb[4], int *code)
+/* The remaining intermediates of a face from its sound speeds, unfloored
+ * guess and regime (what the tape keeps): the same expressions as
+ * hllc_classify / hllc_finish. */
+HD int hllc_fwd_from_guess(const GasConst<double> &c, double rl, double ul, double pl, double rr, double ur,
+                           double pr, double aL, double aR, double pg, int reg, HllcFwd &s)
+{
+    s.aL = aL;
+    s.aR = aR;
+    s.reg = reg;
+    s.region = -1;
+    s.ppv = 0.5 * (pl + pr) - 0.125 * (ur - ul) * (rl + rr) * (aL + aR);
+    s.pg = pg;
+    s.ps = s.qL = s.qR = s.SL = s.SR = s.Ss = 0.0;
+    if (reg == PREG_VACUUM) return DEV_OK;
+    s.ps = (s.pg < c.tol) ? c.tol : s.pg;
+    s.qL = hllc_q(c, pl, s.ps);
+    s.qR = hllc_q(c, pr, s.ps);
+    s.SL = ul - s.aL * s.qL;
+    s.SR = ur + s.aR * s.qR;
+    s.Ss = (pr - pl + rl * ul * (s.SL - ul) - rr * ur * (s.SR - ur))
+         / (rl * (s.SL - ul) - rr * (s.SR - ur));
+    if (0.0 <= s.SL) s.region = 0;
+    else if (s.SL <= 0.0 && 0.0 <= s.Ss) s.region = 1;
+    else if (s.Ss <= 0.0 && 0.0 <= s.SR) s.region = 2;
+    else if (s.SR <= 0.0) s.region = 3;
+    else return DEV_ERR_HLLC_WAVE_SPEED;
+    return DEV_OK;
+}
+
+/* Reverse of the vacuum / vacuum-generation flux (kept out of line: rare,
+ * and its pow-heavy samplers would otherwise raise the register count of
+ * every face). */
+#ifdef __CUDACC__
+static __host__ __device__ __noinline__
+#else
+static
+#endif
+void hllc_vacuum_vjp(const GasConst<double> &c, const double L[4], const double Rs[4], double aL, double aR,
+                     const double Fb[4], double Lb[4], double Rb[4])
 {
     const double rl = L[0], ul = L[1], vl = L[2], pl = L[3];
     const double rr = Rs[0], ur = Rs[1], vr = Rs[2], pr = Rs[3];
-    HllcFwd s;
-    const int rc = hllc_fwd(c, rl, ul, pl, rr, ur, pr, s);
-    if (code) *code = hllc_code(c, s, rl, ul, pl, rr, ur, pr);
+    double rLb = 0, uLb = 0, vLb = 0, pLb = 0, rRb = 0, uRb = 0, vRb = 0, pRb = 0, aLb = 0, aRb = 0;
+    int sub;
+    const int which = vacuum_case(c, rl, ul, aL, rr, ur, aR, sub);
+    double o[4];
+    solve_vacuum(c, rl, ul, vl, pl, aL, rr, ur, vr, pr, aR, 0.0, o);
+    const double E = o[0] * (0.5 * (o[1] * o[1] + o[2] * o[2]) + o[3] / (o[0] * c.gm1));
+    const double Eb = Fb[3] * o[1];
+    double ob[4];
+    ob[0] = Fb[0] * o[1] + Fb[1] * o[1] * o[1] + Fb[2] * o[1] * o[2] + Eb * 0.5 * (o[1] * o[1] + o[2] * o[2]);
+    ob[1] = Fb[0] * o[0] + Fb[1] * 2.0 * o[0] * o[1] + Fb[2] * o[0] * o[2] + Fb[3] * (E + o[3])
+          + Eb * o[0] * o[1];
+    ob[2] = Fb[2] * o[0] * o[1] + Eb * o[0] * o[2];
+    ob[3] = Fb[1] + Fb[3] * o[1] + Eb / c.gm1;
+    if (which == 1) {
+        if (sub == 0) { rLb += ob[0]; uLb += ob[1]; vLb += ob[2]; pLb += ob[3]; }
+        else if (sub == 1) vacuum_fan_vjp(c, true, rl, ul, pl, aL, ob, rLb, uLb, vLb, pLb, aLb);
+    } else if (which == 2) {
+        if (sub == 0) { rRb += ob[0]; uRb += ob[1]; vRb += ob[2]; pRb += ob[3]; }
+        else if (sub == 1) vacuum_fan_vjp(c, false, rr, ur, pr, aR, ob, rRb, uRb, vRb, pRb, aRb);
+    }
+    if (rl > 0.0) sound_speed_vjp(rl, pl, aL, aLb, rLb, pLb);
+    if (rr > 0.0) sound_speed_vjp(rr, pr, aR, aRb, rRb, pRb);
+    Lb[0] = rLb; Lb[1] = uLb; Lb[2] = vLb; Lb[3] = pLb;
+    Rb[0] = rRb; Rb[1] = uRb; Rb[2] = vRb; Rb[3] = pRb;
+}
+
+/*
+ * Reverse of hllc_flux_2d given the face's forward intermediates s.  L, Rs
+ * = (rho, u_normal, u_tangential, p) of the left / right face states, Fb =
+ * adjoint of the flux (mass, normal momentum, tangential momentum, energy).
+ * With have_z the guess factors (z0, z1) are taken as given (from the tape)
+ * instead of recomputed.  Writes Lb, Rb.
+ */
+HD void hllc_vjp_core(const GasConst<double> &c, const double L[4], const double Rs[4], const HllcFwd &s,
+                      bool have_z, double z0, double z1, const double Fb[4], double Lb[4], double Rb[4])
+{
+    if (s.reg == PREG_VACUUM) {
+        hllc_vacuum_vjp(c, L, Rs, s.aL, s.aR, Fb, Lb, Rb);
+        return;
+    }
+    const double rl = L[0], ul = L[1], vl = L[2], pl = L[3];
+    const double rr = Rs[0], ur = Rs[1], vr = Rs[2], pr = Rs[3];
     double rLb = 0, uLb = 0, vLb = 0, pLb = 0, rRb = 0, uRb = 0, vRb = 0, pRb = 0;
     double aLb = 0, aRb = 0;
-    if (rc != DEV_OK) {
-        for (int q = 0; q < 4; q++) { Lb[q] = 0.0; Rb[q] = 0.0; }
-        return rc;
-    }
-    if (s.reg == PREG_VACUUM) {
-        int sub;
-        const int which = vacuum_case(c, rl, ul, s.aL, rr, ur, s.aR, sub);
-        double o[4];
-        solve_vacuum(c, rl, ul, vl, pl, s.aL, rr, ur, vr, pr, s.aR, 0.0, o);
-        const double E = o[0] * (0.5 * (o[1] * o[1] + o[2] * o[2]) + o[3] / (o[0] * c.gm1));
-        const double Eb = Fb[3] * o[1];
-        double ob[4];
-        ob[0] = Fb[0] * o[1] + Fb[1] * o[1] * o[1] + Fb[2] * o[1] * o[2]
-              + Eb * 0.5 * (o[1] * o[1] + o[2] * o[2]);
-        ob[1] = Fb[0] * o[0] + Fb[1] * 2.0 * o[0] * o[1] + Fb[2] * o[0] * o[2] + Fb[3] * (E + o[3])
-              + Eb * o[0] * o[1];
-        ob[2] = Fb[2] * o[0] * o[1] + Eb * o[0] * o[2];
-        ob[3] = Fb[1] + Fb[3] * o[1] + Eb / c.gm1;
-        if (which == 1) {
-            if (sub == 0) { rLb += ob[0]; uLb += ob[1]; vLb += ob[2]; pLb += ob[3]; }
-            else if (sub == 1) vacuum_fan_vjp(c, true, rl, ul, pl, s.aL, ob, rLb, uLb, vLb, pLb, aLb);
-        } else if (which == 2) {
-            if (sub == 0) { rRb += ob[0]; uRb += ob[1]; vRb += ob[2]; pRb += ob[3]; }
-            else if (sub == 1) vacuum_fan_vjp(c, false, rr, ur, pr, s.aR, ob, rRb, uRb, vRb, pRb, aRb);
-        }
-        if (rl > 0.0) sound_speed_vjp(rl, pl, s.aL, aLb, rLb, pLb);
-        if (rr > 0.0) sound_speed_vjp(rr, pr, s.aR, aRb, rRb, pRb);
-        Lb[0] = rLb; Lb[1] = uLb; Lb[2] = vLb; Lb[3] = pLb;
-        Rb[0] = rRb; Rb[1] = uRb; Rb[2] = vRb; Rb[3] = pRb;
-        return DEV_OK;
-    }
-
     /* ---- region flux of the selected side K ---- */
     const bool left = s.region <= 1;
     const double rho = left ? rl : rr, u = left ? ul : ur, v = left ? vl : vr, p = left ? pl : pr;
@@ -365,7 +403,8 @@ HD int hllc_vjp(const GasConst<double> &c, const double L[4], const double Rs[4]
     if (s.reg == PREG_PVRS) {
         ppvb += pgb;
     } else if (s.reg == PREG_TRRS) {
-        const double zL = pow(pl, c.half_gm1_g), zR = pow(pr, c.half_gm1_g);
+        const double zL = have_z ? z0 : pow(pl, c.half_gm1_g);
+        const double zR = have_z ? z1 : pow(pr, c.half_gm1_g);
         const double num = s.aL + s.aR - c.half_gm1 * (ur - ul);
         const double den = s.aL / zL + s.aR / zR;
         const double base = num / den;
@@ -384,8 +423,8 @@ HD int hllc_vjp(const GasConst<double> &c, const double L[4], const double Rs[4]
         pRb += zRb * c.half_gm1_g * zR / pr;
     } else {
         const double BL = s.ppv + pl * c.gm1_gp1, BR = s.ppv + pr * c.gm1_gp1;
-        const double gL = sqrt((2.0 / (c.gp1 * rl)) / BL);
-        const double gR = sqrt((2.0 / (c.gp1 * rr)) / BR);
+        const double gL = have_z ? z0 : sqrt((2.0 / (c.gp1 * rl)) / BL);
+        const double gR = have_z ? z1 : sqrt((2.0 / (c.gp1 * rr)) / BR);
         const double Dd = gL + gR;
         const double Nnb = pgb / Dd;
         const double Ddb = -pgb * s.pg / Dd;
@@ -419,6 +458,22 @@ HD int hllc_vjp(const GasConst<double> &c, const double L[4], const double Rs[4]
     sound_speed_vjp(rr, pr, s.aR, aRb, rRb, pRb);
     Lb[0] = rLb; Lb[1] = uLb; Lb[2] = vLb; Lb[3] = pLb;
     Rb[0] = rRb; Rb[1] = uRb; Rb[2] = vRb; Rb[3] = pRb;
+}
+
+/* Reverse of hllc_flux_2d from the face states alone (forward intermediates
+ * recomputed).  Returns DEV_OK or DEV_ERR_HLLC_WAVE_SPEED; *code (may be
+ * NULL) receives the face's branch code. */
+HD int hllc_vjp(const GasConst<double> &c, const double L[4], const double Rs[4], const double Fb[4],
+                double Lb[4], double Rb[4], int *code)
+{
+    HllcFwd s;
+    const int rc = hllc_fwd(c, L[0], L[1], L[3], Rs[0], Rs[1], Rs[3], s);
+    if (code) *code = hllc_code(c, s, L[0], L[1], L[3], Rs[0], Rs[1], Rs[3]);
+    if (rc != DEV_OK) {
+        for (int q = 0; q < 4; q++) { Lb[q] = 0.0; Rb[q] = 0.0; }
+        return rc;
+    }
+    hllc_vjp_core(c, L, Rs, s, false, 0.0, 0.0, Fb, Lb, Rb);
     return DEV_OK;
 }
 

@@ -108,6 +108,7 @@ int hydro_adj2d_tangent(HydroAdj2D *a, double *const w0[4], double *const dw0[4]
 int hydro_adj2d_replay(HydroAdj2D *a, double *const w0[4], double *const wN[4],
                        unsigned long long *signatures, int frozen, HydroRunOutcome *oc);
 int hydro_adj2d_dt(const HydroAdj2D *a, double *dt);
+void hydro_adj2d_set_tape(HydroAdj2D *a, int enabled);
 void hydro_adj2d_stats(const HydroAdj2D *a, HydroGpuAdjointStats *st);
 void hydro_adj2d_destroy(HydroAdj2D *a);
 

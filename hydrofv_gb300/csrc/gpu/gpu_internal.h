@@ -16,6 +16,8 @@ namespace hydro {
 template <class R>
 cudaError_t mh2d_launch_step(const Mh2dArgs<R> &a, int limiter, cudaStream_t s);
 template <class R>
+cudaError_t mh2d_launch_step_tape(const Mh2dArgs<R> &a, int limiter, cudaStream_t s);
+template <class R>
 int mh2d_resident_ctas(int limiter, int first_order, int device);
 template <class R>
 cudaError_t mh2d_launch_batch_step(const Mh2dBatchArgs<R> &b, int limiter, int first_order, int grid,

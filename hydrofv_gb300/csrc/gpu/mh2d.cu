@@ -11,6 +11,7 @@ namespace hydro {
 template int mh2d_resident_ctas<double>(int, int, int);
 template cudaError_t mh2d_launch_batch_step<double>(const Mh2dBatchArgs<double> &, int, int, int, cudaStream_t);
 template cudaError_t mh2d_launch_step<double>(const Mh2dArgs<double> &, int, cudaStream_t);
+template cudaError_t mh2d_launch_step_tape<double>(const Mh2dArgs<double> &, int, cudaStream_t);
 template cudaError_t mh2d_launch_prepare<double>(const Mh2dArgs<double> &, cudaStream_t);
 template cudaError_t mh2d_launch_materialize<double>(const Mh2dArgs<double> &, int,
                                                      double *const[4], cudaStream_t);

@@ -64,6 +64,40 @@ struct Mh2dArgs {
     double area_x, area_y, vol;
     int first_order;         /* 1: Godunov first order (face states = cell states) */
     int grid_ctas;           /* persistent CTAs per step launch (0: one per work item) */
+    R *tape;                 /* adjoint tape of this step (kernels built with TAPE only) */
+    long long tape_plane;    /* elements per tape field (padded cells) */
+};
+
+/*
+ * Adjoint tape of one step (written by the TAPE build of the step kernel,
+ * read by the reverse sweep).  Per face, at the padded index of its left
+ * (x faces) or lower (y faces) cell, MH2D_TAPE_FIELDS fields per direction
+ * (x fields first, then y): the face states (4 + 4, normal velocity in
+ * slot 1), both sound speeds, the star-pressure guess before the floor, the
+ * guess's factors (p^((g-1)/2g) of each side for the two-rarefaction guess,
+ * g_K of each side for the two-shock guess) and the regime.
+ */
+#define MH2D_TAPE_FIELDS 14
+enum : int {
+    TAPE_L = 0, TAPE_R = 4, TAPE_AL = 8, TAPE_AR = 9, TAPE_PG = 10, TAPE_Z0 = 11, TAPE_Z1 = 12,
+    TAPE_REG = 13,
+};
+
+/* Where solve_faces writes the tape of a batch: faces [0, nxf) are x faces
+ * of row row_x with left cells c0-1+f; the rest are y faces between row_y
+ * and row_y+1 in columns c0+(f-nxf). */
+template <class R>
+struct TapeCtx {
+    R *tape;
+    long long plane;
+    int pitch, nxf, row_x, row_y, c0;
+    __device__ __forceinline__ R *field(int f, int q) const
+    {
+        const bool x = f < nxf;
+        const long long idx = x ? (long long) row_x * pitch + c0 - 1 + f
+                                : (long long) row_y * pitch + c0 + (f - nxf);
+        return tape + ((x ? 0 : MH2D_TAPE_FIELDS) + q) * plane + idx;
+    }
 };
 
 /* Load W at padded (r, c), remapping ghost cells to their source. */
@@ -142,8 +176,9 @@ struct Mh2dShared {
  * regimes, which the one-face-per-thread form serialises.  The flux
  * replaces the left state in sm.FL.  Ends with a barrier.
  */
-template <class R, int NT>
-__device__ __forceinline__ int solve_faces(Mh2dShared<R, NT> &sm, const GasConst<R> &gas, int nF)
+template <class R, int NT, bool TAPE = false>
+__device__ __forceinline__ int solve_faces(Mh2dShared<R, NT> &sm, const GasConst<R> &gas, int nF,
+                                           const TapeCtx<R> &tc = TapeCtx<R>{})
 {
     const int tid = threadIdx.x;
     int err = DEV_OK;
@@ -161,7 +196,21 @@ __device__ __forceinline__ int solve_faces(Mh2dShared<R, NT> &sm, const GasConst
     __syncthreads();
     const int nT = sm.nT, nS = sm.nS;
     for (int i = tid; i < nT + nS; i += NT) {
-        if (i < nT) {
+        if constexpr (TAPE) {
+            R z0, z1;
+            int f;
+            if (i < nT) {
+                f = sm.listT[i];
+                sm.pg[f] = guess_p_trrs_z(gas, sm.FL[1][f], sm.FL[3][f], sm.aL[f],
+                                          sm.FR[1][f], sm.FR[3][f], sm.aR[f], z0, z1);
+            } else {
+                f = sm.listS[i - nT];
+                sm.pg[f] = guess_p_tsrs_g(gas, sm.FL[0][f], sm.FL[1][f], sm.FL[3][f],
+                                          sm.FR[0][f], sm.FR[1][f], sm.FR[3][f], sm.pg[f], z0, z1);
+            }
+            *tc.field(f, TAPE_Z0) = z0;
+            *tc.field(f, TAPE_Z1) = z1;
+        } else if (i < nT) {
             const int f = sm.listT[i];
             sm.pg[f] = guess_p_trrs(gas, sm.FL[1][f], sm.FL[3][f], sm.aL[f],
                                     sm.FR[1][f], sm.FR[3][f], sm.aR[f]);
@@ -176,6 +225,12 @@ __device__ __forceinline__ int solve_faces(Mh2dShared<R, NT> &sm, const GasConst
         R F[4];
         const R rl = sm.FL[0][f], ul = sm.FL[1][f], vl = sm.FL[2][f], pl = sm.FL[3][f];
         const R rr = sm.FR[0][f], ur = sm.FR[1][f], vr = sm.FR[2][f], pr = sm.FR[3][f];
+        if constexpr (TAPE) {
+            const R v[11] = { rl, ul, vl, pl, rr, ur, vr, pr, sm.aL[f], sm.aR[f], sm.pg[f] };
+#pragma unroll
+            for (int q = 0; q < 11; q++) *tc.field(f, q) = v[q];
+            *tc.field(f, TAPE_REG) = (R) sm.reg[f];
+        }
         if (sm.reg[f] == PREG_VACUUM) {
             hllc_vacuum_flux(gas, rl, ul, vl, pl, sm.aL[f], rr, ur, vr, pr, sm.aR[f], F);
         } else {
@@ -195,7 +250,7 @@ __device__ __forceinline__ int solve_faces(Mh2dShared<R, NT> &sm, const GasConst
  * rows) of step n with time step dt.  Shared by the single-grid and the
  * batched kernels; the caller reduces mx_x / mx_y and handles errors.
  */
-template <class R, int LIM, int NT, int FIRST_ORDER>
+template <class R, int LIM, int NT, int FIRST_ORDER, bool TAPE = false>
 __device__ __forceinline__ void mh2d_item(const Mh2dArgs<R> &a, Mh2dShared<R, NT> &sm, int item,
                                           long long n, double dt, double &mx_x, double &mx_y,
                                           int &err)
@@ -304,7 +359,13 @@ __device__ __forceinline__ void mh2d_item(const Mh2dArgs<R> &a, Mh2dShared<R, NT
     }
     __syncthreads();
     {
-        const int rc = solve_faces<R, NT>(sm, a.gas, sw);
+        int rc;
+        if constexpr (TAPE) {
+            const TapeCtx<R> tc{ a.tape, a.tape_plane, a.pitch, 0, -1, r_begin - 1, c0 };
+            rc = solve_faces<R, NT, true>(sm, a.gas, sw, tc);
+        } else {
+            rc = solve_faces<R, NT>(sm, a.gas, sw);
+        }
         if (rc) err = rc;
     }
     if (inner) {
@@ -341,7 +402,13 @@ __device__ __forceinline__ void mh2d_item(const Mh2dArgs<R> &a, Mh2dShared<R, NT
         }
         __syncthreads();
         {
-            const int rc = solve_faces<R, NT>(sm, a.gas, nX + sw);
+            int rc;
+            if constexpr (TAPE) {
+                const TapeCtx<R> tc{ a.tape, a.tape_plane, a.pitch, nX, r, r, c0 };
+                rc = solve_faces<R, NT, true>(sm, a.gas, nX + sw, tc);
+            } else {
+                rc = solve_faces<R, NT>(sm, a.gas, nX + sw);
+            }
             if (rc) err = rc;
         }
 
@@ -410,7 +477,7 @@ __device__ __forceinline__ void mh2d_item(const Mh2dArgs<R> &a, Mh2dShared<R, NT
  * SMs that finish early take more work (the FP64 pipe of an SM is shared by
  * its CTAs).
  */
-template <class R, int LIM, int NT, int FIRST_ORDER>
+template <class R, int LIM, int NT, int FIRST_ORDER, bool TAPE = false>
 __global__ void __launch_bounds__(NT, 4) mh2d_step_kernel(const Mh2dArgs<R> a)
 {
     static_assert(NT % 32 == 0, "NT must be a whole number of warps");
@@ -447,7 +514,7 @@ __global__ void __launch_bounds__(NT, 4) mh2d_step_kernel(const Mh2dArgs<R> a)
         const int item = sm.item;
         __syncthreads();
         if (item >= n_items) break;
-        mh2d_item<R, LIM, NT, FIRST_ORDER>(a, sm, item, n, dt, mx_x, mx_y, err);
+        mh2d_item<R, LIM, NT, FIRST_ORDER, TAPE>(a, sm, item, n, dt, mx_x, mx_y, err);
     }
 
     if (err) record_error(ctrl, err, (int) blockIdx.x);

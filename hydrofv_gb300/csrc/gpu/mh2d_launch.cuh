@@ -107,6 +107,20 @@ cudaError_t mh2d_launch_step(const Mh2dArgs<R> &a, int limiter, cudaStream_t s)
     }
 }
 
+/* The step kernel that also writes the adjoint tape (a.tape, FP64 MUSCL-Hancock). */
+template <class R>
+cudaError_t mh2d_launch_step_tape(const Mh2dArgs<R> &a, int limiter, cudaStream_t s)
+{
+    const int n_items = ((a.nx + a.strip_w - 1) / a.strip_w) * ((a.ny + a.chunk_h - 1) / a.chunk_h);
+    const int grid = (a.grid_ctas > 0 && a.grid_ctas < n_items) ? a.grid_ctas : n_items;
+    switch (limiter) {
+    case LIM_MINMOD: mh2d_step_kernel<R, LIM_MINMOD, MH2D_THREADS, 0, true><<<grid, MH2D_THREADS, 0, s>>>(a); break;
+    case LIM_VAN_LEER: mh2d_step_kernel<R, LIM_VAN_LEER, MH2D_THREADS, 0, true><<<grid, MH2D_THREADS, 0, s>>>(a); break;
+    default: mh2d_step_kernel<R, LIM_MC, MH2D_THREADS, 0, true><<<grid, MH2D_THREADS, 0, s>>>(a); break;
+    }
+    return cudaGetLastError();
+}
+
 template <class R>
 cudaError_t mh2d_launch_prepare(const Mh2dArgs<R> &a, cudaStream_t s)
 {

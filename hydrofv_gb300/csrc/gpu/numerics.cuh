@@ -268,12 +268,33 @@ HD int hllc_classify(const GasConst<R> &c, R rho_L, R u_L, R p_L, R rho_R, R u_R
     return PREG_TSRS;
 }
 
+/* The *_z / *_g forms also hand back the guesses' intermediate factors
+ * (p^((g-1)/2g) of each side for the two-rarefaction guess, g_K of each
+ * side for the two-shock guess), which the adjoint's tape keeps; they
+ * evaluate the same expressions as the plain forms below. */
+template <class R>
+HD R guess_p_trrs_z(const GasConst<R> &c, R u_L, R p_L, R a_L, R u_R, R p_R, R a_R, R &zL, R &zR)
+{
+    zL = pow(p_L, c.half_gm1_g);
+    zR = pow(p_R, c.half_gm1_g);
+    const R pg = (a_L + a_R - c.half_gm1 * (u_R - u_L)) / (a_L / zL + a_R / zR);
+    return pow(pg, c.g_half_gm1);
+}
+
 template <class R>
 HD R guess_p_trrs(const GasConst<R> &c, R u_L, R p_L, R a_L, R u_R, R p_R, R a_R)
 {
     const R pg = (a_L + a_R - c.half_gm1 * (u_R - u_L))
                / (a_L / pow(p_L, c.half_gm1_g) + a_R / pow(p_R, c.half_gm1_g));
     return pow(pg, c.g_half_gm1);
+}
+
+template <class R>
+HD R guess_p_tsrs_g(const GasConst<R> &c, R rho_L, R u_L, R p_L, R rho_R, R u_R, R p_R, R ppv, R &gL, R &gR)
+{
+    gL = sqrt((R(2) / (c.gp1 * rho_L)) / (ppv + p_L * c.gm1_gp1));
+    gR = sqrt((R(2) / (c.gp1 * rho_R)) / (ppv + p_R * c.gm1_gp1));
+    return (gL * p_L + gR * p_R - (u_R - u_L)) / (gL + gR);
 }
 
 template <class R>

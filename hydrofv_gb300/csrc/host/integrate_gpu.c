@@ -853,6 +853,11 @@ ErrorStatus hydro_gpu_adjoint_dt(const HydroGpuAdjoint *ad, double *dt)
     return make_success_error_status();
 }
 
+void hydro_gpu_adjoint_set_tape(HydroGpuAdjoint *ad, int enabled)
+{
+    hydro_adj2d_set_tape(ad->adj, enabled);
+}
+
 void hydro_gpu_adjoint_stats(const HydroGpuAdjoint *ad, HydroGpuAdjointStats *stats)
 {
     hydro_adj2d_stats(ad->adj, stats);

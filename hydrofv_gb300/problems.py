@@ -307,3 +307,19 @@ def four_quadrant_ensemble(count: int = 256, seed: int = 4, steps: int = 500,
     lo, hi = math.log(side_range[0]), math.log(side_range[1])
     sides = np.rint(np.exp(rng.uniform(lo, hi, size=count))).astype(int)
     return [four_quadrant(int(s), rng, steps=steps, limiter=limiter) for s in sides]
+
+
+def right_half_density_squared(p: Problem2D, W: np.ndarray) -> tuple[float, np.ndarray]:
+    """Objective of the adjoint workload: J = sum over the interior cells whose
+    centre has x > (x_min + x_max)/2 of rho^2 * V (V the cell volume the
+    problem's conserved state uses), and dJ/dW (zero elsewhere)."""
+    x = mid_points(p.x_min, p.x_max, p.nx, p.g)
+    mask = np.zeros(W.shape[1:], dtype=bool)
+    mask[p.g:p.g + p.ny, p.g:p.g + p.nx] = True
+    mask &= (x[None, :] > 0.5 * (p.x_min + p.x_max))
+    vol = ((p.x_max - p.x_min) / (p.nx + 2 * p.g)) * ((p.y_max - p.y_min) / (p.ny + 2 * p.g))
+    rho = W[0]
+    J = math.fsum((rho[mask] ** 2).ravel()) * vol
+    seed = np.zeros_like(W)
+    seed[0][mask] = 2.0 * rho[mask] * vol
+    return J, seed

@@ -292,6 +292,14 @@ ErrorStatus hydro_gpu_adjoint_replay(HydroGpuAdjoint *adjoint, double *const w0[
 ErrorStatus hydro_gpu_adjoint_replay_frozen(HydroGpuAdjoint *adjoint, double *const w0[4],
                                             double *const w_final[4]);
 
+/* Tape (default on): the segment recomputation writes, per face and step,
+ * the face states and the HLLC guess with its factors (2 x 14 fields per
+ * cell per step, K steps: about 224 bytes per cell per checkpointed step),
+ * and the reverse sweep reads them instead of re-evaluating the
+ * reconstruction and the guesses.  Off: nothing is stored and the reverse
+ * sweep recomputes them; the gradient is the same bit for bit. */
+void hydro_gpu_adjoint_set_tape(HydroGpuAdjoint *adjoint, int enabled);
+
 /* dt of each forward step (num_steps entries). */
 ErrorStatus hydro_gpu_adjoint_dt(const HydroGpuAdjoint *adjoint, double *dt);
 
