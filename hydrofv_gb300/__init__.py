@@ -328,15 +328,27 @@ def _params(lib, bc, integrator, riemann_solver, slope_limiter, cfl, keep):
     return bcp, ip
 
 
+def _set_custom(bcp, custom_bc, keep):
+    """Install BcCallback objects for the custom sides (kept alive in keep)."""
+    names = ("x_min", "x_max", "y_min", "y_max")
+    for side, cb in zip(names, custom_bc or (None,) * 4):
+        if cb is not None:
+            keep.append(cb)
+            setattr(bcp, "set_boundary_condition_cartesian_2d_" + side, C.cast(cb, C.c_void_p).value)
+
+
 def run_2d(nx: int, ny: int, g: int, bounds, gamma: float, W: np.ndarray, U: np.ndarray,
            bc=("periodic",) * 4, integrator="muscl_hancock_2d",
            riemann_solver="riemann_solver_hllc", slope_limiter="monotonized_central",
            cfl=0.8, tf=1.0, max_steps=-1, options: HydroGpuOptions | None = None,
-           storing: dict | None = None) -> RunResult:
+           storing: dict | None = None, gravity: float = 0.0, custom_bc=None) -> RunResult:
     """Run a 2D problem through hydro_gpu_launch_simulation.  W and U are
-    (4, ny+2g, nx+2g) float64 arrays (rho,u,v,p / mass,mom_x,mom_y,energy)."""
+    (4, ny+2g, nx+2g) float64 arrays (rho,u,v,p / mass,mom_x,mom_y,energy).
+    gravity sets System.gravity; custom_bc gives a problems.BcCallback per
+    side whose boundary name is "custom"."""
     lib = library()
     h = _SystemHandle(lib, "cartesian_2d", nx, ny, g, bounds, gamma)
+    h.s.gravity = gravity
     try:
         for dst, src in zip(h.fields(W2), W):
             dst[:] = np.ascontiguousarray(src, dtype=np.float64).reshape(-1)
@@ -344,6 +356,7 @@ def run_2d(nx: int, ny: int, g: int, bounds, gamma: float, W: np.ndarray, U: np.
             dst[:] = np.ascontiguousarray(src, dtype=np.float64).reshape(-1)
         keep: list = []
         bcp, ip = _params(lib, bc, integrator, riemann_solver, slope_limiter, cfl, keep)
+        _set_custom(bcp, custom_bc, keep)
         sp = lib.get_new_storing_param()
         if storing:
             sp.is_storing = True
@@ -408,9 +421,10 @@ class Solver2D:
 
     def __init__(self, nx, ny, g, bounds, gamma, W, U, bc=("periodic",) * 4,
                  slope_limiter="monotonized_central", cfl=0.8,
-                 options: HydroGpuOptions | None = None):
+                 options: HydroGpuOptions | None = None, gravity: float = 0.0, custom_bc=None):
         self.lib = lib = library()
         self._h = _SystemHandle(lib, "cartesian_2d", nx, ny, g, bounds, gamma)
+        self._h.s.gravity = gravity
         for dst, src in zip(self._h.fields(W2), W):
             dst[:] = np.ascontiguousarray(src).reshape(-1)
         for dst, src in zip(self._h.fields(U2), U):
@@ -418,6 +432,7 @@ class Solver2D:
         self._keep: list = []
         bcp, ip = _params(lib, bc, "muscl_hancock_2d", "riemann_solver_hllc", slope_limiter,
                           cfl, self._keep)
+        _set_custom(bcp, custom_bc, self._keep)
         self._bcp, self._ip = bcp, ip
         opt = options if options is not None else lib.hydro_gpu_default_options()
         self.handle = C.c_void_p()

@@ -42,7 +42,13 @@ typedef struct HydroGrid2D
     int bc[4];                    /* BOUNDARY_CONDITION_* of x_min, x_max, y_min, y_max */
     int limiter;                  /* SLOPE_LIMITER_* */
     int integrator;               /* INTEGRATOR_MUSCL_HANCOCK_2D or INTEGRATOR_GODUNOV_FIRST_ORDER_2D */
+    double gravity;               /* System.gravity (0: no source term) */
 } HydroGrid2D;
+
+/* Host boundary routine for custom sides: receives the padded W arrays
+ * (host memory) holding U->W of every cell after a step, applies the
+ * boundary conditions in place; returns 0 on success. */
+typedef int (*HydroHostBcFn)(void *ctx, double *const W[4]);
 
 /* Called when a snapshot is due; W holds the padded primitive arrays
  * (host memory, valid for the duration of the call).  Returns 0 on success. */
@@ -57,6 +63,10 @@ int hydro_run2d_create(const HydroGrid2D *grid, const HydroGpuOptions *opt,
 int hydro_run2d_upload(HydroRun2D *run, double *const W[4], double *const U[4],
                        int keep_initial, HydroRunOutcome *oc);
 int hydro_run2d_restore(HydroRun2D *run, HydroRunOutcome *oc);
+/* Custom (callback) sides: after every step the state is converted and
+ * handed to `fn`; the ghost bands of the sides whose BC is custom are then
+ * copied back (FP64 only). */
+int hydro_run2d_set_host_bc(HydroRun2D *run, HydroHostBcFn fn, void *ctx, HydroRunOutcome *oc);
 /* Start a run at t = 0 from the uploaded state. */
 int hydro_run2d_begin(HydroRun2D *run, const HydroStepParams *sp, double tf, int64 max_steps,
                       int store_count, HydroRunOutcome *oc);

@@ -28,6 +28,10 @@ template <class R>
 cudaError_t mh2d_launch_materialize(const Mh2dArgs<R> &a, int buf, R *const out[4], cudaStream_t s);
 template <class R>
 cudaError_t mh2d_launch_totals(const Mh2dArgs<R> &a, int buf, double *out4, cudaStream_t s);
+template <class R>
+cudaError_t mh2d_launch_convert_all(const Mh2dArgs<R> &a, int buf, R *const out[4], cudaStream_t s);
+template <class R>
+cudaError_t mh2d_launch_ghost_sound_speed(const Mh2dArgs<R> &a, int buf, int mask, cudaStream_t s);
 cudaError_t convert_f64_to_f32(const double *src, float *dst, long long n, cudaStream_t s);
 cudaError_t convert_f32_to_f64(const float *src, double *dst, long long n, cudaStream_t s);
 

@@ -16,5 +16,7 @@ template cudaError_t mh2d_launch_prepare<double>(const Mh2dArgs<double> &, cudaS
 template cudaError_t mh2d_launch_materialize<double>(const Mh2dArgs<double> &, int,
                                                      double *const[4], cudaStream_t);
 template cudaError_t mh2d_launch_totals<double>(const Mh2dArgs<double> &, int, double *, cudaStream_t);
+template cudaError_t mh2d_launch_convert_all<double>(const Mh2dArgs<double> &, int, double *const[4], cudaStream_t);
+template cudaError_t mh2d_launch_ghost_sound_speed<double>(const Mh2dArgs<double> &, int, int, cudaStream_t);
 
 }  // namespace hydro

@@ -64,6 +64,7 @@ struct Mh2dArgs {
     double area_x, area_y, vol;
     int first_order;         /* 1: Godunov first order (face states = cell states) */
     int grid_ctas;           /* persistent CTAs per step launch (0: one per work item) */
+    double gravity;          /* System.gravity (kernels built with GRAV only) */
     R *tape;                 /* adjoint tape of this step (kernels built with TAPE only) */
     long long tape_plane;    /* elements per tape field (padded cells) */
 };
@@ -100,7 +101,9 @@ struct TapeCtx {
     }
 };
 
-/* Load W at padded (r, c), remapping ghost cells to their source. */
+/* Load W at padded (r, c), remapping ghost cells to their source.  Ghost
+ * cells of custom (host callback) sides are read as stored: the host wrote
+ * them after the previous step. */
 template <class R>
 __device__ __forceinline__ void fetch_w(const Mh2dArgs<R> &a, const R *const *Win,
                                         const R *const *Uin, bool raw, int r, int c, R w[5])
@@ -114,22 +117,22 @@ __device__ __forceinline__ void fetch_w(const Mh2dArgs<R> &a, const R *const *Wi
             f = a.bc[0]; k = g - 1 - c;
             if (f == BC_NONE) cons = true;
             else if (f == BC_PERIODIC) cc = g + nx - 1 - k;
-            else { cc = g + k; neg = (f == BC_REFLECTIVE) ? 1 : 0; }
+            else if (f != BC_CUSTOM) { cc = g + k; neg = (f == BC_REFLECTIVE) ? 1 : 0; }
         } else if (c >= g + nx) {
             f = a.bc[1]; k = c - g - nx;
             if (f == BC_NONE) cons = true;
             else if (f == BC_PERIODIC) cc = g + k;
-            else { cc = g + nx - 1 - k; neg = (f == BC_REFLECTIVE) ? 1 : 0; }
+            else if (f != BC_CUSTOM) { cc = g + nx - 1 - k; neg = (f == BC_REFLECTIVE) ? 1 : 0; }
         } else if (r < g) {
             f = a.bc[2]; k = g - 1 - r;
             if (f == BC_NONE) cons = true;
             else if (f == BC_PERIODIC) rr = g + ny - 1 - k;
-            else { rr = g + k; neg = (f == BC_REFLECTIVE) ? 2 : 0; }
+            else if (f != BC_CUSTOM) { rr = g + k; neg = (f == BC_REFLECTIVE) ? 2 : 0; }
         } else if (r >= g + ny) {
             f = a.bc[3]; k = r - g - ny;
             if (f == BC_NONE) cons = true;
             else if (f == BC_PERIODIC) rr = g + k;
-            else { rr = g + ny - 1 - k; neg = (f == BC_REFLECTIVE) ? 2 : 0; }
+            else if (f != BC_CUSTOM) { rr = g + ny - 1 - k; neg = (f == BC_REFLECTIVE) ? 2 : 0; }
         }
     }
     const long long idx = (long long) rr * a.pitch + cc;
@@ -250,7 +253,7 @@ __device__ __forceinline__ int solve_faces(Mh2dShared<R, NT> &sm, const GasConst
  * rows) of step n with time step dt.  Shared by the single-grid and the
  * batched kernels; the caller reduces mx_x / mx_y and handles errors.
  */
-template <class R, int LIM, int NT, int FIRST_ORDER, bool TAPE = false>
+template <class R, int LIM, int NT, int FIRST_ORDER, bool TAPE = false, bool GRAV = false>
 __device__ __forceinline__ void mh2d_item(const Mh2dArgs<R> &a, Mh2dShared<R, NT> &sm, int item,
                                           long long n, double dt, double &mx_x, double &mx_y,
                                           int &err)
@@ -427,7 +430,20 @@ __device__ __forceinline__ void mh2d_item(const Mh2dArgs<R> &a, Mh2dShared<R, NT
                 v = v + (gbot[ymap[q]] * dtr) * Ay;
                 v = v - (gtop[ymap[q]] * dtr) * Ay;
                 Un[q] = v;
-                Uout[q][idx] = v;
+                if constexpr (!GRAV) Uout[q][idx] = v;
+            }
+            if constexpr (GRAV) {
+                /* gravity source, RK4 on energy (src/source_term.c:185-240) */
+                const R pf = (R) (-dt * a.gravity);
+                const R km = pf * Un[0];
+                const R k1 = pf * Un[2];
+                const R k2 = pf * (Un[2] + R(0.5) * km);
+                const R k3 = k2;
+                const R k4 = pf * (Un[2] + km);
+                Un[2] = Un[2] + km;
+                Un[3] = Un[3] + (k1 + R(2) * k2 + R(2) * k3 + k4) / R(6);
+#pragma unroll
+                for (int q = 0; q < 4; q++) Uout[q][idx] = Un[q];
             }
             R w[4];
             cons_to_prim_2d_guarded(a.gas, (R) a.vol, Un[0], Un[1], Un[2], Un[3], w);
@@ -477,7 +493,7 @@ __device__ __forceinline__ void mh2d_item(const Mh2dArgs<R> &a, Mh2dShared<R, NT
  * SMs that finish early take more work (the FP64 pipe of an SM is shared by
  * its CTAs).
  */
-template <class R, int LIM, int NT, int FIRST_ORDER, bool TAPE = false>
+template <class R, int LIM, int NT, int FIRST_ORDER, bool TAPE = false, bool GRAV = false>
 __global__ void __launch_bounds__(NT, 4) mh2d_step_kernel(const Mh2dArgs<R> a)
 {
     static_assert(NT % 32 == 0, "NT must be a whole number of warps");
@@ -514,7 +530,7 @@ __global__ void __launch_bounds__(NT, 4) mh2d_step_kernel(const Mh2dArgs<R> a)
         const int item = sm.item;
         __syncthreads();
         if (item >= n_items) break;
-        mh2d_item<R, LIM, NT, FIRST_ORDER, TAPE>(a, sm, item, n, dt, mx_x, mx_y, err);
+        mh2d_item<R, LIM, NT, FIRST_ORDER, TAPE, GRAV>(a, sm, item, n, dt, mx_x, mx_y, err);
     }
 
     if (err) record_error(ctrl, err, (int) blockIdx.x);

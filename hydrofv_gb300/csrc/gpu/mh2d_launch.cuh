@@ -74,8 +74,14 @@ __global__ void mh2d_materialize_kernel(const Mh2dArgs<R> a, int buf, R *out0, R
         const bool in_x = c >= a.g && c < a.g + a.nx;
         const bool in_y = r >= a.g && r < a.g + a.ny;
         R w[5];
-        if (!in_x && !in_y) {
-            /* corners: converted, never overwritten by a boundary routine */
+        const bool custom_band = (c < a.g && a.bc[0] == BC_CUSTOM) || (c >= a.g + a.nx && a.bc[1] == BC_CUSTOM) ||
+                                 (r < a.g && a.bc[2] == BC_CUSTOM) || (r >= a.g + a.ny && a.bc[3] == BC_CUSTOM);
+        if (!in_x && !in_y && custom_band) {
+            /* a corner inside a custom side's band: what the host routine left there */
+#pragma unroll
+            for (int q = 0; q < 4; q++) w[q] = W[q][idx];
+        } else if (!in_x && !in_y) {
+            /* corners: converted, never overwritten by a built-in boundary routine */
             cons_to_prim_2d_guarded(a.gas, (R) a.vol, U[0][idx], U[1][idx], U[2][idx], U[3][idx], w);
         } else {
             fetch_w(a, W, U, false, r, c, w);
@@ -85,12 +91,51 @@ __global__ void mh2d_materialize_kernel(const Mh2dArgs<R> a, int buf, R *out0, R
     }
 }
 
+/* W = U->W(U) over every padded cell (src/system.c:763-802, the reference's
+ * all-cell conversion before its boundary routine): what a host boundary
+ * callback sees. */
+template <class R>
+__global__ void mh2d_convert_all_kernel(const Mh2dArgs<R> a, int buf, R *out0, R *out1, R *out2, R *out3)
+{
+    const long long total = (long long) (a.nx + 2 * a.g) * (a.ny + 2 * a.g);
+    const R *const *U = a.U[buf];
+    for (long long k = blockIdx.x * (long long) blockDim.x + threadIdx.x; k < total;
+         k += (long long) gridDim.x * blockDim.x) {
+        R w[4];
+        cons_to_prim_2d_guarded(a.gas, (R) a.vol, U[0][k], U[1][k], U[2][k], U[3][k], w);
+        out0[k] = w[0];
+        out1[k] = w[1];
+        out2[k] = w[2];
+        out3[k] = w[3];
+    }
+}
+
+/* Sound speed of the ghost cells of custom sides (mask bit s = side s:
+ * x_min, x_max, y_min, y_max) after the host wrote their W. */
+template <class R>
+__global__ void mh2d_ghost_sound_speed_kernel(const Mh2dArgs<R> a, int buf, int mask)
+{
+    const int tx = a.nx + 2 * a.g, ty = a.ny + 2 * a.g;
+    const long long total = (long long) tx * ty;
+    R *const *W = a.W[buf];
+    for (long long k = blockIdx.x * (long long) blockDim.x + threadIdx.x; k < total;
+         k += (long long) gridDim.x * blockDim.x) {
+        const int r = (int) (k / tx), c = (int) (k % tx);
+        const bool on = ((mask & 1) && c < a.g) || ((mask & 2) && c >= a.g + a.nx) ||
+                        ((mask & 4) && r < a.g) || ((mask & 8) && r >= a.g + a.ny);
+        if (on) W[4][k] = sound_speed(a.gas, W[0][k], W[3][k]);
+    }
+}
+
 /* ------------------------------------------------------------- launchers */
 
 template <class R, int LIM, int FIRST_ORDER>
 static cudaError_t launch_step_lim(const Mh2dArgs<R> &a, int grid, cudaStream_t s)
 {
-    mh2d_step_kernel<R, LIM, MH2D_THREADS, FIRST_ORDER><<<grid, MH2D_THREADS, 0, s>>>(a);
+    if (a.gravity != 0.0)
+        mh2d_step_kernel<R, LIM, MH2D_THREADS, FIRST_ORDER, false, true><<<grid, MH2D_THREADS, 0, s>>>(a);
+    else
+        mh2d_step_kernel<R, LIM, MH2D_THREADS, FIRST_ORDER><<<grid, MH2D_THREADS, 0, s>>>(a);
     return cudaGetLastError();
 }
 
@@ -125,6 +170,20 @@ template <class R>
 cudaError_t mh2d_launch_prepare(const Mh2dArgs<R> &a, cudaStream_t s)
 {
     mh2d_prepare_kernel<R><<<1024, 256, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+template <class R>
+cudaError_t mh2d_launch_convert_all(const Mh2dArgs<R> &a, int buf, R *const out[4], cudaStream_t s)
+{
+    mh2d_convert_all_kernel<R><<<1024, 256, 0, s>>>(a, buf, out[0], out[1], out[2], out[3]);
+    return cudaGetLastError();
+}
+
+template <class R>
+cudaError_t mh2d_launch_ghost_sound_speed(const Mh2dArgs<R> &a, int buf, int mask, cudaStream_t s)
+{
+    mh2d_ghost_sound_speed_kernel<R><<<1024, 256, 0, s>>>(a, buf, mask);
     return cudaGetLastError();
 }
 

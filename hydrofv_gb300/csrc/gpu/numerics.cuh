@@ -53,6 +53,7 @@ enum : int {
     BC_REFLECTIVE = 2,
     BC_TRANSMISSIVE = 3,
     BC_PERIODIC = 4,
+    BC_CUSTOM = 5,      /* host callback: ghost W is written by the host, read as stored */
 };
 
 /* Device error codes (mapped to ErrorStatus on the host). */

@@ -86,6 +86,9 @@ struct HydroRun2D {
     Mh2dArgs<float> args32{};
     cudaGraphExec_t graph = nullptr;
     cudaEvent_t ev[6] = {};
+    HydroHostBcFn host_bc = nullptr;  /* custom sides: host boundary routine after every step */
+    void *host_bc_ctx = nullptr;
+    int custom_mask = 0;              /* bit s: side s (x_min, x_max, y_min, y_max) is custom */
     bool begun = false;
     bool have_initial = false;
     /* statistics */
@@ -133,6 +136,7 @@ static void setup_args(HydroRun2D *run, Mh2dArgs<R> &a, const HydroGrid2D *grid,
     a.vol = grid->vol;
     a.first_order = (grid->integrator == INTEGRATOR_GODUNOV_FIRST_ORDER_2D) ? 1 : 0;
     a.grid_ctas = mh2d_resident_ctas<R>(grid->limiter, a.first_order, run->device);
+    a.gravity = grid->gravity;
 }
 
 static cudaError_t launch_step(HydroRun2D *run)
@@ -504,6 +508,69 @@ static int record_graph(HydroRun2D *run, HydroRunOutcome *oc)
     return 0;
 }
 
+extern "C" int hydro_run2d_set_host_bc(HydroRun2D *run, HydroHostBcFn fn, void *ctx, HydroRunOutcome *oc)
+{
+    memset(oc, 0, sizeof *oc);
+    int mask = 0;
+    for (int s = 0; s < 4; s++)
+        if (run->grid.bc[s] == BC_CUSTOM) mask |= 1 << s;
+    if (mask && run->fp32) {
+        oc->kind = HYDRO_RUN_UNSUPPORTED;
+        snprintf(oc->message, sizeof oc->message, "Custom boundary conditions need the FP64 state.");
+        return -1;
+    }
+    run->host_bc = mask ? fn : nullptr;
+    run->host_bc_ctx = ctx;
+    run->custom_mask = mask;
+    return 0;
+}
+
+/* After a step: U->W of every cell to the host, the host boundary routine,
+ * the ghost bands of the custom sides back into the W the next step reads,
+ * and their sound speed (src/integrator_muscl_hancock.c:1121-1130 with the
+ * boundary routine on the host). */
+static int apply_host_bc(HydroRun2D *run, HydroRunOutcome *oc)
+{
+    const int buf = (int) (run->ctrl_h->num_steps & 1);
+    double *out[4];
+    for (int q = 0; q < 4; q++) out[q] = static_cast<double *>(run->snap_d[q]);
+    CK(mh2d_launch_convert_all<double>(run->args, buf, out, run->stream), "convert kernel");
+    run->kernel_launches++;
+    if (!run->snap_h)
+        CK(cudaMallocHost(&run->snap_h, 4 * run->ncell * sizeof(double)), "cudaMallocHost(boundary)");
+    double *Wh[4];
+    for (int q = 0; q < 4; q++) Wh[q] = run->snap_h + q * run->ncell;
+    if (download_fields(run, run->snap_d, Wh, oc)) return -1;
+    CK(cudaStreamSynchronize(run->stream), "boundary download");
+    const int rc = run->host_bc(run->host_bc_ctx, Wh);
+    if (rc != 0) {
+        oc->kind = HYDRO_RUN_CALLBACK_ERROR;
+        oc->code = rc;
+        snprintf(oc->message, sizeof oc->message, "The host boundary routine failed.");
+        return -1;
+    }
+    const int g = run->grid.g, nx = run->grid.nx, ny = run->grid.ny, tx = run->tx, ty = run->ty;
+    const size_t pitch = (size_t) tx * sizeof(double);
+    for (int q = 0; q < 4; q++) {
+        double *dst = run->args.W[buf][q];
+        const double *src = Wh[q];
+        if (run->custom_mask & 1)
+            CK(cudaMemcpy2DAsync(dst, pitch, src, pitch, (size_t) g * sizeof(double), (size_t) ty,
+                                 cudaMemcpyHostToDevice, run->stream), "H2D boundary");
+        if (run->custom_mask & 2)
+            CK(cudaMemcpy2DAsync(dst + g + nx, pitch, src + g + nx, pitch, (size_t) g * sizeof(double),
+                                 (size_t) ty, cudaMemcpyHostToDevice, run->stream), "H2D boundary");
+        if (run->custom_mask & 4)
+            CK(cudaMemcpyAsync(dst, src, (size_t) g * pitch, cudaMemcpyHostToDevice, run->stream), "H2D boundary");
+        if (run->custom_mask & 8)
+            CK(cudaMemcpyAsync(dst + (size_t) (g + ny) * tx, src + (size_t) (g + ny) * tx, (size_t) g * pitch,
+                               cudaMemcpyHostToDevice, run->stream), "H2D boundary");
+    }
+    CK(mh2d_launch_ghost_sound_speed<double>(run->args, buf, run->custom_mask, run->stream), "sound speed kernel");
+    run->kernel_launches++;
+    return 0;
+}
+
 /* Enqueue `k` step kernels. */
 static int enqueue_steps(HydroRun2D *run, long long k, HydroRunOutcome *oc)
 {
@@ -578,8 +645,17 @@ extern "C" int hydro_run2d_advance(HydroRun2D *run, HydroSnapshotFn snap, void *
         }
         if (k > remaining) k = remaining;
         if (k < 1) k = 1;
+        if (run->host_bc) k = 1;   /* the host boundary routine runs after every step */
+        const long long steps_before = c->num_steps;
         CK(cudaEventRecord(run->ev[2], run->stream), "cudaEventRecord");
         if (enqueue_steps(run, k, oc)) return -1;
+        if (run->host_bc) {
+            if (pull_control(run, oc)) return -1;
+            if (c->num_steps > steps_before && c->error_code == 0 && apply_host_bc(run, oc)) {
+                fill_outcome(run, oc);
+                return -1;
+            }
+        }
         CK(cudaEventRecord(run->ev[3], run->stream), "cudaEventRecord");
         if (pull_control(run, oc)) return -1;
         float ms = 0;

@@ -118,18 +118,11 @@ static ErrorStatus setup_grid2d(const BoundaryConditionParam *bcp, const System 
                            bcp->boundary_condition_flag_y_min_, bcp->boundary_condition_flag_y_max_ };
     for (int k = 0; k < 4; k++)
     {
-        if (flags[k] == BOUNDARY_CONDITION_CUSTOM)
-            return WRAP_RAISE_ERROR(NOT_IMPLEMENTED_ERROR,
-                                    "Custom boundary conditions are not available on the GPU path.");
-        if (flags[k] < BOUNDARY_CONDITION_NONE || flags[k] > BOUNDARY_CONDITION_PERIODIC)
+        if (flags[k] < BOUNDARY_CONDITION_NONE || flags[k] > BOUNDARY_CONDITION_CUSTOM)
             return WRAP_RAISE_ERROR(VALUE_ERROR, "Boundary condition flag not recognized.");
         grid->bc[k] = flags[k];
     }
-    if (s->gravity != 0.0)
-    {
-        return WRAP_RAISE_ERROR(NOT_IMPLEMENTED_ERROR,
-                                "A non-zero gravity source is not available on the GPU path.");
-    }
+    grid->gravity = s->gravity;
     const int g = s->num_ghost_cells_side;
     const long long tx = s->num_cells_x + 2 * g, ty = s->num_cells_y + 2 * g;
     if (!uniform(s->surface_area_x_, tx) || !uniform(s->surface_area_y_, ty) || !uniform(s->volume_, tx * ty))
@@ -181,6 +174,36 @@ static int snapshot_cb(void *vctx, double *const W[4], int64 num_steps, double t
     SimulationStatus st = { num_steps, t, dt };
     ctx->status = WRAP_TRACEBACK(store_snapshot(ctx->bcp, &view, ctx->ip, &st, ctx->sp));
     return ctx->status.return_code == SUCCESS ? 0 : 1;
+}
+
+/* Host boundary routine for custom sides: the reference's boundary routine
+ * (src/boundary.c:513-777, custom sides through their callbacks) on a
+ * System view of the converted state. */
+typedef struct HostBcCtx
+{
+    BoundaryConditionParam bcp;
+    System system;
+    ErrorStatus status;
+} HostBcCtx;
+
+static int host_bc_cb(void *vctx, double *const W[4])
+{
+    HostBcCtx *ctx = vctx;
+    System view = ctx->system;
+    view.density_ = W[0];
+    view.velocity_x_ = W[1];
+    view.velocity_y_ = W[2];
+    view.pressure_ = W[3];
+    free_traceback(&ctx->status);
+    ctx->status = WRAP_TRACEBACK(set_boundary_condition(&ctx->bcp, &view));
+    return ctx->status.return_code == SUCCESS ? 0 : 1;
+}
+
+static int has_custom(const HydroGrid2D *grid)
+{
+    for (int k = 0; k < 4; k++)
+        if (grid->bc[k] == BOUNDARY_CONDITION_CUSTOM) return 1;
+    return 0;
 }
 
 static HydroStepParams step_params(const IntegratorParam *ip, const StoringParam *sp)
@@ -236,8 +259,14 @@ static ErrorStatus run_2d(
     double *U[4] = { s->mass_, s->momentum_x_, s->momentum_y_, s->energy_ };
     const HydroStepParams params = step_params(ip, sp);
     SnapCtx ctx = { bcp, s, ip, sp, make_success_error_status() };
+    HostBcCtx bctx;
+    memset(&bctx, 0, sizeof bctx);
+    bctx.bcp = *bcp;
+    bctx.system = *s;
+    bctx.status = make_success_error_status();
 
     int rc = hydro_run2d_create(&grid, opt, &run, &oc);
+    if (rc == 0 && has_custom(&grid)) rc = hydro_run2d_set_host_bc(run, host_bc_cb, &bctx, &oc);
     if (rc == 0) rc = hydro_run2d_upload(run, W, U, 0, &oc);
     if (rc == 0) rc = hydro_run2d_begin(run, &params, simp->tf, opt->max_steps, sp->store_count_, &oc);
     int advanced = 0;
@@ -273,10 +302,17 @@ static ErrorStatus run_2d(
 
     if (rc != 0)
     {
+        if (oc.kind == HYDRO_RUN_CALLBACK_ERROR && bctx.status.return_code != SUCCESS)
+        {
+            free_traceback(&ctx.status);
+            return bctx.status;
+        }
+        free_traceback(&bctx.status);
         if (oc.kind == HYDRO_RUN_CALLBACK_ERROR && ctx.status.return_code != SUCCESS) return ctx.status;
         free_traceback(&ctx.status);
         return outcome_error(&oc);
     }
+    free_traceback(&bctx.status);
     return make_success_error_status();
 }
 
@@ -508,6 +544,7 @@ struct HydroGpuSolver
     HydroStepParams params;
     int begun;
     int64 launches_at_create;
+    HostBcCtx bc;                 /* custom sides: the boundary routine's inputs */
 };
 
 ErrorStatus hydro_gpu_solver_create(
@@ -541,7 +578,11 @@ ErrorStatus hydro_gpu_solver_create(
     HydroRunOutcome oc;
     double *W[4] = { system->density_, system->velocity_x_, system->velocity_y_, system->pressure_ };
     double *U[4] = { system->mass_, system->momentum_x_, system->momentum_y_, system->energy_ };
+    sv->bc.bcp = *bcp;
+    sv->bc.system = *system;
+    sv->bc.status = make_success_error_status();
     int rc = hydro_run2d_create(&sv->grid, &opt, &sv->run, &oc);
+    if (rc == 0 && has_custom(&sv->grid)) rc = hydro_run2d_set_host_bc(sv->run, host_bc_cb, &sv->bc, &oc);
     if (rc == 0) rc = hydro_run2d_upload(sv->run, W, U, 1, &oc);
     if (rc != 0)
     {
@@ -587,7 +628,16 @@ ErrorStatus hydro_gpu_solver_advance(
         status->t = oc.t;
         status->dt = oc.dt;
     }
-    if (rc != 0) return outcome_error(&oc);
+    if (rc != 0)
+    {
+        if (oc.kind == HYDRO_RUN_CALLBACK_ERROR && sv->bc.status.return_code != SUCCESS)
+        {
+            ErrorStatus e = sv->bc.status;
+            sv->bc.status = make_success_error_status();
+            return e;
+        }
+        return outcome_error(&oc);
+    }
     return make_success_error_status();
 }
 
@@ -618,6 +668,7 @@ int64 hydro_gpu_solver_kernel_launches(const HydroGpuSolver *sv)
 void hydro_gpu_solver_destroy(HydroGpuSolver *sv)
 {
     if (!sv) return;
+    free_traceback(&sv->bc.status);
     hydro_run2d_destroy(sv->run);
     free(sv);
 }
@@ -660,6 +711,9 @@ ErrorStatus hydro_gpu_batch_create(
         e = WRAP_TRACEBACK(finalize_boundary_condition_param(&systems[i], &bcps[i]));
         if (e.return_code == SUCCESS) e = WRAP_TRACEBACK(hydro_final_check(&systems[i], ip));
         if (e.return_code == SUCCESS) e = setup_grid2d(&bcps[i], &systems[i], ip, &grids[i]);
+        if (e.return_code == SUCCESS && (has_custom(&grids[i]) || grids[i].gravity != 0.0))
+            e = WRAP_RAISE_ERROR(NOT_IMPLEMENTED_ERROR,
+                                 "Batches take built-in boundary conditions and no gravity source.");
         if (e.return_code != SUCCESS)
         {
             free(grids);
@@ -792,6 +846,8 @@ ErrorStatus hydro_gpu_adjoint_create(
     memset(&grid, 0, sizeof grid);
     e = setup_grid2d(bcp, system, ip, &grid);
     if (e.return_code != SUCCESS) return e;
+    if (grid.gravity != 0.0)
+        return WRAP_RAISE_ERROR(NOT_IMPLEMENTED_ERROR, "The adjoint does not differentiate the gravity source.");
     HydroGpuAdjoint *ad = calloc(1, sizeof *ad);
     if (!ad) return WRAP_RAISE_ERROR(MEMORY_ERROR, "Failed to allocate the adjoint session.");
     const HydroGpuOptions opt = options ? *options : hydro_gpu_default_options();

@@ -12,10 +12,18 @@ np.random.default_rng(seed).
 """
 from __future__ import annotations
 
+import ctypes as C
 import math
 from dataclasses import dataclass
 
 import numpy as np
+
+_dp = C.POINTER(C.c_double)
+
+# Custom boundary callback of a 2D side, as BoundaryConditionParam stores it
+# (src/boundary.h:40-48): (density, velocity_x, velocity_y, pressure,
+# num_ghost_cells_side, num_cells_x, num_cells_y), padded arrays in place.
+BcCallback = C.CFUNCTYPE(None, _dp, _dp, _dp, _dp, C.c_int, C.c_int, C.c_int)
 
 
 @dataclass
@@ -39,6 +47,8 @@ class Problem2D:
     tf: float = 1.0
     max_steps: int = -1
     name: str = ""
+    gravity: float = 0.0
+    custom_bc: tuple = (None, None, None, None)   # BcCallback per side for "custom" sides
 
     def copy(self) -> "Problem2D":
         import copy
@@ -104,11 +114,21 @@ def primitive_to_conserved_1d(W: np.ndarray, gamma: float, vol: float) -> np.nda
     return U
 
 
-def apply_bc_2d(W: np.ndarray, g: int, nx: int, ny: int, bc) -> None:
-    """Built-in ghost fill on W in place (src/boundary.c:513-777)."""
+def apply_bc_2d(W: np.ndarray, g: int, nx: int, ny: int, bc, custom=(None, None, None, None)) -> None:
+    """Ghost fill on W in place, sides in the reference's order
+    (src/boundary.c:513-777); custom sides call their BcCallback."""
     flags = list(bc)
+
+    def call(side):
+        assert W.flags.c_contiguous and W.dtype == np.float64
+        ptrs = [W[q].ctypes.data_as(_dp) for q in range(4)]
+        custom[side](*ptrs, g, nx, ny)
+
     for side in (0, 1):
         f = flags[side]
+        if f == "custom":
+            call(side)
+            continue
         if f == "none" or (f == "periodic" and side == 0):
             continue
         for k in range(g):
@@ -123,6 +143,9 @@ def apply_bc_2d(W: np.ndarray, g: int, nx: int, ny: int, bc) -> None:
                 W[1, rows, dst] = -W[1, rows, src]
     for side in (0, 1):
         f = flags[2 + side]
+        if f == "custom":
+            call(2 + side)
+            continue
         if f == "none" or (f == "periodic" and side == 0):
             continue
         cols = slice(g, g + nx)
@@ -323,3 +346,66 @@ def right_half_density_squared(p: Problem2D, W: np.ndarray) -> tuple[float, np.n
     seed = np.zeros_like(W)
     seed[0][mask] = 2.0 * rho[mask] * vol
     return J, seed
+
+
+def lid_top_bc(lid_u: float = 10.0, lid_v: float = -0.5) -> BcCallback:
+    """Top-side callback of the modified lid-driven cavity example
+    (examples/modified_lid_driven_cavity_2d/lid_driven_cavity_2d.c:39-58):
+    every column of the top ghost rows mirrors density and pressure and
+    takes the lid velocity."""
+    def fn(rho, vx, vy, p, g, nx, ny):
+        tx, ty = nx + 2 * g, ny + 2 * g
+        R, X, Y, P = (np.ctypeslib.as_array(a, shape=(ty, tx)) for a in (rho, vx, vy, p))
+        for j in range(g):
+            R[g + ny + j, :] = R[g + ny - 1 - j, :]
+            X[g + ny + j, :] = lid_u
+            Y[g + ny + j, :] = lid_v
+            P[g + ny + j, :] = P[g + ny - 1 - j, :]
+    return BcCallback(fn)
+
+
+def rayleigh_taylor(nx: int = 122, ny: int = 122, g: int = 3, steps: int = 200) -> Problem2D:
+    """Rayleigh-Taylor example (examples/rayleign_taylor_2d/rayleigh_taylor_2d.c:
+    20-110): [0,0.5] x [0,2], gamma 5/3, gravity 0.1, periodic x, reflective y;
+    rho = 1 below y = 1, 2 above, hydrostatic p = 2.5 - 0.1 rho (y - 0.75),
+    vy = 0.0025 (1 - cos 4 pi x)(1 - cos(4/3 pi (y - 0.5))); MUSCL-Hancock,
+    MC, CFL 0.5."""
+    gamma = 5.0 / 3.0
+    grav = 0.1
+    x = mid_points(0.0, 0.5, nx, g)
+    y = mid_points(0.0, 2.0, ny, g)
+    X, Y = np.meshgrid(x, y)
+    W = np.zeros((4, ny + 2 * g, nx + 2 * g))
+    I = (slice(g, g + ny), slice(g, g + nx))
+    lower = Y < 1.0
+    W[0][I] = np.where(lower, 1.0, 2.0)[I]
+    W[1][I] = 0.0
+    W[3][I] = np.where(lower, 2.5 - grav * 1.0 * (Y - 0.75), 2.5 - grav * 2.0 * (Y - 0.75))[I]
+    W[2][I] = (0.0025 * (1.0 - np.cos(4 * math.pi * X)) * (1.0 - np.cos(4.0 / 3.0 * math.pi * (Y - 0.5))))[I]
+    bc = ("periodic", "periodic", "reflective", "reflective")
+    apply_bc_2d(W, g, nx, ny, bc)
+    vol = (0.5 / (nx + 2 * g)) * (2.0 / (ny + 2 * g))
+    U = primitive_to_conserved_2d(W, gamma, vol)
+    return Problem2D(nx, ny, g, 0.0, 0.5, 0.0, 2.0, gamma, W, U, bc, "muscl_hancock_2d",
+                     "riemann_solver_hllc", "monotonized_central", cfl=0.5, tf=1e300,
+                     max_steps=steps, name=f"rayleigh_taylor_{nx}x{ny}", gravity=grav)
+
+
+def lid_driven_cavity(n: int = 250, g: int = 3, steps: int = 200) -> Problem2D:
+    """Modified lid-driven cavity example
+    (examples/modified_lid_driven_cavity_2d/lid_driven_cavity_2d.c:20-110):
+    [0,1]^2, gamma 5/3, rho = 1, u = v = 0, p = 1; reflective except a custom
+    top side (lid_top_bc); MUSCL-Hancock, MC, CFL 0.5."""
+    gamma = 5.0 / 3.0
+    W = np.zeros((4, n + 2 * g, n + 2 * g))
+    I = (slice(g, g + n), slice(g, g + n))
+    W[0][I] = 1.0
+    W[3][I] = 1.0
+    bc = ("reflective", "reflective", "reflective", "custom")
+    custom = (None, None, None, lid_top_bc())
+    apply_bc_2d(W, g, n, n, bc, custom)
+    vol = (1.0 / (n + 2 * g)) ** 2
+    U = primitive_to_conserved_2d(W, gamma, vol)
+    return Problem2D(n, n, g, 0.0, 1.0, 0.0, 1.0, gamma, W, U, bc, "muscl_hancock_2d",
+                     "riemann_solver_hllc", "monotonized_central", cfl=0.5, tf=1e300,
+                     max_steps=steps, name=f"lid_driven_cavity_{n}", custom_bc=custom)

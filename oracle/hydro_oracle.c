@@ -29,7 +29,7 @@
 enum { OK = 0, FAILURE = 1, VALUE_ERROR = 2, POINTER_ERROR = 3, MEMORY_ERROR = 4,
        NOT_IMPLEMENTED_ERROR = 6 };
 enum { LIM_MINMOD = 1, LIM_VAN_LEER = 2, LIM_MC = 3 };
-enum { BC_NONE = 1, BC_REFLECTIVE = 2, BC_TRANSMISSIVE = 3, BC_PERIODIC = 4 };
+enum { BC_NONE = 1, BC_REFLECTIVE = 2, BC_TRANSMISSIVE = 3, BC_PERIODIC = 4, BC_CUSTOM = 5 };
 enum { SOLVER_EXACT = 1, SOLVER_HLLC = 2 };
 
 #define NEWTON_MAX_ITER 100      /* src/riemann_solver_exact.c:26 */
@@ -525,6 +525,7 @@ static int parse_bc(const char *s)
     if (!strcmp(s, "reflective")) return BC_REFLECTIVE;
     if (!strcmp(s, "transmissive")) return BC_TRANSMISSIVE;
     if (!strcmp(s, "periodic")) return BC_PERIODIC;
+    if (!strcmp(s, "custom")) return BC_CUSTOM;
     return -1;
 }
 
@@ -544,6 +545,8 @@ typedef struct
     int lim, solver;
     double tol;
     int bc[4];                   /* x_min, x_max, y_min, y_max */
+    OracleBcFn custom[4];        /* callbacks of custom sides (src/boundary.h:40-48) */
+    double gravity;              /* System.gravity */
     double *W[4];                /* rho, u, v, p */
     double *U[4];                /* mass, mom_x, mom_y, energy */
 } Grid;
@@ -579,6 +582,11 @@ static void boundary_2d(Grid *G)
     for (int side = 0; side < 2; side++)
     {
         const int f = G->bc[side];
+        if (f == BC_CUSTOM)
+        {
+            G->custom[side](W[0], W[1], W[2], W[3], g, nx, ny);
+            continue;
+        }
         if (f == BC_NONE || (f == BC_PERIODIC && side == 0)) continue;
         for (int k = 0; k < g; k++)
         {
@@ -606,6 +614,11 @@ static void boundary_2d(Grid *G)
     for (int side = 0; side < 2; side++)
     {
         const int f = G->bc[2 + side];
+        if (f == BC_CUSTOM)
+        {
+            G->custom[2 + side](W[0], W[1], W[2], W[3], g, nx, ny);
+            continue;
+        }
         if (f == BC_NONE || (f == BC_PERIODIC && side == 0)) continue;
         for (int i = g; i < g + nx; i++)
         {
@@ -831,6 +844,34 @@ static int godunov2d_step(Grid *G, double dt)
     return err;
 }
 
+/* Gravity source (src/source_term.c:185-259): RK4 kick of the interior
+ * momentum_y / energy after the step's conversion and boundary routine, then
+ * the conversion and the boundary routine again. */
+static void gravity_2d(Grid *G, double dt)
+{
+    if (G->gravity == 0.0) return;
+    const int g = G->g;
+    for (int i = g; i < g + G->nx; i++)
+    {
+        for (int j = g; j < g + G->ny; j++)
+        {
+            const int k = j * G->tx + i;
+            const double m = G->U[0][k];
+            const double my = G->U[2][k];
+            const double pf = - dt * G->gravity;
+            const double km = pf * m;
+            const double k1 = pf * my;
+            const double k2 = pf * (my + 0.5 * km);
+            const double k3 = k2;
+            const double k4 = pf * (my + km);
+            G->U[2][k] += km;
+            G->U[3][k] += (k1 + 2.0 * k2 + 2.0 * k3 + k4) / 6.0;
+        }
+    }
+    conserved_to_primitive_2d(G);
+    boundary_2d(G);
+}
+
 int oracle_run_2d(
     int nx, int ny, int g,
     double x_min, double x_max, double y_min, double y_max, double gamma,
@@ -841,6 +882,25 @@ int oracle_run_2d(
     double *mass, double *mom_x, double *mom_y, double *energy,
     long long *num_steps, double *t, double *dt,
     char *errbuf, int errlen)
+{
+    return oracle_run_2d_ex(nx, ny, g, x_min, x_max, y_min, y_max, gamma, integrator, riemann_solver,
+                            slope_limiter, bc_x_min, bc_x_max, bc_y_min, bc_y_max, cfl, tf, max_steps,
+                            rho, u, v, p, mass, mom_x, mom_y, energy, num_steps, t, dt, errbuf, errlen,
+                            0.0, NULL, NULL, NULL, NULL);
+}
+
+int oracle_run_2d_ex(
+    int nx, int ny, int g,
+    double x_min, double x_max, double y_min, double y_max, double gamma,
+    const char *integrator, const char *riemann_solver, const char *slope_limiter,
+    const char *bc_x_min, const char *bc_x_max, const char *bc_y_min, const char *bc_y_max,
+    double cfl, double tf, long long max_steps,
+    double *rho, double *u, double *v, double *p,
+    double *mass, double *mom_x, double *mom_y, double *energy,
+    long long *num_steps, double *t, double *dt,
+    char *errbuf, int errlen,
+    double gravity, OracleBcFn bc_fn_x_min, OracleBcFn bc_fn_x_max, OracleBcFn bc_fn_y_min,
+    OracleBcFn bc_fn_y_max)
 {
     set_err(errbuf, errlen, "");
     *num_steps = 0; *t = 0.0; *dt = 0.0;
@@ -867,6 +927,15 @@ int oracle_run_2d(
     if (G.lim < 0) { set_err(errbuf, errlen, "Slope limiter not recognized."); return VALUE_ERROR; }
     for (int s = 0; s < 4; s++)
         if (G.bc[s] < 0) { set_err(errbuf, errlen, "Boundary condition not recognized."); return VALUE_ERROR; }
+    G.custom[0] = bc_fn_x_min; G.custom[1] = bc_fn_x_max;
+    G.custom[2] = bc_fn_y_min; G.custom[3] = bc_fn_y_max;
+    for (int s = 0; s < 4; s++)
+        if (G.bc[s] == BC_CUSTOM && !G.custom[s])
+        {
+            set_err(errbuf, errlen, "A custom boundary condition needs its callback.");
+            return VALUE_ERROR;
+        }
+    G.gravity = gravity;
     G.W[0] = rho; G.W[1] = u; G.W[2] = v; G.W[3] = p;
     G.U[0] = mass; G.U[1] = mom_x; G.U[2] = mom_y; G.U[3] = energy;
 
@@ -887,6 +956,7 @@ int oracle_run_2d(
         }
         conserved_to_primitive_2d(&G);
         boundary_2d(&G);
+        gravity_2d(&G, step);
         *t += step;
         (*num_steps)++;
     }

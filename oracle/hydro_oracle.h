@@ -23,6 +23,24 @@ int oracle_run_2d(
     long long *num_steps, double *t, double *dt,
     char *errbuf, int errlen);
 
+/* Custom boundary callback, as in BoundaryConditionParam (src/boundary.h:40-48). */
+typedef void (*OracleBcFn)(double *density, double *velocity_x, double *velocity_y, double *pressure,
+                           int num_ghost_cells_side, int num_cells_x, int num_cells_y);
+
+/* oracle_run_2d plus the gravity source and custom-side callbacks. */
+int oracle_run_2d_ex(
+    int nx, int ny, int g,
+    double x_min, double x_max, double y_min, double y_max, double gamma,
+    const char *integrator, const char *riemann_solver, const char *slope_limiter,
+    const char *bc_x_min, const char *bc_x_max, const char *bc_y_min, const char *bc_y_max,
+    double cfl, double tf, long long max_steps,
+    double *rho, double *u, double *v, double *p,
+    double *mass, double *mom_x, double *mom_y, double *energy,
+    long long *num_steps, double *t, double *dt,
+    char *errbuf, int errlen,
+    double gravity, OracleBcFn bc_fn_x_min, OracleBcFn bc_fn_x_max, OracleBcFn bc_fn_y_min,
+    OracleBcFn bc_fn_y_max);
+
 int oracle_run_1d(
     int nx, int g, double x_min, double x_max, double gamma,
     const char *integrator, const char *riemann_solver, const char *slope_limiter,

@@ -51,6 +51,11 @@ def _bind(lib: C.CDLL, prefix: str) -> C.CDLL:
     f.argtypes = ([C.c_int] * 3 + [C.c_double] * 5 + [C.c_char_p] * 7
                   + [C.c_double, C.c_double, C.c_longlong] + [_dp] * 8
                   + [_i64p, _dp, _dp, C.c_char_p, C.c_int])
+    f = getattr(lib, prefix + "run_2d_ex")
+    f.restype = C.c_int
+    f.argtypes = ([C.c_int] * 3 + [C.c_double] * 5 + [C.c_char_p] * 7
+                  + [C.c_double, C.c_double, C.c_longlong] + [_dp] * 8
+                  + [_i64p, _dp, _dp, C.c_char_p, C.c_int] + [C.c_double] + [C.c_void_p] * 4)
     f = getattr(lib, prefix + "run_1d")
     f.restype = C.c_int
     f.argtypes = ([C.c_int] * 2 + [C.c_double] * 3 + [C.c_char_p] * 5
@@ -120,8 +125,10 @@ class Backend:
         t = C.c_double(0)
         dt = C.c_double(0)
         err = C.create_string_buffer(4096)
-        f = getattr(self.lib, self.prefix + "run_2d")
+        f = getattr(self.lib, self.prefix + "run_2d_ex")
         enc = lambda s: s.encode() if s is not None else None
+        cbs = [C.cast(cb, C.c_void_p) if cb is not None else None
+               for cb in getattr(prob, "custom_bc", (None,) * 4)]
         t0 = time.perf_counter()
         rc = f(prob.nx, prob.ny, prob.g, prob.x_min, prob.x_max, prob.y_min, prob.y_max,
                prob.gamma, enc(prob.integrator), enc(prob.riemann_solver),
@@ -129,7 +136,8 @@ class Backend:
                prob.cfl, prob.tf, prob.max_steps,
                _ptr(W[0]), _ptr(W[1]), _ptr(W[2]), _ptr(W[3]),
                _ptr(U[0]), _ptr(U[1]), _ptr(U[2]), _ptr(U[3]),
-               C.byref(n), C.byref(t), C.byref(dt), err, len(err))
+               C.byref(n), C.byref(t), C.byref(dt), err, len(err),
+               float(getattr(prob, "gravity", 0.0)), *cbs)
         secs = time.perf_counter() - t0
         return Result(rc, W, U, n.value, t.value, dt.value,
                       err.value.decode(errors="replace"), secs)
@@ -173,9 +181,9 @@ class Backend:
 # Seeded workloads live with the package (hydrofv_gb300/problems.py); they are
 # re-exported here so tests can use one namespace.
 from hydrofv_gb300.problems import (  # noqa: E402,F401
-    Problem1D, Problem2D, apply_bc_2d, four_quadrant, mid_points, point_blast,
-    primitive_to_conserved_1d, primitive_to_conserved_2d, random_problem_2d, shear_layer,
-    sod_1d,
+    Problem1D, Problem2D, apply_bc_2d, four_quadrant, lid_driven_cavity, lid_top_bc, mid_points,
+    point_blast, primitive_to_conserved_1d, primitive_to_conserved_2d, random_problem_2d,
+    rayleigh_taylor, shear_layer, sod_1d,
 )
 
 

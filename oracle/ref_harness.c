@@ -83,7 +83,10 @@ static int finish(ErrorStatus e, char *errbuf, int errlen, int fixed_stop)
  * overwritten with the final state.  bc[] = {x_min, x_max, y_min, y_max}.
  * max_steps < 0 runs to tf.  Returns the reference's return_code (0 = OK).
  */
-int ref_run_2d(
+typedef void (*RefBcFn)(double *, double *, double *, double *, int, int, int);
+
+/* ref_run_2d plus System.gravity and the callbacks of custom sides. */
+int ref_run_2d_ex(
     int nx, int ny, int g,
     double x_min, double x_max, double y_min, double y_max, double gamma,
     const char *integrator, const char *riemann_solver, const char *slope_limiter,
@@ -92,7 +95,8 @@ int ref_run_2d(
     double *rho, double *u, double *v, double *p,
     double *mass, double *mom_x, double *mom_y, double *energy,
     long long *num_steps, double *t, double *dt,
-    char *errbuf, int errlen
+    char *errbuf, int errlen,
+    double gravity, RefBcFn fn_x_min, RefBcFn fn_x_max, RefBcFn fn_y_min, RefBcFn fn_y_max
 )
 {
     System system = get_new_system_struct();
@@ -105,6 +109,7 @@ int ref_run_2d(
     system.num_cells_x = nx;
     system.num_cells_y = ny;
     system.num_ghost_cells_side = g;
+    system.gravity = gravity;
     ErrorStatus e = system_init(&system);
     if (e.return_code != SUCCESS)
     {
@@ -125,6 +130,10 @@ int ref_run_2d(
     bcp.boundary_condition_x_max = bc_x_max;
     bcp.boundary_condition_y_min = bc_y_min;
     bcp.boundary_condition_y_max = bc_y_max;
+    bcp.set_boundary_condition_cartesian_2d_x_min = fn_x_min;
+    bcp.set_boundary_condition_cartesian_2d_x_max = fn_x_max;
+    bcp.set_boundary_condition_cartesian_2d_y_min = fn_y_min;
+    bcp.set_boundary_condition_cartesian_2d_y_max = fn_y_max;
 
     IntegratorParam ip = get_new_integrator_param();
     ip.integrator = (char *) integrator;
@@ -159,6 +168,24 @@ int ref_run_2d(
     *dt = st.dt;
     free_system_memory(&system);
     return finish(e, errbuf, errlen, max_steps >= 0);
+}
+
+int ref_run_2d(
+    int nx, int ny, int g,
+    double x_min, double x_max, double y_min, double y_max, double gamma,
+    const char *integrator, const char *riemann_solver, const char *slope_limiter,
+    const char *bc_x_min, const char *bc_x_max, const char *bc_y_min, const char *bc_y_max,
+    double cfl, double tf, long long max_steps,
+    double *rho, double *u, double *v, double *p,
+    double *mass, double *mom_x, double *mom_y, double *energy,
+    long long *num_steps, double *t, double *dt,
+    char *errbuf, int errlen
+)
+{
+    return ref_run_2d_ex(nx, ny, g, x_min, x_max, y_min, y_max, gamma, integrator, riemann_solver,
+                         slope_limiter, bc_x_min, bc_x_max, bc_y_min, bc_y_max, cfl, tf, max_steps,
+                         rho, u, v, p, mass, mom_x, mom_y, energy, num_steps, t, dt, errbuf, errlen,
+                         0.0, NULL, NULL, NULL, NULL);
 }
 
 /* Run a 1D Cartesian problem; arrays are padded to nx+2g. */

@@ -51,6 +51,9 @@ def cases_2d():
     p.max_steps = -1
     p.tf = 0.04
     out["four_quadrant_24_mm_tf0.04"] = p
+    # gravity source (the Rayleigh-Taylor example) and a custom side (the lid-driven cavity)
+    out["rayleigh_taylor_24x40_g3_30"] = P.rayleigh_taylor(24, 40, g=3, steps=30)
+    out["lid_cavity_32_g3_30"] = P.lid_driven_cavity(32, g=3, steps=30)
     return out
 
 

@@ -18,7 +18,8 @@ REL_L1_TOL = 1e-12
 def run_gpu(p, **kw):
     return H.run_2d(p.nx, p.ny, p.g, (p.x_min, p.x_max, p.y_min, p.y_max), p.gamma, p.W, p.U,
                     bc=p.bc, integrator=p.integrator, riemann_solver=p.riemann_solver,
-                    slope_limiter=p.slope_limiter, cfl=p.cfl, tf=p.tf, max_steps=p.max_steps, **kw)
+                    slope_limiter=p.slope_limiter, cfl=p.cfl, tf=p.tf, max_steps=p.max_steps,
+                    gravity=p.gravity, custom_bc=p.custom_bc, **kw)
 
 
 def assert_parity(p, gpu, ref, tol=REL_L1_TOL):
@@ -80,3 +81,81 @@ def test_run_to_tf(gpu_available, oracle_mod):
     gpu = run_gpu(p)
     assert ref.t == pytest.approx(0.05)
     assert_parity(p, gpu, ref)
+
+
+# ----------------------------------------------------------- gravity, custom sides
+
+GOLDEN = __import__("os").path.join(__import__("os").path.dirname(__import__("os").path.abspath(__file__)),
+                                     "golden")
+
+
+@pytest.mark.parametrize("integrator", ["muscl_hancock_2d", "godunov_first_order_2d"])
+def test_gravity_source_rayleigh_taylor(gpu_available, oracle_mod, integrator):
+    """The gravity source (RK4 kick after the step, src/source_term.c:185-259)
+    on the Rayleigh-Taylor example's set-up (G = 3, periodic x, reflective y)."""
+    O = oracle_mod
+    p = O.rayleigh_taylor(40, 64, g=3, steps=80)
+    p.integrator = integrator
+    gpu = run_gpu(p)
+    ref = O.load("oracle").run_2d(p)
+    l1 = assert_parity(p, gpu, ref)
+    assert np.all(l1 == 0.0), l1
+
+
+def test_custom_side_lid_cavity(gpu_available, oracle_mod):
+    """A custom side: the lid-driven cavity's top callback runs on the host
+    after every step and its ghost rows feed the next step."""
+    O = oracle_mod
+    p = O.lid_driven_cavity(48, g=3, steps=80)
+    gpu = run_gpu(p)
+    ref = O.load("oracle").run_2d(p)
+    # <= 1e-12 relative L1; the lid drives two-rarefaction faces, whose pow
+    # may differ from the CPU's by an ulp
+    assert_parity(p, gpu, ref)
+    # the lid rows hold the callback's velocity
+    assert np.all(gpu.W[1, p.g + p.ny:, :] == 10.0)
+
+
+@pytest.mark.parametrize("name", ["rayleigh_taylor_24x40_g3_30", "lid_cavity_32_g3_30"])
+def test_gravity_and_custom_against_reference_golden(gpu_available, name):
+    """Against the unmodified reference's outputs (committed fixtures)."""
+    import os
+    import sys
+    sys.path.insert(0, GOLDEN)
+    import make_golden as MG
+    p = MG.cases_2d()[name]
+    g = np.load(os.path.join(GOLDEN, f"{name}.npz"))
+    gpu = run_gpu(p)
+    assert gpu.code == 0, gpu.message
+    assert gpu.num_steps == int(g["num_steps"]) and gpu.t == float(g["t"])
+    import oracle as O
+    assert np.all(O.rel_l1(gpu.U, g["U"], p.g) <= REL_L1_TOL)
+    assert np.all(O.rel_l1(gpu.W, g["W"], p.g) <= REL_L1_TOL)
+
+
+def test_custom_side_session_in_chunks(gpu_available, oracle_mod):
+    """The device-resident session with a custom side, advanced in two calls."""
+    O = oracle_mod
+    p = O.lid_driven_cavity(40, g=3, steps=50)
+    with H.Solver2D(p.nx, p.ny, p.g, (p.x_min, p.x_max, p.y_min, p.y_max), p.gamma, p.W, p.U,
+                    bc=p.bc, slope_limiter=p.slope_limiter, cfl=p.cfl, custom_bc=p.custom_bc) as s:
+        s.advance(20)
+        st, _ = s.advance(30)
+        assert st.num_steps == 50
+        W, U = s.download()
+    ref = O.load("oracle").run_2d(p)
+    assert np.all(O.rel_l1(U, ref.U, p.g) <= REL_L1_TOL)
+    assert np.all(O.rel_l1(W, ref.W, p.g) <= REL_L1_TOL)
+
+
+def test_fp32_gravity_and_custom_rejection(gpu_available, oracle_mod):
+    O = oracle_mod
+    p = O.rayleigh_taylor(32, 48, g=3, steps=40)
+    r64 = run_gpu(p)
+    r32 = run_gpu(p, options=H.default_options(precision=H.PRECISION_FP32))
+    assert r32.code == 0, r32.message
+    l1 = O.rel_l1(r32.U, r64.U, p.g)
+    assert l1[0] < 1e-6 and l1[3] < 1e-6, l1     # mass and energy (the velocities start at 0)
+    q = O.lid_driven_cavity(16, g=3, steps=4)
+    r = run_gpu(q, options=H.default_options(precision=H.PRECISION_FP32))
+    assert r.code != 0 and "FP64" in r.message
