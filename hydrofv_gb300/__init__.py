@@ -96,7 +96,7 @@ class HydroGpuOptions(C.Structure):
     _fields_ = [
         ("device", C.c_int), ("max_steps", C.c_int64), ("precision", C.c_int),
         ("chunk_steps", C.c_int), ("use_graph", C.c_int), ("block_threads", C.c_int),
-        ("chunk_rows", C.c_int), ("autotune", C.c_int),
+        ("chunk_rows", C.c_int), ("autotune", C.c_int), ("sync_snapshots", C.c_int),
     ]
 
 

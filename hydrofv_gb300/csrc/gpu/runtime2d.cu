@@ -27,6 +27,7 @@
 #include <map>
 #include <mutex>
 #include <new>
+#include <thread>
 #include <tuple>
 
 #include "gpu_bridge.h"
@@ -86,6 +87,13 @@ struct HydroRun2D {
     Mh2dArgs<float> args32{};
     cudaGraphExec_t graph = nullptr;
     cudaEvent_t ev[6] = {};
+    /* asynchronous snapshots: D2H on a side stream, the writer on a host thread */
+    cudaStream_t side = nullptr;
+    cudaEvent_t snap_ready = nullptr;    /* materialized state complete (main stream) */
+    cudaEvent_t snap_copied = nullptr;   /* host copy complete (side stream) */
+    std::thread writer;
+    int writer_rc = 0;
+    long long snapshots_async = 0;
     HydroHostBcFn host_bc = nullptr;  /* custom sides: host boundary routine after every step */
     void *host_bc_ctx = nullptr;
     int custom_mask = 0;              /* bit s: side s (x_min, x_max, y_min, y_max) is custom */
@@ -592,6 +600,81 @@ static int enqueue_steps(HydroRun2D *run, long long k, HydroRunOutcome *oc)
     return 0;
 }
 
+/* Wait for the snapshot writer thread; its callback status becomes the outcome. */
+static int join_writer(HydroRun2D *run, HydroRunOutcome *oc)
+{
+    if (run->writer.joinable()) run->writer.join();
+    if (run->writer_rc != 0) {
+        oc->kind = HYDRO_RUN_CALLBACK_ERROR;
+        oc->code = run->writer_rc;
+        run->writer_rc = 0;
+        return -1;
+    }
+    return 0;
+}
+
+/*
+ * Snapshot without stopping the stream: the materialized state (and, for
+ * the FP32 form, its FP64 conversion) is produced on the main stream; a
+ * side stream waits for it and copies it to pinned host memory; a host
+ * thread waits for that copy and runs the writer while the main stream
+ * steps on.  One snapshot is in flight at a time (the next one, and the
+ * end of the run, join the writer first), so the snapshot buffers and the
+ * writer's state are never shared.
+ */
+static int snapshot_async(HydroRun2D *run, HydroSnapshotFn snap, void *ctx, HydroRunOutcome *oc)
+{
+    if (join_writer(run, oc)) return -1;
+    if (!run->side) {
+        CK(cudaStreamCreateWithFlags(&run->side, cudaStreamNonBlocking), "cudaStreamCreate(snapshots)");
+        CK(cudaEventCreateWithFlags(&run->snap_ready, cudaEventDisableTiming), "cudaEventCreate");
+        CK(cudaEventCreateWithFlags(&run->snap_copied, cudaEventDisableTiming), "cudaEventCreate");
+    }
+    if (!run->snap_h)
+        CK(cudaMallocHost(&run->snap_h, 4 * run->ncell * sizeof(double)), "cudaMallocHost(snapshot)");
+    const int buf = (int) (run->ctrl_h->num_steps & 1);
+    const void *src[4];
+    if (run->fp32) {
+        float *out[4];
+        for (int q = 0; q < 4; q++) out[q] = static_cast<float *>(run->snap_d[q]);
+        CK(mh2d_launch_materialize<float>(run->args32, buf, out, run->stream), "materialize kernel");
+        for (int q = 0; q < 4; q++) {
+            double *st = run->stage_d + q * run->ncell;
+            CK(convert_f32_to_f64(out[q], st, (long long) run->ncell, run->stream), "convert");
+            src[q] = st;
+        }
+        run->kernel_launches += 4;
+    } else {
+        double *out[4];
+        for (int q = 0; q < 4; q++) out[q] = static_cast<double *>(run->snap_d[q]);
+        CK(mh2d_launch_materialize<double>(run->args, buf, out, run->stream), "materialize kernel");
+        for (int q = 0; q < 4; q++) src[q] = out[q];
+    }
+    run->kernel_launches++;
+    CK(cudaEventRecord(run->snap_ready, run->stream), "cudaEventRecord");
+    CK(cudaStreamWaitEvent(run->side, run->snap_ready, 0), "cudaStreamWaitEvent");
+    const size_t bytes = run->ncell * sizeof(double);
+    for (int q = 0; q < 4; q++)
+        CK(cudaMemcpyAsync(run->snap_h + q * run->ncell, src[q], bytes, cudaMemcpyDeviceToHost, run->side),
+           "D2H snapshot");
+    CK(cudaEventRecord(run->snap_copied, run->side), "cudaEventRecord");
+    const long long steps = run->ctrl_h->num_steps;
+    const double t = run->ctrl_h->t, dt = run->ctrl_h->dt;
+    const int device = run->device;
+    run->snapshots_async++;
+    run->writer = std::thread([run, snap, ctx, steps, t, dt, device]() {
+        cudaSetDevice(device);
+        if (cudaEventSynchronize(run->snap_copied) != cudaSuccess) {
+            run->writer_rc = -1;
+            return;
+        }
+        double *Wh[4];
+        for (int q = 0; q < 4; q++) Wh[q] = run->snap_h + q * run->ncell;
+        run->writer_rc = snap(ctx, Wh, steps, t, dt);
+    });
+    return 0;
+}
+
 static int materialize_to_host(HydroRun2D *run, double *const W[4], HydroRunOutcome *oc)
 {
     const int buf = (int) (run->ctrl_h->num_steps & 1);
@@ -671,7 +754,14 @@ extern "C" int hydro_run2d_advance(HydroRun2D *run, HydroSnapshotFn snap, void *
             return -1;
         }
         if (c->snapshot_due) {
-            if (snap) {
+            if (snap && !run->opt.sync_snapshots) {
+                if (snapshot_async(run, snap, ctx, oc)) {
+                    fill_outcome(run, oc);
+                    run->step_ms += elapsed;
+                    if (step_ms) *step_ms = elapsed;
+                    return -1;
+                }
+            } else if (snap) {
                 if (!run->snap_h) {
                     CK(cudaMallocHost(&run->snap_h, 4 * run->ncell * sizeof(double)), "cudaMallocHost(snapshot)");
                 }
@@ -698,6 +788,7 @@ extern "C" int hydro_run2d_advance(HydroRun2D *run, HydroSnapshotFn snap, void *
     run->step_ms += elapsed;
     if (step_ms) *step_ms = elapsed;
     fill_outcome(run, oc);
+    if (join_writer(run, oc)) return -1;
     return 0;
 }
 
@@ -706,6 +797,7 @@ extern "C" int hydro_run2d_download(HydroRun2D *run, double *const W[4], double 
 {
     memset(oc, 0, sizeof *oc);
     CK(cudaSetDevice(run->device), "cudaSetDevice");
+    if (run->writer.joinable()) run->writer.join();   /* the snapshot buffers are reused */
     const int buf = (int) (run->ctrl_h->num_steps & 1);
     const size_t bytes = run->ncell * sizeof(double);
     CK(cudaEventRecord(run->ev[4], run->stream), "cudaEventRecord");
@@ -755,7 +847,14 @@ extern "C" void hydro_run2d_destroy(HydroRun2D *run)
 {
     if (!run) return;
     cudaSetDevice(run->device);
+    if (run->writer.joinable()) run->writer.join();
     if (run->stream) cudaStreamSynchronize(run->stream);
+    if (run->side) {
+        cudaStreamSynchronize(run->side);
+        cudaStreamDestroy(run->side);
+    }
+    if (run->snap_ready) cudaEventDestroy(run->snap_ready);
+    if (run->snap_copied) cudaEventDestroy(run->snap_copied);
     if (run->graph) cudaGraphExecDestroy(run->graph);
     for (auto &e : run->ev)
         if (e) cudaEventDestroy(e);

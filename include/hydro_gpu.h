@@ -42,6 +42,12 @@ typedef struct HydroGpuOptions
                                shapes and persistent grid sizes on the actual
                                state (then rewind) and keep the fastest; cached
                                per shape for the process */
+    int sync_snapshots;     /* 0 (default, 2D): a snapshot is copied to the host on a
+                               side stream and written by a host thread while the
+                               steps go on; a write error is reported at the next
+                               snapshot or at the end of the run.  1: stepping
+                               waits for each write (the reference's behaviour:
+                               a failed write stops the run at that step). */
 } HydroGpuOptions;
 
 typedef struct HydroGpuStats
