@@ -356,6 +356,63 @@ def run_adjoint(args, H, device, ws, rank) -> None:
     print(json.dumps(line))
 
 
+def run_snapshots(args, H, device, ws, rank) -> None:
+    """Snapshot overlap: the config-2 shear layer through the drop-in call with
+    a snapshot every ~10 steps, written synchronously (stepping waits for each
+    file) and asynchronously (side-stream copy, host-thread writer).  Wall
+    clock of the whole call; the files are identical."""
+    import shutil
+    import tempfile
+    from hydrofv_gb300.problems import shear_layer
+    side = args.size
+    p = shear_layer(side, steps=-1)
+    cells = p.nx * p.ny
+    # dt of the first steps (CFL 0.8 after the 10 shrunk steps) sets the interval
+    with H.Solver2D(p.nx, p.ny, p.g, (0, 1, 0, 1), p.gamma, p.W, p.U, bc=p.bc,
+                    slope_limiter=p.slope_limiter, cfl=p.cfl,
+                    options=H.default_options(device=device)) as s:
+        st, _ = s.advance(20)
+        dt = st.dt
+    steps = args.steps
+    tf = st.t + (steps - 20) * dt
+    interval = tf / max(1, steps // 10)
+    res = {}
+    root = tempfile.mkdtemp(prefix="hydro_snap_", dir=os.environ.get("HYDRO_SNAPSHOT_DIR", None))
+    try:
+        for name, sync in (("sync", 1), ("async", 0)):
+            out = os.path.join(root, name) + "/"
+            os.makedirs(out, exist_ok=True)
+            t0 = time.perf_counter()
+            r = H.run_2d(p.nx, p.ny, p.g, (0, 1, 0, 1), p.gamma, p.W, p.U, bc=p.bc,
+                         slope_limiter=p.slope_limiter, cfl=p.cfl, tf=tf, max_steps=-1,
+                         options=H.default_options(device=device, sync_snapshots=sync),
+                         storing={"interval": interval, "output_dir": out, "store_initial": False})
+            wall = time.perf_counter() - t0
+            assert r.code == 0, r.message
+            files = sorted(os.listdir(out))
+            res[name] = {"seconds": wall, "steps": r.num_steps, "snapshots": len(files),
+                         "cell_updates_per_s": cells * r.num_steps / wall,
+                         "bytes_per_snapshot": os.path.getsize(out + files[0]) if files else 0}
+        same = all(open(os.path.join(root, "sync", f), "rb").read() == open(os.path.join(root, "async", f), "rb").read()
+                   for f in sorted(os.listdir(os.path.join(root, "sync"))))
+    finally:
+        shutil.rmtree(root, ignore_errors=True)
+    if rank != 0:
+        return
+    line = {
+        "metric": "2D MUSCL-HLLC cell-updates/s with snapshots (drop-in call, wall clock)",
+        "value": res["async"]["cell_updates_per_s"], "unit": "cell-updates/s", "n_gpus": ws,
+        "steps": res["async"]["steps"], "warmup": 0, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded shear layer)",
+        "config": {"workload": f"snapshots_shear_layer_{side}x{side}_fp64", "snapshot_interval": interval,
+                   "tf": tf},
+        "sync": res["sync"], "async": res["async"],
+        "speedup_async_vs_sync": res["sync"]["seconds"] / res["async"]["seconds"],
+        "files_identical": same,
+    }
+    print(json.dumps(line))
+
+
 def main() -> None:
     global N_SIDE, WORKLOAD
     ap = argparse.ArgumentParser()
@@ -369,7 +426,7 @@ def main() -> None:
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"],
                     help="state precision of the timed path (fp64 is the drop-in)")
     ap.add_argument("--workload", default="shear_layer",
-                    choices=["shear_layer", "point_blast", "ensemble", "adjoint"],
+                    choices=["shear_layer", "point_blast", "ensemble", "adjoint", "snapshots"],
                     help="shear_layer: MC, periodic, CFL 0.8; point_blast: Van Leer, reflective, "
                          "CFL 0.4; ensemble: 256 four-quadrant problems, side log-uniform in "
                          "[128, 1024], minmod, transmissive, one launch per step for all")
@@ -406,6 +463,9 @@ def main() -> None:
         return
     if args.workload == "adjoint":
         run_adjoint(args, H, local, ws, rank)
+        return
+    if args.workload == "snapshots":
+        run_snapshots(args, H, local, ws, rank)
         return
 
     device = local
