@@ -385,10 +385,12 @@ def run_2d(nx: int, ny: int, g: int, bounds, gamma: float, W: np.ndarray, U: np.
 def run_1d(nx: int, g: int, bounds, gamma: float, W: np.ndarray, U: np.ndarray,
            bc=("transmissive", "transmissive"), integrator="godunov_first_order_1d",
            riemann_solver="riemann_solver_exact", slope_limiter="minmod", cfl=0.9, tf=0.2,
-           max_steps=-1, options: HydroGpuOptions | None = None) -> RunResult:
-    """Run a 1D Cartesian problem (W, U: (3, nx+2g))."""
+           max_steps=-1, options: HydroGpuOptions | None = None,
+           coord_sys: str = "cartesian_1d") -> RunResult:
+    """Run a 1D problem (W, U: (3, nx+2g)) on a cartesian_1d, cylindrical_1d
+    or spherical_1d grid."""
     lib = library()
-    h = _SystemHandle(lib, "cartesian_1d", nx, 0, g, bounds, gamma)
+    h = _SystemHandle(lib, coord_sys, nx, 0, g, bounds, gamma)
     try:
         for dst, src in zip(h.fields(W1), W):
             dst[:] = src

@@ -126,11 +126,15 @@ void hydro_adj2d_destroy(HydroAdj2D *a);
 typedef struct HydroGrid1D
 {
     int nx, g;
-    double gamma, tol, dx, area, vol;
+    double gamma, tol, dx;
+    const double *area;           /* System.surface_area_x_ (nx + 2G + 1 entries) */
+    const double *vol;            /* System.volume_ (nx + 2G) */
+    const double *mid;            /* System.mid_points_x_ (nx + 2G) */
+    double alpha;                 /* geometry source: 0 Cartesian, 1 cylindrical, 2 spherical */
     int bc[2];
     int limiter;
     int riemann_solver;           /* RIEMANN_SOLVER_* */
-    int integrator;               /* INTEGRATOR_GODUNOV_FIRST_ORDER_1D or INTEGRATOR_MUSCL_HANCOCK_1D */
+    int integrator;               /* INTEGRATOR_{RANDOM_CHOICE,GODUNOV_FIRST_ORDER,MUSCL_HANCOCK}_1D */
 } HydroGrid1D;
 
 /* Whole 1D run in one launch (W, U: padded host arrays, in/out). */

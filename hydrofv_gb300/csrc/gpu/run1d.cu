@@ -1,12 +1,20 @@
 /*
- * run1d.cu -- 1D Cartesian integrators in one persistent CTA.
+ * run1d.cu -- 1D integrators (Cartesian, cylindrical, spherical) in one
+ * persistent CTA.
  *
  * Replaces the time loops of godunov_first_order_1d
- * (src/integrator_godunov_first_order.c:26-261) and muscl_hancock_1d
- * (src/integrator_muscl_hancock.c:26-383) with their exact / HLLC flux
+ * (src/integrator_godunov_first_order.c:26-261), muscl_hancock_1d
+ * (src/integrator_muscl_hancock.c:26-383) and random_choice_1d
+ * (src/integrator_random_choice_1d.c:28-290) with their exact / HLLC flux
  * (src/riemann_solver.c:47-97), get_time_step_1d (src/utils.c:28-53),
- * convert_conserved_to_primitive_1d (src/system.c:735-761) and
- * set_boundary_condition_1d (src/boundary.c:411-511).
+ * convert_conserved_to_primitive_1d (src/system.c:735-761),
+ * set_boundary_condition_1d (src/boundary.c:411-511) and the cylindrical /
+ * spherical geometry source (src/source_term.c:14-183).
+ *
+ * Geometry: face areas and cell volumes are per cell, as system_init sets
+ * them (src/system.c:365-529).  As in the reference, the flux through face i
+ * updates cell i-1 with surface_area_x[i-1] and cell i with surface_area_x[i]
+ * (src/integrator_godunov_first_order.c:182-192).
  *
  * 1D problems are small (the Sod tube of the benchmark configurations has
  * 1000 cells), so the whole run is one launch of one CTA of 1024 threads:
@@ -52,6 +60,9 @@ struct Run1dArgs {
     double *F[3];          /* face fluxes, index = face (= right cell) */
     double *Lf[3];         /* MUSCL interface states (left of face i at [i]) */
     double *Rf[3];         /* (right of face i at [i]) */
+    const double *area;    /* surface_area_x (per cell index) */
+    const double *vol;     /* volume */
+    const double *mid;     /* mid_points_x */
     HydroStepControl *ctrl;
     HydroStepParams sp;
     GasConst<double> gas;
@@ -59,9 +70,37 @@ struct Run1dArgs {
     int bc[2];
     int limiter;
     int solver;            /* RIEMANN_SOLVER_EXACT (1) or _HLLC (2) */
-    int muscl;             /* 0: Godunov first order, 1: MUSCL-Hancock */
-    double dx, area, vol;
+    int scheme;            /* 0: Godunov first order, 1: MUSCL-Hancock, 2: random choice */
+    double dx;
+    double alpha;          /* 0: Cartesian; 1 cylindrical, 2 spherical (geometry source) */
 };
+
+/* src/integrator_random_choice_1d.c:28-43: base-5 van der Corput sequence
+ * with digit scrambling a -> 3a mod 5. */
+__device__ double van_der_corput(long long n)
+{
+    double result = 0;
+    const int base = 5;
+    double bk = 1.0 / (double) base;
+    while (n > 0) {
+        const int a_i = (int) (n % base);
+        const int A_i = (3 * a_i) % 5;
+        result += A_i * bk;
+        n /= base;
+        bk /= (double) base;
+    }
+    return result;
+}
+
+/* src/source_term.c:25-39 */
+__device__ __forceinline__ void geometry_rates(double pf, double gm1, double rho, double sm, double se,
+                                               double &dm, double &dmom, double &de)
+{
+    const double p = gm1 * (se - 0.5 * sm * sm / rho);
+    dm = pf * sm;
+    dmom = pf * sm * sm / rho;
+    de = pf * sm * (se + p) / rho;
+}
 
 __device__ int face_flux(const Run1dArgs &a, double rl, double ul, double pl, double rr,
                          double ur, double pr, double F[3])
@@ -90,6 +129,41 @@ __device__ double block_max(double v, double *red)
     const double r = red[0];
     __syncthreads();
     return r;
+}
+
+/* All-cell U -> W (src/system.c:735-761). */
+__device__ void convert_all(const Run1dArgs &a, double *const *U, double *const *W, int ntot)
+{
+    for (int i = threadIdx.x; i < ntot; i += kThreads) {
+        const double m = U[0][i];
+        const double vol = a.vol[i];
+        const double rho = m / vol;
+        const double u = U[1][i] / m;
+        W[0][i] = rho;
+        W[1][i] = u;
+        W[2][i] = a.gas.gm1 * (U[2][i] - 0.5 * m * u * u) / vol;
+    }
+}
+
+/* Ghost fill (src/boundary.c:411-511). */
+__device__ void ghost_fill(const Run1dArgs &a, double *const *W, int g, int n)
+{
+    for (int k = threadIdx.x; k < g; k += kThreads) {
+        for (int side = 0; side < 2; side++) {
+            const int f = a.bc[side];
+            if (f == BC_NONE || (f == BC_PERIODIC && side == 0)) continue;
+            if (f == BC_PERIODIC) {
+                for (int q = 0; q < 3; q++) W[q][g + n + k] = W[q][g + k];
+                for (int q = 0; q < 3; q++) W[q][g - 1 - k] = W[q][g + n - 1 - k];
+                continue;
+            }
+            const int dst = side == 0 ? g - 1 - k : g + n + k;
+            const int src = side == 0 ? g + k : g + n - 1 - k;
+            W[0][dst] = W[0][src];
+            W[1][dst] = (f == BC_REFLECTIVE) ? -W[1][src] : W[1][src];
+            W[2][dst] = W[2][src];
+        }
+    }
 }
 
 __global__ void __launch_bounds__(kThreads) run1d_kernel(const Run1dArgs a)
@@ -131,10 +205,10 @@ __global__ void __launch_bounds__(kThreads) run1d_kernel(const Run1dArgs a)
         __syncthreads();
 
         /* ---- interface states (MUSCL-Hancock, :159-246) ---- */
-        if (a.muscl) {
-            const double dtA = dt * a.area / a.vol;
+        if (a.scheme == 1) {
             for (int i = tid; i < n + 2; i += kThreads) {
                 const int k = g + i - 1;
+                const double dtA = dt * a.area[k] / a.vol[k];
                 const double rho = W[0][k], u = W[1][k], p = W[2][k];
                 const double as = sound_speed(a.gas, rho, p);
                 double d[3];
@@ -151,68 +225,120 @@ __global__ void __launch_bounds__(kThreads) run1d_kernel(const Run1dArgs a)
             __syncthreads();
         }
 
-        /* ---- face fluxes: face i between cells i-1 and i, i in [g, g+n] ---- */
-        for (int i = g + tid; i <= g + n; i += kThreads) {
-            double F[3] = { 0.0, 0.0, 0.0 };
-            int rc;
-            if (a.muscl)
-                rc = face_flux(a, a.Lf[0][i], a.Lf[1][i], a.Lf[2][i], a.Rf[0][i], a.Rf[1][i],
-                               a.Rf[2][i], F);
-            else
-                rc = face_flux(a, W[0][i - 1], W[1][i - 1], W[2][i - 1], W[0][i], W[1][i], W[2][i], F);
-            if (rc != DEV_OK && !a.muscl) atomicCAS(&s_err, 0, rc);
-            for (int q = 0; q < 3; q++) a.F[q][i] = F[q];
-        }
-        __syncthreads();
-        if (s_err) {
-            if (tid == 0) {
-                ctrl->dt = dt;
-                ctrl->error_code = s_err;
-                ctrl->active = 0;
+        if (a.scheme == 2) {
+            /* ---- random choice (src/integrator_random_choice_1d.c:157-237): the
+             * exact solution of the left or right Riemann problem of each cell,
+             * sampled at theta dx / dt or (theta - 1) dx / dt, from a copy of W ---- */
+            const double theta = van_der_corput(ns + 1);
+            for (int i = tid; i < ntot; i += kThreads)
+                for (int q = 0; q < 3; q++) a.Lf[q][i] = W[q][i];
+            __syncthreads();
+            double *const *T = a.Lf;
+            for (int i = g + tid; i <= g + n; i += kThreads) {
+                const bool left = theta <= 0.5;
+                const int l = left ? i - 1 : i, r = left ? i : i + 1;
+                const double speed = left ? theta * a.dx / dt : (theta - 1.0) * a.dx / dt;
+                double o[3];
+                const int rc = exact_solve_1d(a.gas, T[0][l], T[1][l], T[2][l], T[0][r], T[1][r], T[2][r],
+                                              speed, o);
+                if (rc != DEV_OK) atomicCAS(&s_err, 0, rc);
+                W[0][i] = o[0];
+                W[1][i] = o[1];
+                W[2][i] = o[2];
             }
-            return;
-        }
-
-        /* ---- gather update in the serial order ---- */
-        for (int c = g - 1 + tid; c <= g + n; c += kThreads) {
-            for (int q = 0; q < 3; q++) {
-                double v = U[q][c];
-                if (c >= g) v = v + (a.F[q][c] * dt) * a.area;          /* face c: c is its right cell */
-                if (c + 1 <= g + n) v = v - (a.F[q][c + 1] * dt) * a.area; /* face c+1: c is its left cell */
-                U[q][c] = v;
-            }
-        }
-        __syncthreads();
-
-        /* ---- all-cell conversion (src/system.c:735-761) ---- */
-        for (int i = tid; i < ntot; i += kThreads) {
-            const double m = U[0][i];
-            const double rho = m / a.vol;
-            const double u = U[1][i] / m;
-            W[0][i] = rho;
-            W[1][i] = u;
-            W[2][i] = a.gas.gm1 * (U[2][i] - 0.5 * m * u * u) / a.vol;
-        }
-        __syncthreads();
-
-        /* ---- ghost fill (src/boundary.c:411-511) ---- */
-        for (int k = tid; k < g; k += kThreads) {
-            for (int side = 0; side < 2; side++) {
-                const int f = a.bc[side];
-                if (f == BC_NONE || (f == BC_PERIODIC && side == 0)) continue;
-                if (f == BC_PERIODIC) {
-                    for (int q = 0; q < 3; q++) W[q][g + n + k] = W[q][g + k];
-                    for (int q = 0; q < 3; q++) W[q][g - 1 - k] = W[q][g + n - 1 - k];
-                    continue;
+            __syncthreads();
+            if (s_err) {
+                /* the state from before the failing step */
+                for (int i = tid; i < ntot; i += kThreads)
+                    for (int q = 0; q < 3; q++) W[q][i] = T[q][i];
+                __syncthreads();
+                if (tid == 0) {
+                    ctrl->dt = dt;
+                    ctrl->error_code = s_err;
+                    ctrl->active = 0;
                 }
-                const int dst = side == 0 ? g - 1 - k : g + n + k;
-                const int src = side == 0 ? g + k : g + n - 1 - k;
-                W[0][dst] = W[0][src];
-                W[1][dst] = (f == BC_REFLECTIVE) ? -W[1][src] : W[1][src];
-                W[2][dst] = W[2][src];
+                return;
             }
+            ghost_fill(a, W, g, n);
+            __syncthreads();
+            /* all-cell W -> U (src/system.c:866-883) */
+            for (int i = tid; i < ntot; i += kThreads) {
+                const double rho = W[0][i], u = W[1][i], p = W[2][i], vol = a.vol[i];
+                const double m = rho * vol;
+                U[0][i] = m;
+                U[1][i] = m * u;
+                U[2][i] = vol * (0.5 * rho * u * u + p / a.gas.gm1);
+            }
+            __syncthreads();
+        } else {
+            /* ---- face fluxes: face i between cells i-1 and i, i in [g, g+n] ---- */
+            for (int i = g + tid; i <= g + n; i += kThreads) {
+                double F[3] = { 0.0, 0.0, 0.0 };
+                int rc;
+                if (a.scheme == 1)
+                    rc = face_flux(a, a.Lf[0][i], a.Lf[1][i], a.Lf[2][i], a.Rf[0][i], a.Rf[1][i],
+                                   a.Rf[2][i], F);
+                else
+                    rc = face_flux(a, W[0][i - 1], W[1][i - 1], W[2][i - 1], W[0][i], W[1][i], W[2][i], F);
+                if (rc != DEV_OK && a.scheme == 0) atomicCAS(&s_err, 0, rc);
+                for (int q = 0; q < 3; q++) a.F[q][i] = F[q];
+            }
+            __syncthreads();
+            if (s_err) {
+                if (tid == 0) {
+                    ctrl->dt = dt;
+                    ctrl->error_code = s_err;
+                    ctrl->active = 0;
+                }
+                return;
+            }
+
+            /* ---- gather update in the serial order ---- */
+            for (int c = g - 1 + tid; c <= g + n; c += kThreads) {
+                const double A = a.area[c];
+                for (int q = 0; q < 3; q++) {
+                    double v = U[q][c];
+                    if (c >= g) v = v + (a.F[q][c] * dt) * A;          /* face c: c is its right cell */
+                    if (c + 1 <= g + n) v = v - (a.F[q][c + 1] * dt) * A; /* face c+1: c is its left cell */
+                    U[q][c] = v;
+                }
+            }
+            __syncthreads();
+            convert_all(a, U, W, ntot);
+            __syncthreads();
+            ghost_fill(a, W, g, n);
+            __syncthreads();
         }
-        __syncthreads();
+
+        /* ---- cylindrical / spherical source, RK4 (src/source_term.c:45-183) ---- */
+        if (a.alpha != 0.0) {
+            const double gm1 = a.gas.gm1;
+            for (int i = g + tid; i < g + n; i += kThreads) {
+                const double vol = a.vol[i];
+                const double m = U[0][i], mom = U[1][i], E = U[2][i], rho = W[0][i];
+                const double pf = -a.alpha * vol / a.mid[i];
+                double k1m, k1p, k1e, k2m, k2p, k2e, k3m, k3p, k3e, k4m, k4p, k4e;
+                geometry_rates(pf, gm1, rho, mom / vol, E / vol, k1m, k1p, k1e);
+                double tm = m + 0.5 * dt * k1m, tp = mom + 0.5 * dt * k1p, te = E + 0.5 * dt * k1e;
+                geometry_rates(pf, gm1, tm / vol, tp / vol, te / vol, k2m, k2p, k2e);
+                tm = m + 0.5 * dt * k2m;
+                tp = mom + 0.5 * dt * k2p;
+                te = E + 0.5 * dt * k2e;
+                geometry_rates(pf, gm1, tm / vol, tp / vol, te / vol, k3m, k3p, k3e);
+                tm = m + dt * k3m;
+                tp = mom + dt * k3p;
+                te = E + dt * k3e;
+                geometry_rates(pf, gm1, tm / vol, tp / vol, te / vol, k4m, k4p, k4e);
+                U[0][i] = m + dt * (k1m + 2.0 * k2m + 2.0 * k3m + k4m) / 6.0;
+                U[1][i] = mom + dt * (k1p + 2.0 * k2p + 2.0 * k3p + k4p) / 6.0;
+                U[2][i] = E + dt * (k1e + 2.0 * k2e + 2.0 * k3e + k4e) / 6.0;
+            }
+            __syncthreads();
+            convert_all(a, U, W, ntot);
+            __syncthreads();
+            ghost_fill(a, W, g, n);
+            __syncthreads();
+        }
 
         /* ---- clock (thread 0 only; everyone re-reads after the barrier) ---- */
         if (tid == 0) {
@@ -272,7 +398,7 @@ extern "C" int hydro_run1d(const HydroGrid1D *grid, double *const Wh[3], double 
     CK1(cudaSetDevice(opt->device), "cudaSetDevice");
     CK1(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "cudaStreamCreate");
     for (auto &e : ev) CK1(cudaEventCreate(&e), "cudaEventCreate");
-    CK1(cudaMalloc(&slab, 15 * bytes), "cudaMalloc(state)");
+    CK1(cudaMalloc(&slab, 18 * bytes + sizeof(double)), "cudaMalloc(state)");
     CK1(cudaMalloc(&ctrl_d, sizeof(HydroStepControl)), "cudaMalloc(control)");
     for (int q = 0; q < 3; q++) {
         a.W[q] = slab + q * ntot;
@@ -280,6 +406,15 @@ extern "C" int hydro_run1d(const HydroGrid1D *grid, double *const Wh[3], double 
         a.F[q] = slab + (6 + q) * ntot;
         a.Lf[q] = slab + (9 + q) * ntot;
         a.Rf[q] = slab + (12 + q) * ntot;
+    }
+    {
+        double *geo = slab + 15 * ntot;   /* area (ntot + 1), volume, mid points */
+        CK1(cudaMemcpyAsync(geo, grid->area, bytes + sizeof(double), cudaMemcpyHostToDevice, s), "H2D area");
+        CK1(cudaMemcpyAsync(geo + ntot + 1, grid->vol, bytes, cudaMemcpyHostToDevice, s), "H2D volume");
+        CK1(cudaMemcpyAsync(geo + 2 * ntot + 1, grid->mid, bytes, cudaMemcpyHostToDevice, s), "H2D mid points");
+        a.area = geo;
+        a.vol = geo + ntot + 1;
+        a.mid = geo + 2 * ntot + 1;
     }
     a.ctrl = ctrl_d;
     a.sp = *sp;
@@ -290,10 +425,10 @@ extern "C" int hydro_run1d(const HydroGrid1D *grid, double *const Wh[3], double 
     a.bc[1] = grid->bc[1];
     a.limiter = grid->limiter;
     a.solver = grid->riemann_solver;
-    a.muscl = grid->integrator == INTEGRATOR_MUSCL_HANCOCK_1D;
+    a.scheme = grid->integrator == INTEGRATOR_MUSCL_HANCOCK_1D ? 1
+             : grid->integrator == INTEGRATOR_RANDOM_CHOICE_1D ? 2 : 0;
     a.dx = grid->dx;
-    a.area = grid->area;
-    a.vol = grid->vol;
+    a.alpha = grid->alpha;
 
     CK1(cudaEventRecord(ev[0], s), "cudaEventRecord");
     for (int q = 0; q < 3; q++) {

@@ -369,11 +369,6 @@ static ErrorStatus run_1d(
                  "\"cylindrical_1d\" and \"spherical_1d\", got: \"%s\"", s->coord_sys);
         return WRAP_RAISE_ERROR(VALUE_ERROR, msg);
     }
-    if (cs != COORD_SYS_CARTESIAN_1D)
-    {
-        return WRAP_RAISE_ERROR(NOT_IMPLEMENTED_ERROR,
-                                "Cylindrical and spherical grids (geometric source term) are not available on the GPU path.");
-    }
     const int flags[2] = { bcp->boundary_condition_flag_x_min_, bcp->boundary_condition_flag_x_max_ };
     for (int k = 0; k < 2; k++)
     {
@@ -388,16 +383,15 @@ static ErrorStatus run_1d(
         return WRAP_RAISE_ERROR(NOT_IMPLEMENTED_ERROR, "Requested precision is not available for this integrator.");
     }
     const int g = s->num_ghost_cells_side;
-    const long long tx = s->num_cells_x + 2 * g;
-    if (!uniform(s->surface_area_x_, tx + 1) || !uniform(s->volume_, tx))
-    {
-        return WRAP_RAISE_ERROR(NOT_IMPLEMENTED_ERROR,
-                                "The GPU path needs uniform face areas and cell volumes (as system_init sets them).");
-    }
     if (s->num_cells_x < g)
     {
         return WRAP_RAISE_ERROR(NOT_IMPLEMENTED_ERROR,
                                 "The GPU path needs at least num_ghost_cells_side interior cells.");
+    }
+    if (ip->integrator_flag_ == INTEGRATOR_RANDOM_CHOICE_1D && g < 2)
+    {
+        /* the reference's random choice reads the cell beyond the last face (src/integrator_random_choice_1d.c:190) */
+        return WRAP_RAISE_ERROR(VALUE_ERROR, "random_choice_1d needs at least 2 ghost cells per side.");
     }
     HydroGrid1D grid;
     memset(&grid, 0, sizeof grid);
@@ -406,8 +400,10 @@ static ErrorStatus run_1d(
     grid.gamma = s->gamma;
     grid.tol = ip->tol;
     grid.dx = s->dx_;
-    grid.area = s->surface_area_x_[0];
-    grid.vol = s->volume_[0];
+    grid.area = s->surface_area_x_;
+    grid.vol = s->volume_;
+    grid.mid = s->mid_points_x_;
+    grid.alpha = (cs == COORD_SYS_CYLINDRICAL_1D) ? 1.0 : (cs == COORD_SYS_SPHERICAL_1D) ? 2.0 : 0.0;
     grid.bc[0] = flags[0];
     grid.bc[1] = flags[1];
     grid.limiter = ip->slope_limiter_flag_;
@@ -484,9 +480,8 @@ ErrorStatus random_choice_1d(
     SimulationStatus *__restrict status
 )
 {
-    (void) bcp; (void) system; (void) ip; (void) sp; (void) settings; (void) simp; (void) status;
-    return WRAP_RAISE_ERROR(NOT_IMPLEMENTED_ERROR,
-                            "random_choice_1d is not part of the GPU library (use godunov_first_order_1d).");
+    const HydroGpuOptions opt = process_options();
+    return run_1d(bcp, system, ip, sp, settings, simp, status, &opt, NULL);
 }
 
 /* ------------------------------------------------------- extension API */
@@ -521,6 +516,7 @@ ErrorStatus hydro_gpu_launch_simulation(
             return WRAP_TRACEBACK(run_2d(bcp, system, ip, sp, settings, simp, status, &opt, stats));
         case INTEGRATOR_GODUNOV_FIRST_ORDER_1D:
         case INTEGRATOR_MUSCL_HANCOCK_1D:
+        case INTEGRATOR_RANDOM_CHOICE_1D:
             return WRAP_TRACEBACK(run_1d(bcp, system, ip, sp, settings, simp, status, &opt, stats));
         default:
         {

@@ -83,6 +83,7 @@ class Problem1D:
     tf: float = 0.2
     max_steps: int = -1
     name: str = ""
+    coord_sys: str = "cartesian_1d"   # or "cylindrical_1d", "spherical_1d"
 
     def copy(self) -> "Problem1D":
         import copy
@@ -282,10 +283,46 @@ def random_problem_2d(nx: int, ny: int, seed: int, bc, limiter: str, steps: int,
                      tf=1e300, max_steps=steps, name=f"random_{nx}x{ny}_{seed}")
 
 
-def sod_1d(n: int = 1000, g: int = 2) -> Problem1D:
+def geometry_1d(x_min: float, x_max: float, n: int, g: int, coord_sys: str):
+    """(surface_area_x, volume, mid_points_x) of a 1D grid as system_init sets
+    them (src/system.c:318-356, :365-529): areas at the faces r = x_min + i dx
+    (2 pi r cylindrical, entry 0 unset there and 0 here; 4 pi r^2 spherical;
+    1 Cartesian), shell volumes, cell-centre mid points."""
+    tot = n + 2 * g
+    dx = (x_max - x_min) / tot
+    i = np.arange(tot + 1, dtype=np.float64)
+    r = x_min + i * dx
+    if coord_sys == "cartesian_1d":
+        area = np.ones(tot + 1)
+        vol = np.full(tot, dx)
+    elif coord_sys == "cylindrical_1d":
+        area = 2.0 * math.pi * r
+        area[0] = 0.0
+        vol = math.pi * (r[1:] * r[1:] - r[:-1] * r[:-1])
+    elif coord_sys == "spherical_1d":
+        area = 4.0 * math.pi * r * r
+        vol = (4.0 / 3.0) * math.pi * (r[1:] * r[1:] * r[1:] - r[:-1] * r[:-1] * r[:-1])
+    else:
+        raise ValueError(coord_sys)
+    mid = x_min + (np.arange(tot) + 0.5) * dx
+    return area, vol, mid
+
+
+def conserved_to_primitive_1d(U: np.ndarray, gamma: float, vol) -> np.ndarray:
+    """src/system.c:735-761."""
+    m, mom, E = U
+    W = np.empty_like(U)
+    W[0] = m / vol
+    W[1] = mom / m
+    W[2] = (gamma - 1.0) * (E - 0.5 * m * W[1] * W[1]) / vol
+    return W
+
+
+def sod_1d(n: int = 1000, g: int = 2, coord_sys: str = "cartesian_1d") -> Problem1D:
     """Sod shock tube as in examples/sod_shock_1d/sod_shock_1d.c:47-62: left
     (1, 0, 1) for x < 0.5, right (0.125, 0, 0.1), set over the padded range;
-    transmissive; Godunov first order + exact solver; CFL 0.9, tf = 0.2."""
+    transmissive; Godunov first order + exact solver; CFL 0.9, tf = 0.2.  On
+    cylindrical / spherical grids x is the radius."""
     gamma = 1.4
     x = mid_points(0.0, 1.0, n, g)
     left = x < 0.5
@@ -293,11 +330,44 @@ def sod_1d(n: int = 1000, g: int = 2) -> Problem1D:
     W[0] = np.where(left, 1.0, 0.125)
     W[1] = 0.0
     W[2] = np.where(left, 1.0, 0.1)
-    vol = 1.0 / (n + 2 * g)
+    vol = geometry_1d(0.0, 1.0, n, g, coord_sys)[1] if coord_sys != "cartesian_1d" else 1.0 / (n + 2 * g)
     U = primitive_to_conserved_1d(W, gamma, vol)
     return Problem1D(n, g, 0.0, 1.0, gamma, W, U, ("transmissive", "transmissive"),
                      "godunov_first_order_1d", "riemann_solver_exact", "minmod",
-                     cfl=0.9, tf=0.2, max_steps=-1, name=f"sod_{n}")
+                     cfl=0.9, tf=0.2, max_steps=-1, name=f"sod_{n}_{coord_sys}", coord_sys=coord_sys)
+
+
+def sedov_1d(n_total: int = 64, g: int = 2, coord_sys: str = "cylindrical_1d",
+             steps: int = -1) -> Problem1D:
+    """Sedov blast as in examples/sedov_blast_1d/sedov_blast_1d.c:20-105: [0, 1.2],
+    rho = 1, u = 0, p = 1e-5, reflective at r = 0 and transmissive outside; the
+    first 3 interior cells get the energy E_0 / 3 (E_0 = 0.0673185, 0.311357,
+    0.851072 for Cartesian, cylindrical, spherical) after W -> U, then U -> W
+    and the ghost fill.  MUSCL-Hancock + HLLC + MC, CFL 0.4, tf = 1."""
+    gamma = 1.4
+    n = n_total - 2 * g
+    area, vol, mid = geometry_1d(0.0, 1.2, n, g, coord_sys)
+    W = np.zeros((3, n_total))
+    W[0, g:g + n] = 1.0
+    W[1, g:g + n] = 0.0
+    W[2, g:g + n] = 1e-5
+    bc = ("reflective", "transmissive")
+
+    def fill(W):
+        W[0, g - 1 - np.arange(g)] = W[0, g + np.arange(g)]
+        W[1, g - 1 - np.arange(g)] = -W[1, g + np.arange(g)]
+        W[2, g - 1 - np.arange(g)] = W[2, g + np.arange(g)]
+        W[:, g + n + np.arange(g)] = W[:, g + n - 1 - np.arange(g)]
+
+    fill(W)
+    U = primitive_to_conserved_1d(W, gamma, vol)
+    E0 = {"cartesian_1d": 0.0673185, "cylindrical_1d": 0.311357, "spherical_1d": 0.851072}[coord_sys] / 3
+    U[2, g:g + 3] = E0
+    W = conserved_to_primitive_1d(U, gamma, vol)
+    fill(W)
+    return Problem1D(n, g, 0.0, 1.2, gamma, W, U, bc, "muscl_hancock_1d", "riemann_solver_hllc",
+                     "monotonized_central", cfl=0.4, tf=1.0, max_steps=steps,
+                     name=f"sedov_{n}_{coord_sys}", coord_sys=coord_sys)
 
 
 

@@ -968,10 +968,35 @@ int oracle_run_2d_ex(
 typedef struct
 {
     int nx, g;
-    double gamma, dx, A, vol, tol;
+    double gamma, dx, tol;
+    double *A, *V, *X;           /* surface_area_x (per cell index), volume, mid_points_x */
+    double alpha;                /* 0 Cartesian, 1 cylindrical, 2 spherical */
     int lim, solver, bc[2];
     double *W[3], *U[3];
 } Grid1;
+
+/* src/system.c:318-356, :365-529 for the 1D coordinate systems. */
+static void geometry_1d(Grid1 *G, double x_min, int coord)
+{
+    const int tot = G->nx + 2 * G->g;
+    const double dx = G->dx;
+    for (int i = 0; i < tot; i++) G->X[i] = x_min + (i + 0.5) * dx;
+    for (int i = 0; i < tot + 1; i++)
+    {
+        const double r = x_min + i * dx;
+        if (coord == 1) G->A[i] = 1.0;
+        else if (coord == 2) G->A[i] = (i == 0) ? 0.0 : 2.0 * M_PI * r;
+        else G->A[i] = 4.0 * M_PI * r * r;
+    }
+    for (int i = 0; i < tot; i++)
+    {
+        const double r_min = x_min + i * dx;
+        const double r_max = x_min + (i + 1) * dx;
+        if (coord == 1) G->V[i] = dx;
+        else if (coord == 2) G->V[i] = M_PI * (r_max * r_max - r_min * r_min);
+        else G->V[i] = (4.0 / 3.0) * M_PI * (r_max * r_max * r_max - r_min * r_min * r_min);
+    }
+}
 
 /* src/system.c:735-761 */
 static void conserved_to_primitive_1d(Grid1 *G)
@@ -979,9 +1004,21 @@ static void conserved_to_primitive_1d(Grid1 *G)
     for (int i = 0; i < G->nx + 2 * G->g; i++)
     {
         const double m = G->U[0][i], mx = G->U[1][i], E = G->U[2][i];
-        G->W[0][i] = m / G->vol;
+        G->W[0][i] = m / G->V[i];
         G->W[1][i] = mx / m;
-        G->W[2][i] = (G->gamma - 1.0) * (E - 0.5 * m * G->W[1][i] * G->W[1][i]) / G->vol;
+        G->W[2][i] = (G->gamma - 1.0) * (E - 0.5 * m * G->W[1][i] * G->W[1][i]) / G->V[i];
+    }
+}
+
+/* src/system.c:866-883 */
+static void primitive_to_conserved_1d(Grid1 *G)
+{
+    for (int i = 0; i < G->nx + 2 * G->g; i++)
+    {
+        const double rho = G->W[0][i], u = G->W[1][i], p = G->W[2][i], V = G->V[i];
+        G->U[0][i] = rho * V;
+        G->U[1][i] = G->U[0][i] * u;
+        G->U[2][i] = V * (0.5 * rho * u * u + p / (G->gamma - 1.0));
     }
 }
 
@@ -1030,7 +1067,9 @@ static int flux_1d(const Grid1 *G, double rl, double ul, double pl, double rr, d
     return hllc_1d(G->gamma, rl, ul, pl, rr, ur, pr, G->tol, F);
 }
 
-/* src/integrator_godunov_first_order.c:152-193 (serial order). */
+/* src/integrator_godunov_first_order.c:152-193 (serial order): the flux of
+ * face i updates cell i-1 with surface_area_x[i-1] and cell i with
+ * surface_area_x[i]. */
 static int godunov1d_step(Grid1 *G, double dt)
 {
     double **W = G->W, **U = G->U;
@@ -1042,8 +1081,8 @@ static int godunov1d_step(Grid1 *G, double dt)
         for (int q = 0; q < 3; q++)
         {
             const double d = F[q] * dt;
-            U[q][i - 1] -= d * G->A;
-            U[q][i] += d * G->A;
+            U[q][i - 1] -= d * G->A[i - 1];
+            U[q][i] += d * G->A[i];
         }
     }
     return OK;
@@ -1063,7 +1102,7 @@ static int mh1d_step(Grid1 *G, double dt)
     {
         const int k = g + i - 1;
         const double rho = W[0][k], u = W[1][k], p = W[2][k];
-        const double dtA = dt * G->A / G->vol;
+        const double dtA = dt * G->A[k] / G->V[k];
         const double a = sound_speed(G->gamma, rho, p);
         double d[3];
         for (int q = 0; q < 3; q++)
@@ -1085,12 +1124,114 @@ static int mh1d_step(Grid1 *G, double dt)
         for (int q = 0; q < 3; q++)
         {
             const double d = F[q] * dt;
-            U[q][k - 1] -= d * G->A;
-            U[q][k] += d * G->A;
+            U[q][k - 1] -= d * G->A[k - 1];
+            U[q][k] += d * G->A[k];
         }
     }
     free(L); free(R);
     return OK;
+}
+
+/* src/integrator_random_choice_1d.c:28-43 */
+static double van_der_corput(long long n)
+{
+    double result = 0;
+    const int base = 5;
+    double bk = 1.0 / (double) base;
+    while (n > 0)
+    {
+        const int a_i = (int) (n % base);
+        const int A_i = (3 * a_i) % 5;
+        result += A_i * bk;
+        n /= base;
+        bk /= (double) base;
+    }
+    return result;
+}
+
+/* src/riemann_solver_exact.c:332-469: the exact solution sampled at x/t = S. */
+static int exact_state_1d(double gamma, double rho_L, double u_L, double p_L,
+                          double rho_R, double u_R, double p_R, double tol, double S, double *o)
+{
+    const double a_L = (rho_L > 0.0) ? sound_speed(gamma, rho_L, p_L) : 0.0;
+    const double a_R = (rho_R > 0.0) ? sound_speed(gamma, rho_R, p_R) : 0.0;
+    double s[4];
+    if (rho_L <= 0.0 || rho_R <= 0.0 || ((a_L + a_R) * 2.0 / (gamma + 1.0)) <= (u_R - u_L))
+    {
+        solve_vacuum(gamma, rho_L, u_L, 0.0, p_L, a_L, rho_R, u_R, 0.0, p_R, a_R, S, s);
+        o[0] = s[0]; o[1] = s[1]; o[2] = s[3];
+        return OK;
+    }
+    double ps;
+    const int rc = exact_p_star(gamma, rho_L, u_L, p_L, a_L, rho_R, u_R, p_R, a_R, tol, &ps);
+    if (rc != OK) return rc;
+    const double us = 0.5 * (u_L + u_R) + 0.5 * (exact_fK(gamma, rho_R, p_R, a_R, ps)
+                                                - exact_fK(gamma, rho_L, p_L, a_L, ps));
+    exact_sample(gamma, rho_L, u_L, p_L, a_L, rho_R, u_R, p_R, a_R, us, ps, S, o);
+    return OK;
+}
+
+/* One random-choice step (src/integrator_random_choice_1d.c:157-237), then
+ * the boundary routine and W -> U. */
+static int random_choice_step(Grid1 *G, double dt, long long step_index)
+{
+    const int n = G->nx, g = G->g, tot = n + 2 * g;
+    double **W = G->W;
+    const double theta = van_der_corput(step_index + 1);
+    double *T = malloc(sizeof(double) * 3 * (size_t) tot);
+    if (!T) return MEMORY_ERROR;
+    for (int q = 0; q < 3; q++) memcpy(T + q * tot, W[q], sizeof(double) * (size_t) tot);
+    int err = OK;
+    for (int i = g; i < g + n + 1; i++)
+    {
+        const int left = theta <= 0.5;
+        const int l = left ? i - 1 : i, r = left ? i : i + 1;
+        const double speed = left ? theta * G->dx / dt : (theta - 1.0) * G->dx / dt;
+        double o[3];
+        const int rc = exact_state_1d(G->gamma, T[l], T[tot + l], T[2 * tot + l], T[r], T[tot + r], T[2 * tot + r],
+                                      G->tol, speed, o);
+        if (rc != OK) { err = rc; continue; }
+        W[0][i] = o[0]; W[1][i] = o[1]; W[2][i] = o[2];
+    }
+    free(T);
+    if (err != OK) return err;
+    boundary_1d(G);
+    primitive_to_conserved_1d(G);
+    return OK;
+}
+
+/* Cylindrical / spherical source, RK4 (src/source_term.c:14-183), then
+ * U -> W and the boundary routine. */
+static void rates(double pf, double gamma, double rho, double sm, double se, double *dm, double *dp, double *de)
+{
+    const double p = (gamma - 1) * (se - 0.5 * sm * sm / rho);
+    *dm = pf * sm;
+    *dp = pf * sm * sm / rho;
+    *de = pf * sm * (se + p) / rho;
+}
+
+static void geometry_source_1d(Grid1 *G, double dt)
+{
+    if (G->alpha == 0.0) return;
+    double **U = G->U;
+    for (int i = G->g; i < G->nx + G->g; i++)
+    {
+        const double V = G->V[i], m = U[0][i], mom = U[1][i], E = U[2][i], rho = G->W[0][i];
+        const double pf = -G->alpha * V / G->X[i];
+        double k1m, k1p, k1e, k2m, k2p, k2e, k3m, k3p, k3e, k4m, k4p, k4e;
+        rates(pf, G->gamma, rho, mom / V, E / V, &k1m, &k1p, &k1e);
+        double tm = m + 0.5 * dt * k1m, tp = mom + 0.5 * dt * k1p, te = E + 0.5 * dt * k1e;
+        rates(pf, G->gamma, tm / V, tp / V, te / V, &k2m, &k2p, &k2e);
+        tm = m + 0.5 * dt * k2m; tp = mom + 0.5 * dt * k2p; te = E + 0.5 * dt * k2e;
+        rates(pf, G->gamma, tm / V, tp / V, te / V, &k3m, &k3p, &k3e);
+        tm = m + dt * k3m; tp = mom + dt * k3p; te = E + dt * k3e;
+        rates(pf, G->gamma, tm / V, tp / V, te / V, &k4m, &k4p, &k4e);
+        U[0][i] += dt * (k1m + 2.0 * k2m + 2.0 * k3m + k4m) / 6.0;
+        U[1][i] += dt * (k1p + 2.0 * k2p + 2.0 * k3p + k4p) / 6.0;
+        U[2][i] += dt * (k1e + 2.0 * k2e + 2.0 * k3e + k4e) / 6.0;
+    }
+    conserved_to_primitive_1d(G);
+    boundary_1d(G);
 }
 
 int oracle_run_1d(
@@ -1103,16 +1244,37 @@ int oracle_run_1d(
     long long *num_steps, double *t, double *dt,
     char *errbuf, int errlen)
 {
+    return oracle_run_1d_ex(nx, g, x_min, x_max, gamma, integrator, riemann_solver, slope_limiter,
+                            bc_x_min, bc_x_max, cfl, tf, max_steps, rho, u, p, mass, mom_x, energy,
+                            num_steps, t, dt, errbuf, errlen, "cartesian_1d");
+}
+
+int oracle_run_1d_ex(
+    int nx, int g, double x_min, double x_max, double gamma,
+    const char *integrator, const char *riemann_solver, const char *slope_limiter,
+    const char *bc_x_min, const char *bc_x_max,
+    double cfl, double tf, long long max_steps,
+    double *rho, double *u, double *p,
+    double *mass, double *mom_x, double *energy,
+    long long *num_steps, double *t, double *dt,
+    char *errbuf, int errlen, const char *coord_sys)
+{
     set_err(errbuf, errlen, "");
     *num_steps = 0; *t = 0.0; *dt = 0.0;
     const int is_mh = integrator && !strcmp(integrator, "muscl_hancock_1d");
     const int is_god = integrator && !strcmp(integrator, "godunov_first_order_1d");
-    if (!is_mh && !is_god) { set_err(errbuf, errlen, "Integrator not recognized."); return VALUE_ERROR; }
+    const int is_rc = integrator && !strcmp(integrator, "random_choice_1d");
+    if (!is_mh && !is_god && !is_rc) { set_err(errbuf, errlen, "Integrator not recognized."); return VALUE_ERROR; }
+    int coord = 0;
+    if (coord_sys && !strcmp(coord_sys, "cartesian_1d")) coord = 1;
+    else if (coord_sys && !strcmp(coord_sys, "cylindrical_1d")) coord = 2;
+    else if (coord_sys && !strcmp(coord_sys, "spherical_1d")) coord = 3;
+    if (!coord) { set_err(errbuf, errlen, "Coordinate system not recognized."); return VALUE_ERROR; }
     Grid1 G;
     G.nx = nx; G.g = g; G.gamma = gamma;
     G.dx = (x_max - x_min) / (nx + 2 * g);
-    G.A = 1.0; G.vol = G.dx;
     G.tol = 1e-6;
+    G.alpha = (coord == 2) ? 1.0 : (coord == 3) ? 2.0 : 0.0;
     G.lim = parse_limiter(slope_limiter);
     if (!riemann_solver) { set_err(errbuf, errlen, "Riemann solver is not set."); return POINTER_ERROR; }
     if (!strcmp(riemann_solver, "riemann_solver_exact")) G.solver = SOLVER_EXACT;
@@ -1121,24 +1283,43 @@ int oracle_run_1d(
     if (G.lim < 0) { set_err(errbuf, errlen, "Slope limiter not recognized."); return VALUE_ERROR; }
     G.bc[0] = parse_bc(bc_x_min); G.bc[1] = parse_bc(bc_x_max);
     if (G.bc[0] < 0 || G.bc[1] < 0) { set_err(errbuf, errlen, "Boundary condition not recognized."); return VALUE_ERROR; }
+    const int tot = nx + 2 * g;
+    double *geo = malloc(sizeof(double) * (size_t) (3 * tot + 1));
+    if (!geo) { set_err(errbuf, errlen, "Memory allocation failed."); return MEMORY_ERROR; }
+    G.A = geo; G.V = geo + tot + 1; G.X = geo + 2 * tot + 1;
+    geometry_1d(&G, x_min, coord);
     G.W[0] = rho; G.W[1] = u; G.W[2] = p;
     G.U[0] = mass; G.U[1] = mom_x; G.U[2] = energy;
 
+    int status = OK;
     const double t_end = (max_steps >= 0) ? INFINITY : tf;
     while (*t < t_end && (max_steps < 0 || *num_steps < max_steps))
     {
         double step = time_step_1d(&G, (*num_steps < 10) ? cfl * 0.2 : cfl);
         if (*t + step > t_end) step = t_end - *t;
         *dt = step;
-        if (step == 0.0) { set_err(errbuf, errlen, "dt is zero."); return VALUE_ERROR; }
-        const int rc = is_mh ? mh1d_step(&G, step) : godunov1d_step(&G, step);
-        if (rc != OK) { set_err(errbuf, errlen, "Riemann solver failed."); return rc; }
-        conserved_to_primitive_1d(&G);
-        boundary_1d(&G);
+        if (step == 0.0) { set_err(errbuf, errlen, "dt is zero."); status = VALUE_ERROR; break; }
+        int rc;
+        if (is_rc)
+        {
+            rc = random_choice_step(&G, step, *num_steps);
+        }
+        else
+        {
+            rc = is_mh ? mh1d_step(&G, step) : godunov1d_step(&G, step);
+            if (rc == OK)
+            {
+                conserved_to_primitive_1d(&G);
+                boundary_1d(&G);
+            }
+        }
+        if (rc != OK) { set_err(errbuf, errlen, "Riemann solver failed."); status = rc; break; }
+        geometry_source_1d(&G, step);
         *t += step;
         (*num_steps)++;
     }
-    return OK;
+    free(geo);
+    return status;
 }
 
 /* ------------------------------------------------------- pointwise exports */

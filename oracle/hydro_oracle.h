@@ -51,6 +51,18 @@ int oracle_run_1d(
     long long *num_steps, double *t, double *dt,
     char *errbuf, int errlen);
 
+/* oracle_run_1d on a "cartesian_1d", "cylindrical_1d" or "spherical_1d"
+ * grid, with the random-choice integrator as well. */
+int oracle_run_1d_ex(
+    int nx, int g, double x_min, double x_max, double gamma,
+    const char *integrator, const char *riemann_solver, const char *slope_limiter,
+    const char *bc_x_min, const char *bc_x_max,
+    double cfl, double tf, long long max_steps,
+    double *rho, double *u, double *p,
+    double *mass, double *mom_x, double *energy,
+    long long *num_steps, double *t, double *dt,
+    char *errbuf, int errlen, const char *coord_sys);
+
 int oracle_hllc_2d(double gamma, double rho_L, double u_L, double v_L, double p_L,
                    double rho_R, double u_R, double v_R, double p_R, double tol, double *out4);
 int oracle_exact_flux_1d(double gamma, double rho_L, double u_L, double p_L,

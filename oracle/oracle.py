@@ -61,6 +61,11 @@ def _bind(lib: C.CDLL, prefix: str) -> C.CDLL:
     f.argtypes = ([C.c_int] * 2 + [C.c_double] * 3 + [C.c_char_p] * 5
                   + [C.c_double, C.c_double, C.c_longlong] + [_dp] * 6
                   + [_i64p, _dp, _dp, C.c_char_p, C.c_int])
+    f = getattr(lib, prefix + "run_1d_ex")
+    f.restype = C.c_int
+    f.argtypes = ([C.c_int] * 2 + [C.c_double] * 3 + [C.c_char_p] * 5
+                  + [C.c_double, C.c_double, C.c_longlong] + [_dp] * 6
+                  + [_i64p, _dp, _dp, C.c_char_p, C.c_int, C.c_char_p])
     f = getattr(lib, prefix + "hllc_2d")
     f.restype = C.c_int
     f.argtypes = [C.c_double] * 10 + [_dp]
@@ -149,13 +154,14 @@ class Backend:
         t = C.c_double(0)
         dt = C.c_double(0)
         err = C.create_string_buffer(4096)
-        f = getattr(self.lib, self.prefix + "run_1d")
+        f = getattr(self.lib, self.prefix + "run_1d_ex")
         enc = lambda s: s.encode() if s is not None else None
         rc = f(prob.nx, prob.g, prob.x_min, prob.x_max, prob.gamma,
                enc(prob.integrator), enc(prob.riemann_solver), enc(prob.slope_limiter),
                enc(prob.bc[0]), enc(prob.bc[1]), prob.cfl, prob.tf, prob.max_steps,
                _ptr(W[0]), _ptr(W[1]), _ptr(W[2]), _ptr(U[0]), _ptr(U[1]), _ptr(U[2]),
-               C.byref(n), C.byref(t), C.byref(dt), err, len(err))
+               C.byref(n), C.byref(t), C.byref(dt), err, len(err),
+               enc(getattr(prob, "coord_sys", "cartesian_1d")))
         return Result(rc, W, U, n.value, t.value, dt.value, err.value.decode(errors="replace"))
 
     def hllc_2d(self, gamma, L, R, tol=1e-6):
@@ -181,9 +187,9 @@ class Backend:
 # Seeded workloads live with the package (hydrofv_gb300/problems.py); they are
 # re-exported here so tests can use one namespace.
 from hydrofv_gb300.problems import (  # noqa: E402,F401
-    Problem1D, Problem2D, apply_bc_2d, four_quadrant, lid_driven_cavity, lid_top_bc, mid_points,
-    point_blast, primitive_to_conserved_1d, primitive_to_conserved_2d, random_problem_2d,
-    rayleigh_taylor, shear_layer, sod_1d,
+    Problem1D, Problem2D, apply_bc_2d, four_quadrant, geometry_1d, lid_driven_cavity, lid_top_bc,
+    mid_points, point_blast, primitive_to_conserved_1d, primitive_to_conserved_2d, random_problem_2d,
+    rayleigh_taylor, sedov_1d, shear_layer, sod_1d,
 )
 
 

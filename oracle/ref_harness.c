@@ -189,6 +189,17 @@ int ref_run_2d(
 }
 
 /* Run a 1D Cartesian problem; arrays are padded to nx+2g. */
+int ref_run_1d_ex(
+    int nx, int g, double x_min, double x_max, double gamma,
+    const char *integrator, const char *riemann_solver, const char *slope_limiter,
+    const char *bc_x_min, const char *bc_x_max,
+    double cfl, double tf, long long max_steps,
+    double *rho, double *u, double *p,
+    double *mass, double *mom_x, double *energy,
+    long long *num_steps, double *t, double *dt,
+    char *errbuf, int errlen, const char *coord_sys
+);
+
 int ref_run_1d(
     int nx, int g, double x_min, double x_max, double gamma,
     const char *integrator, const char *riemann_solver, const char *slope_limiter,
@@ -200,8 +211,25 @@ int ref_run_1d(
     char *errbuf, int errlen
 )
 {
+    return ref_run_1d_ex(nx, g, x_min, x_max, gamma, integrator, riemann_solver, slope_limiter, bc_x_min,
+                         bc_x_max, cfl, tf, max_steps, rho, u, p, mass, mom_x, energy, num_steps, t, dt,
+                         errbuf, errlen, "cartesian_1d");
+}
+
+/* ref_run_1d on a cartesian_1d, cylindrical_1d or spherical_1d grid. */
+int ref_run_1d_ex(
+    int nx, int g, double x_min, double x_max, double gamma,
+    const char *integrator, const char *riemann_solver, const char *slope_limiter,
+    const char *bc_x_min, const char *bc_x_max,
+    double cfl, double tf, long long max_steps,
+    double *rho, double *u, double *p,
+    double *mass, double *mom_x, double *energy,
+    long long *num_steps, double *t, double *dt,
+    char *errbuf, int errlen, const char *coord_sys
+)
+{
     System system = get_new_system_struct();
-    system.coord_sys = "cartesian_1d";
+    system.coord_sys = coord_sys;
     system.gamma = gamma;
     system.x_min = x_min;
     system.x_max = x_max;

@@ -67,8 +67,21 @@ def cases_1d():
     mhx.integrator = "muscl_hancock_1d"
     mhx.riemann_solver = "riemann_solver_exact"
     mhx.slope_limiter = "monotonized_central"
-    return {"sod_1000_godunov_exact": sod, "sod_200_muscl_hllc_vl": mh,
-            "sod_100_muscl_exact_mc": mhx}
+    out = {"sod_1000_godunov_exact": sod, "sod_200_muscl_hllc_vl": mh,
+           "sod_100_muscl_exact_mc": mhx}
+    # cylindrical / spherical grids (geometry source) and the random-choice integrator
+    for coord in ("cylindrical_1d", "spherical_1d"):
+        p = P.sod_1d(100, coord_sys=coord)
+        out[f"sod_100_{coord}_godunov_exact"] = p
+        p = P.sod_1d(100, coord_sys=coord)
+        p.integrator, p.riemann_solver, p.slope_limiter = "muscl_hancock_1d", "riemann_solver_hllc", "van_leer"
+        out[f"sod_100_{coord}_muscl_hllc_vl"] = p
+        out[f"sedov_60_{coord}_muscl_hllc_mc"] = P.sedov_1d(64, coord_sys=coord)
+    for coord in ("cartesian_1d", "spherical_1d"):
+        p = P.sod_1d(100, coord_sys=coord)
+        p.integrator = "random_choice_1d"
+        out[f"sod_100_{coord}_random_choice"] = p
+    return out
 
 
 def pointwise(ref):
