@@ -139,6 +139,22 @@ HD R limit_slope_rt(int lim, R a, R b)
     }
 }
 
+/*
+ * p_max / p_min <= 2, decided without the divide where that is exact.  For
+ * p_min > 0 (normal or subnormal) the rounded quotient is <= 2 exactly when
+ * p_max <= 2 p_min: if p_max > 2 p_min, the next representable p_max above
+ * 2 p_min puts the exact quotient more than half an ulp of 2 above 2, so it
+ * cannot round down to 2; otherwise the quotient is <= 2 and rounding is
+ * monotone.  (2 p_min overflowing is consistent too: both tests are true.)
+ * Zero, negative and NaN pressures take the reference's divide.
+ */
+template <class R>
+HD bool ratio_at_most_two(R p_max, R p_min)
+{
+    if (p_min > R(0)) return p_max <= R(2) * p_min;
+    return p_max / p_min <= R(2);
+}
+
 /* Star-pressure guess (PVRS / two-rarefaction / two-shock). */
 template <class R>
 HD R guess_p(const GasConst<R> &c, R rho_L, R u_L, R p_L, R a_L,
@@ -148,7 +164,7 @@ HD R guess_p(const GasConst<R> &c, R rho_L, R u_L, R p_L, R a_L,
     const R p_max = (p_L > p_R) ? p_L : p_R;
     const R ppv = R(0.5) * (p_L + p_R) - R(0.125) * (u_R - u_L) * (rho_L + rho_R) * (a_L + a_R);
     R pg;
-    if (p_max / p_min <= R(2) && (p_min <= ppv && ppv <= p_max)) {
+    if (ratio_at_most_two(p_max, p_min) && (p_min <= ppv && ppv <= p_max)) {
         pg = ppv;
     } else if (ppv < p_min) {
         pg = (a_L + a_R - c.half_gm1 * (u_R - u_L))
@@ -264,7 +280,7 @@ HD int hllc_classify(const GasConst<R> &c, R rho_L, R u_L, R p_L, R rho_R, R u_R
     const R p_min = (p_L > p_R) ? p_R : p_L;
     const R p_max = (p_L > p_R) ? p_L : p_R;
     ppv = R(0.5) * (p_L + p_R) - R(0.125) * (u_R - u_L) * (rho_L + rho_R) * (a_L + a_R);
-    if (p_max / p_min <= R(2) && (p_min <= ppv && ppv <= p_max)) return PREG_PVRS;
+    if (ratio_at_most_two(p_max, p_min) && (p_min <= ppv && ppv <= p_max)) return PREG_PVRS;
     if (ppv < p_min) return PREG_TRRS;
     return PREG_TSRS;
 }

@@ -232,3 +232,30 @@ def test_adjoint_rejects_boundary_none():
     p = random_problem_2d(16, 16, seed=1, bc=("none",) * 4, limiter="minmod", steps=4, smooth=True)
     with pytest.raises(H.HydroError):
         H.Adjoint2D(p, steps=4, checkpoint_every=2)
+
+
+
+def test_guess_p_divide_free_ratio_test_matches_reference(oracle_mod):
+    """The PVRS test p_max/p_min <= 2 is decided by p_max <= 2 p_min for
+    p_min > 0 in the library; the oracle keeps the reference's divide.  Edge
+    values around the boundary (quotients within an ulp of 2, subnormal and
+    huge pressures) must select the same guess."""
+    import math
+    rng = np.random.default_rng(5)
+    orc = oracle_mod.load("oracle")
+    lib = H.library()
+    cases = []
+    for _ in range(4000):
+        p_min = 10.0 ** rng.uniform(-310, 300)
+        k = int(rng.integers(-3, 4))
+        p_max = 2.0 * p_min
+        for _ in range(abs(k)):
+            p_max = math.nextafter(p_max, math.inf if k > 0 else 0.0)
+        cases.append((p_min, p_max))
+    cases += [(5e-324, 1e-323), (5e-324, 1.5e-323), (1e308, 1.7e308), (1e308, 1.79e308)]
+    for pl, pr in cases:
+        for a in ((pl, pr), (pr, pl)):
+            args = (1.4, 1.0, 0.0, a[0], 1.0, 1.0, 1e-3, a[1], 1.0, 1e-300)
+            ref = orc.guess_p(*args)
+            got = lib.guess_p(*args)
+            assert (ref == got) or (math.isnan(ref) and math.isnan(got)), (a, ref, got)
