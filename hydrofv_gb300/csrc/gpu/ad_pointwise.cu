@@ -63,9 +63,10 @@ extern "C" void hydro_ad_recon_vjp(int limiter, int dir, double gamma, double dt
 {
     const GasConst<double> c = make_gas_const<double>(gamma, 0.0);
     double own[4], A[4], B[4];
-    if (limiter == LIM_MINMOD) recon_cell_vjp<LIM_MINMOD>(dir, c, dtA, wm, w0, wp, lob, hib, own, A, B);
-    else if (limiter == LIM_VAN_LEER) recon_cell_vjp<LIM_VAN_LEER>(dir, c, dtA, wm, w0, wp, lob, hib, own, A, B);
-    else recon_cell_vjp<LIM_MC>(dir, c, dtA, wm, w0, wp, lob, hib, own, A, B);
+    const double a0 = sound_speed(c, w0[0], w0[3]), ir = 1.0 / w0[0], ip = 1.0 / w0[3];
+    if (limiter == LIM_MINMOD) recon_cell_vjp<LIM_MINMOD>(dir, dtA, wm, w0, wp, a0, ir, ip, lob, hib, own, A, B);
+    else if (limiter == LIM_VAN_LEER) recon_cell_vjp<LIM_VAN_LEER>(dir, dtA, wm, w0, wp, a0, ir, ip, lob, hib, own, A, B);
+    else recon_cell_vjp<LIM_MC>(dir, dtA, wm, w0, wp, a0, ir, ip, lob, hib, own, A, B);
     for (int q = 0; q < 4; q++) {
         w0b[q] = own[q];
         wmb[q] = -A[q];

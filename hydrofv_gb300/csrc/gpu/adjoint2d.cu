@@ -570,15 +570,16 @@ __global__ void __launch_bounds__(kThreads) ad_recon_vjp_kernel(const AdGeom q, 
         const int r = (int) (k / q.tx), c = (int) (k % q.tx);
         const bool nx_ = need_x(q, r, c), ny_ = need_y(q, r, c);
         if (!nx_ && !ny_) continue;
-        double w0[4], o[4] = { 0, 0, 0, 0 };
-        load_w4(q, s.W, r, c, w0);
+        double w0[4], a0, o[4] = { 0, 0, 0, 0 };
+        load_w(q, s.W, r, c, w0, a0);
+        const double inv_rho = 1.0 / w0[0], inv_p = 1.0 / w0[3];
         if (nx_) {
             double wm[4], wp[4], lob[4], hib[4], ox[4], A[4], B[4];
             load_w4(q, s.W, r, c - 1, wm);
             load_w4(q, s.W, r, c + 1, wp);
 #pragma unroll
             for (int e = 0; e < 4; e++) { lob[e] = fb.xlo[e][k]; hib[e] = fb.xhi[e][k]; }
-            recon_cell_vjp<LIM>(0, gas, dtA_x, wm, w0, wp, lob, hib, ox, A, B);
+            recon_cell_vjp<LIM>(0, dtA_x, wm, w0, wp, a0, inv_rho, inv_p, lob, hib, ox, A, B);
 #pragma unroll
             for (int e = 0; e < 4; e++) { o[e] += ox[e]; sh.Ax[e][k] = A[e]; sh.Bx[e][k] = B[e]; }
         }
@@ -588,7 +589,7 @@ __global__ void __launch_bounds__(kThreads) ad_recon_vjp_kernel(const AdGeom q, 
             load_w4(q, s.W, r + 1, c, wp);
 #pragma unroll
             for (int e = 0; e < 4; e++) { lob[e] = fb.ylo[e][k]; hib[e] = fb.yhi[e][k]; }
-            recon_cell_vjp<LIM>(1, gas, dtA_y, wm, w0, wp, lob, hib, oy, A, B);
+            recon_cell_vjp<LIM>(1, dtA_y, wm, w0, wp, a0, inv_rho, inv_p, lob, hib, oy, A, B);
 #pragma unroll
             for (int e = 0; e < 4; e++) { o[e] += oy[e]; sh.Ay[e][k] = A[e]; sh.By[e][k] = B[e]; }
         }

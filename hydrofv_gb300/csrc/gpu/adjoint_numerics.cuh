@@ -82,7 +82,7 @@ HD void sound_speed_vjp(double rho, double p, double a, double ab, double &rhob,
  * states.  Accumulates into rhob, nb, tb, pb, ab, the slope adjoints db[4]
  * and d_rho_velb (the slope that feeds the density row).
  */
-HD void hancock_2d_vjp(double dtA, double dtA_rho, double rho, double n, double a,
+HD void hancock_2d_vjp(double dtA, double dtA_rho, double rho, double inv_rho, double n, double a,
                        const double d[4], double d_rho_vel, const double lob[4],
                        const double hib[4], double &rhob, double &nb, double &tb, double &pb,
                        double &ab, double db[4], double &d_rho_velb)
@@ -107,7 +107,7 @@ HD void hancock_2d_vjp(double dtA, double dtA_rho, double rho, double n, double 
     const double s1 = lob[1] + hib[1];
     const double dtA_rhob = -0.5 * d[3] * s1;
     db[3] += -0.5 * dtA_rho * s1;
-    rhob += -dtA_rhob * dtA_rho / rho;                     /* d(dtA/rho)/drho */
+    rhob += -dtA_rhob * dtA_rho * inv_rho;                 /* d(dtA/rho)/drho */
     rhob += drb * dtA;
     db[0] += -0.5 * up * lob[0] + 0.5 * um * hib[0];
     db[1] += -0.5 * up * lob[1] + 0.5 * um * hib[1];
@@ -291,14 +291,20 @@ HD void hllc_vjp_core(const GasConst<double> &c, const double L[4], const double
         hllc_vacuum_vjp(c, L, Rs, s.aL, s.aR, Fb, Lb, Rb);
         return;
     }
+    /* Only the forward intermediates in s decide branches; the reverse below
+     * is derivatives only, so a quotient that appears several times is
+     * formed once as a reciprocal (a derivative, not a bit-parity value). */
     const double rl = L[0], ul = L[1], vl = L[2], pl = L[3];
     const double rr = Rs[0], ur = Rs[1], vr = Rs[2], pr = Rs[3];
+    const double inv_rl = 1.0 / rl, inv_rr = 1.0 / rr, inv_pl = 1.0 / pl, inv_pr = 1.0 / pr;
+    const double inv_gm1 = 1.0 / c.gm1;
     double rLb = 0, uLb = 0, vLb = 0, pLb = 0, rRb = 0, uRb = 0, vRb = 0, pRb = 0;
     double aLb = 0, aRb = 0;
     /* ---- region flux of the selected side K ---- */
     const bool left = s.region <= 1;
     const double rho = left ? rl : rr, u = left ? ul : ur, v = left ? vl : vr, p = left ? pl : pr;
-    const double E = rho * (0.5 * (u * u + v * v) + p / (rho * c.gm1));
+    const double inv_rho = left ? inv_rl : inv_rr;
+    const double E = 0.5 * rho * (u * u + v * v) + p * inv_gm1;
     const double fm = rho * u;
     double rhob = 0, ub = 0, vb = 0, pb = 0;
     double fmb = Fb[0] + Fb[1] * u + Fb[2] * v;
@@ -311,10 +317,14 @@ HD void hllc_vjp_core(const GasConst<double> &c, const double L[4], const double
         const double S = left ? s.SL : s.SR;
         const double Ss = s.Ss;
         const double Smu = S - u, SmS = S - Ss;
-        const double rs = rho * Smu / SmS;
+        const double inv_SmS = 1.0 / SmS;
         const double D = rho * Smu;
-        const double Z = Ss + p / D;
-        const double Y = E / rho + (Ss - u) * Z;
+        const double inv_D = 1.0 / D;
+        const double rs = D * inv_SmS;
+        const double pD = p * inv_D;
+        const double Z = Ss + pD;
+        const double Er = E * inv_rho;
+        const double Y = Er + (Ss - u) * Z;
         const double es = rs * Y;
         double Sb = Fb[0] * (rs - rho) + Fb[1] * (rs * Ss - rho * u) + Fb[2] * (rs * v - rho * v)
                   + Fb[3] * (es - E);
@@ -327,19 +337,17 @@ HD void hllc_vjp_core(const GasConst<double> &c, const double L[4], const double
         vb += Fb[2] * S * (rs - rho);
         rsb += esb * Y;
         const double Yb = esb * rs;
-        Eb += Yb / rho;
-        rhob += -Yb * E / (rho * rho);
+        Eb += Yb * inv_rho;
+        rhob += -Yb * Er * inv_rho;
         Ssb += Yb * Z;
         ub += -Yb * Z;
         const double Zb = Yb * (Ss - u);
         Ssb += Zb;
-        pb += Zb / D;
-        const double Db = -Zb * p / (D * D);
-        rhob += Db * Smu;
-        Sb += Db * rho;
-        ub += -Db * rho;
-        const double Nb = rsb / SmS;
-        const double Mb = -rsb * rs / SmS;
+        pb += Zb * inv_D;
+        const double Db = -Zb * pD * inv_D;
+        /* rs = N / M, N = D = rho (S - u), M = S - Ss */
+        const double Nb = rsb * inv_SmS + Db;
+        const double Mb = -rsb * rs * inv_SmS;
         rhob += Nb * Smu;
         Sb += Nb * rho;
         ub += -Nb * rho;
@@ -353,29 +361,24 @@ HD void hllc_vjp_core(const GasConst<double> &c, const double L[4], const double
     rhob += Eb * 0.5 * (u * u + v * v);
     ub += Eb * rho * u;
     vb += Eb * rho * v;
-    pb += Eb / c.gm1;
+    pb += Eb * inv_gm1;
     if (left) { rLb += rhob; uLb += ub; vLb += vb; pLb += pb; }
     else { rRb += rhob; uRb += ub; vRb += vb; pRb += pb; }
 
     /* ---- S* ---- */
     if (Ssb != 0.0) {
-        const double Dd = rl * (s.SL - ul) - rr * (s.SR - ur);
+        const double dL = s.SL - ul, dR = s.SR - ur;
+        const double Dd = rl * dL - rr * dR;
         const double Nnb = Ssb / Dd;
-        const double Ddb = -Ssb * s.Ss / Dd;
+        const double Ddb = -Nnb * s.Ss;
         pRb += Nnb;
         pLb -= Nnb;
-        rLb += Nnb * ul * (s.SL - ul);
-        uLb += Nnb * rl * (s.SL - ul) - Nnb * rl * ul;
-        SLb += Nnb * rl * ul;
-        rRb -= Nnb * ur * (s.SR - ur);
-        uRb -= Nnb * rr * (s.SR - ur) - Nnb * rr * ur;
-        SRb -= Nnb * rr * ur;
-        rLb += Ddb * (s.SL - ul);
-        SLb += Ddb * rl;
-        uLb -= Ddb * rl;
-        rRb -= Ddb * (s.SR - ur);
-        SRb -= Ddb * rr;
-        uRb += Ddb * rr;
+        rLb += Nnb * ul * dL + Ddb * dL;
+        uLb += Nnb * rl * (dL - ul) - Ddb * rl;
+        SLb += (Nnb * ul + Ddb) * rl;
+        rRb -= Nnb * ur * dR + Ddb * dR;
+        uRb -= Nnb * rr * (dR - ur) - Ddb * rr;
+        SRb -= (Nnb * ur + Ddb) * rr;
     }
 
     /* ---- wave speeds ---- */
@@ -387,14 +390,14 @@ HD void hllc_vjp_core(const GasConst<double> &c, const double L[4], const double
     const double qRb = SRb * s.aR;
     double psb = 0.0;
     if (s.ps > pl) {
-        const double t = c.q_coef / (2.0 * s.qL);
-        psb += qLb * t / pl;
-        pLb -= qLb * t * s.ps / (pl * pl);
+        const double t = qLb * (0.5 * c.q_coef) / s.qL * inv_pl;
+        psb += t;
+        pLb -= t * s.ps * inv_pl;
     }
     if (s.ps > pr) {
-        const double t = c.q_coef / (2.0 * s.qR);
-        psb += qRb * t / pr;
-        pRb -= qRb * t * s.ps / (pr * pr);
+        const double t = qRb * (0.5 * c.q_coef) / s.qR * inv_pr;
+        psb += t;
+        pRb -= t * s.ps * inv_pr;
     }
     const double pgb = (s.pg < c.tol) ? 0.0 : psb;
 
@@ -405,37 +408,35 @@ HD void hllc_vjp_core(const GasConst<double> &c, const double L[4], const double
     } else if (s.reg == PREG_TRRS) {
         const double zL = have_z ? z0 : pow(pl, c.half_gm1_g);
         const double zR = have_z ? z1 : pow(pr, c.half_gm1_g);
+        const double izL = 1.0 / zL, izR = 1.0 / zR;
         const double num = s.aL + s.aR - c.half_gm1 * (ur - ul);
-        const double den = s.aL / zL + s.aR / zR;
-        const double base = num / den;
-        const double baseb = pgb * c.g_half_gm1 * s.pg / base;
-        const double numb = baseb / den;
-        const double denb = -baseb * base / den;
-        aLb += numb;
-        aRb += numb;
+        const double den = s.aL * izL + s.aR * izR;
+        /* pg = (num / den)^(1/hg): d pg = (pg / hg) (d num / num - d den / den) */
+        const double k = pgb * c.g_half_gm1 * s.pg;
+        const double numb = k / num;
+        const double denb = -k / den;
+        aLb += numb + denb * izL;
+        aRb += numb + denb * izR;
         uRb -= numb * c.half_gm1;
         uLb += numb * c.half_gm1;
-        aLb += denb / zL;
-        aRb += denb / zR;
-        const double zLb = -denb * s.aL / (zL * zL);
-        const double zRb = -denb * s.aR / (zR * zR);
-        pLb += zLb * c.half_gm1_g * zL / pl;
-        pRb += zRb * c.half_gm1_g * zR / pr;
+        /* den = aL zL^-1 + aR zR^-1, zK = pK^hg: d den / d pK = -aK hg zK^-1 / pK */
+        pLb -= denb * s.aL * izL * c.half_gm1_g * inv_pl;
+        pRb -= denb * s.aR * izR * c.half_gm1_g * inv_pr;
     } else {
         const double BL = s.ppv + pl * c.gm1_gp1, BR = s.ppv + pr * c.gm1_gp1;
         const double gL = have_z ? z0 : sqrt((2.0 / (c.gp1 * rl)) / BL);
         const double gR = have_z ? z1 : sqrt((2.0 / (c.gp1 * rr)) / BR);
-        const double Dd = gL + gR;
-        const double Nnb = pgb / Dd;
-        const double Ddb = -pgb * s.pg / Dd;
+        const double Nnb = pgb / (gL + gR);
+        const double Ddb = -Nnb * s.pg;
         const double gLb = Nnb * pl + Ddb, gRb = Nnb * pr + Ddb;
         pLb += Nnb * gL;
         pRb += Nnb * gR;
         uRb -= Nnb;
         uLb += Nnb;
-        rLb += -gLb * gL / (2.0 * rl);
-        rRb += -gRb * gR / (2.0 * rr);
-        const double BLb = -gLb * gL / (2.0 * BL), BRb = -gRb * gR / (2.0 * BR);
+        const double hL = 0.5 * gLb * gL, hR = 0.5 * gRb * gR;
+        rLb -= hL * inv_rl;
+        rRb -= hR * inv_rr;
+        const double BLb = -hL / BL, BRb = -hR / BR;
         ppvb += BLb + BRb;
         pLb += BLb * c.gm1_gp1;
         pRb += BRb * c.gm1_gp1;
@@ -444,9 +445,10 @@ HD void hllc_vjp_core(const GasConst<double> &c, const double L[4], const double
         pLb += 0.5 * ppvb;
         pRb += 0.5 * ppvb;
         const double du = ur - ul, sr = rl + rr, sa = s.aL + s.aR;
-        const double dub = -0.125 * sr * sa * ppvb;
-        const double srb = -0.125 * du * sa * ppvb;
-        const double sab = -0.125 * du * sr * ppvb;
+        const double w = -0.125 * ppvb;
+        const double dub = w * sr * sa;
+        const double srb = w * du * sa;
+        const double sab = w * du * sr;
         uRb += dub;
         uLb -= dub;
         rLb += srb;
@@ -454,8 +456,12 @@ HD void hllc_vjp_core(const GasConst<double> &c, const double L[4], const double
         aLb += sab;
         aRb += sab;
     }
-    sound_speed_vjp(rl, pl, s.aL, aLb, rLb, pLb);
-    sound_speed_vjp(rr, pr, s.aR, aRb, rRb, pRb);
+    /* a = sqrt(gamma p / rho): da = a/2 (dp/p - drho/rho) */
+    const double hL = 0.5 * aLb * s.aL, hR = 0.5 * aRb * s.aR;
+    rLb -= hL * inv_rl;
+    pLb += hL * inv_pl;
+    rRb -= hR * inv_rr;
+    pRb += hR * inv_pr;
     Lb[0] = rLb; Lb[1] = uLb; Lb[2] = vLb; Lb[3] = pLb;
     Rb[0] = rRb; Rb[1] = uRb; Rb[2] = vRb; Rb[3] = pRb;
 }
@@ -521,22 +527,22 @@ HD int recon_code(const double wm[4], const double w0[4], const double wp[4])
 }
 
 /*
- * Reverse of recon_cell (a0 = sound speed of w0, folded back into w0).
+ * Reverse of recon_cell (a0 = sound speed of w0, folded back into w0;
+ * inv_rho, inv_p = 1/rho, 1/p of w0).
  * Given lob / hib (sweep order), writes in storage order (rho, vx, vy, p):
  *   own  adjoint reaching w0 itself, including its share of the slopes;
  *   A    adjoint of the backward differences w0 - wm (wm receives -A);
  *   B    adjoint of the forward differences wp - w0 (wp receives +B).
  */
 template <int LIM>
-HD void recon_cell_vjp(int dir, const GasConst<double> &gas, double dtA, const double wm[4],
-                       const double w0[4], const double wp[4], const double lob[4],
-                       const double hib[4], double own[4], double A[4], double B[4])
+HD void recon_cell_vjp(int dir, double dtA, const double wm[4], const double w0[4], const double wp[4],
+                       double a0, double inv_rho, double inv_p, const double lob[4], const double hib[4],
+                       double own[4], double A[4], double B[4])
 {
     double pa[4], pb[4], d[4];
     int code;
 #pragma unroll
     for (int q = 0; q < 4; q++) d[q] = limit_slope_partials<LIM>(w0[q] - wm[q], wp[q] - w0[q], pa[q], pb[q], code);
-    const double a0 = sound_speed(gas, w0[0], w0[3]);
     const int in_ = (dir == 0) ? 1 : 2;    /* storage index of the normal velocity */
     const int it_ = (dir == 0) ? 2 : 1;    /* storage index of the tangential velocity */
     double ds[4];                          /* slopes in sweep order */
@@ -546,8 +552,8 @@ HD void recon_cell_vjp(int dir, const GasConst<double> &gas, double dtA, const d
     ds[3] = d[3];
     double rhob = 0, nb = 0, tb = 0, pbb = 0, ab = 0, dvxb = 0;
     double dsb[4] = { 0, 0, 0, 0 };
-    hancock_2d_vjp(dtA, dtA / w0[0], w0[0], w0[in_], a0, ds, d[1], lob, hib, rhob, nb, tb, pbb, ab,
-                   dsb, dvxb);
+    hancock_2d_vjp(dtA, dtA * inv_rho, w0[0], inv_rho, w0[in_], a0, ds, d[1], lob, hib, rhob, nb, tb, pbb,
+                   ab, dsb, dvxb);
     double db[4];                          /* slope adjoints, storage order */
     db[0] = dsb[0];
     db[in_] = dsb[1];
@@ -558,7 +564,10 @@ HD void recon_cell_vjp(int dir, const GasConst<double> &gas, double dtA, const d
     own[in_] = nb;
     own[it_] = tb;
     own[3] = pbb;
-    sound_speed_vjp(w0[0], w0[3], a0, ab, own[0], own[3]);
+    /* a = sqrt(gamma p / rho): da = a/2 (dp/p - drho/rho) */
+    const double h = 0.5 * ab * a0;
+    own[0] -= h * inv_rho;
+    own[3] += h * inv_p;
 #pragma unroll
     for (int q = 0; q < 4; q++) {
         A[q] = db[q] * pa[q];
