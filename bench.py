@@ -65,6 +65,15 @@ def profile_traffic() -> float | None:
     return float(d["dram_bytes_per_launch_2048"])
 
 
+def profile_fp64_counts() -> dict | None:
+    """FP64 instructions per cell-update of the step kernel (committed ncu counts)."""
+    path = os.path.join(ROOT, "profiles", "mh2d_fp64_counts.json")
+    if not os.path.exists(path):
+        return None
+    with open(path) as f:
+        return json.load(f)
+
+
 class ClockSampler:
     """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
 
@@ -167,6 +176,27 @@ def cpu_sample(steps_hint: int, budget_s: float = 12.0) -> dict:
             "sample": f"first {n} steps of the {N_SIDE}x{N_SIDE} shear layer "
                       f"({r.seconds:.1f} s, OpenMP {threads} threads)",
             "seconds": r.seconds, "steps": n}
+
+
+def fp_roofline(prec, value, fp64_tflops, fp32_tflops, H) -> dict:
+    """The binding roof of the FP64 step: its FP64 pipe.  achieved = FP64 warp
+    instructions issued per second (ncu count per cell-update x measured
+    cell-updates/s); peak = the measured FMA rate of hydro_gpu_calibrate as
+    warp instructions per second (every FP64 instruction takes one pipe slot
+    per lane)."""
+    out = {"bound": "fp64_pipe" if prec == H.PRECISION_FP64 else "fp32_pipe",
+           "peak_tflops_fp64": fp64_tflops, "peak_tflops_fp32": fp32_tflops}
+    counts = profile_fp64_counts()
+    if prec == H.PRECISION_FP64 and counts and N_SIDE == 2048:
+        per_cell = counts["fp64_warp_inst_per_cell_update"]
+        achieved = value * per_cell
+        peak = fp64_tflops * 1e12 / 2 / 32
+        out.update({"achieved": achieved, "peak": peak, "unit": "FP64 warp instructions/s",
+                    "frac": achieved / peak, "of": "measured (hydro_gpu_calibrate)",
+                    "fp64_warp_inst_per_cell_update": per_cell,
+                    "fp64_thread_inst_per_cell_update": counts["fp64_thread_inst_per_cell_update"],
+                    "counts_source": counts["source"]})
+    return out
 
 
 def run_reference_arm(args) -> None:
@@ -556,10 +586,7 @@ def main() -> None:
                      "unit": "GB/s", "frac": achieved_gbs / pk["hbm_gbs"],
                      "traffic": traffic, "peak_source": pk["source"],
                      "bytes_per_cell_update": bytes_per_cell},
-        "fp_roofline": {"bound": "fp64_pipe" if prec == H.PRECISION_FP64 else "fp32_pipe",
-                        "peak_tflops_fp64": fp64_tflops, "peak_tflops_fp32": fp32_tflops,
-                        "note": "peaks measured by hydro_gpu_calibrate (FMA chains); "
-                                "FP64 instruction counts per launch are in profiles/"},
+        "fp_roofline": fp_roofline(prec, value, fp64_tflops, fp32_tflops, H),
         "forms": {
             "fp64": {"value": cells * args.steps / (fp64_ms * 1e-3), "ms_per_step": fp64_ms / args.steps,
                      "conserved_drift": drift_main if prec == H.PRECISION_FP64 else drift_o},

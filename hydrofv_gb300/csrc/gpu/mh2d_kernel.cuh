@@ -493,8 +493,12 @@ __device__ __forceinline__ void mh2d_item(const Mh2dArgs<R> &a, Mh2dShared<R, NT
  * SMs that finish early take more work (the FP64 pipe of an SM is shared by
  * its CTAs).
  */
+/* FP64: 4 CTAs per SM (128 registers; the FP64 pipe is the bound).  FP32:
+ * 8 CTAs per SM (64 registers, a few spills): the FP32 form is latency
+ * bound, and at 8 per SM the 1088 work items of a 2048^2 grid run in one
+ * wave (measured 7.4 -> 10.5 G cell-updates/s). */
 template <class R, int LIM, int NT, int FIRST_ORDER, bool TAPE = false, bool GRAV = false>
-__global__ void __launch_bounds__(NT, 4) mh2d_step_kernel(const Mh2dArgs<R> a)
+__global__ void __launch_bounds__(NT, (sizeof(R) == 4 ? 8 : 4)) mh2d_step_kernel(const Mh2dArgs<R> a)
 {
     static_assert(NT % 32 == 0, "NT must be a whole number of warps");
     HydroStepControl *ctrl = a.ctrl;
@@ -672,7 +676,7 @@ __device__ __forceinline__ void instance_bookkeeping(HydroStepControl *ctrl, con
  * items.
  */
 template <class R, int LIM, int NT, int FIRST_ORDER>
-__global__ void __launch_bounds__(NT, 4) mh2d_batch_step_kernel(const Mh2dBatchArgs<R> b)
+__global__ void __launch_bounds__(NT, (sizeof(R) == 4 ? 8 : 4)) mh2d_batch_step_kernel(const Mh2dBatchArgs<R> b)
 {
     __shared__ Mh2dShared<R, NT> sm;
     __shared__ int s_inst, s_local, s_go, s_last;
