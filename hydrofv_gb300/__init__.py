@@ -184,6 +184,8 @@ _SIGNATURES = {
     "hydro_ad_hllc_forced": (None, [C.c_double, C.c_double, _dp, _dp, C.c_int, _dp]),
     "hydro_ad_recon_forced": (None, [C.c_int, C.c_int, C.c_double, C.c_double, _dp, _dp, _dp, C.c_int,
                                      _dp, _dp, _P(C.c_int)]),
+    "hydro_fx_eval_host": (None, [C.c_int, C.c_longlong, _dp, _dp, _dp, C.c_void_p]),
+    "hydro_gpu_fx_eval": (C.c_int, [C.c_int, C.c_int, C.c_longlong, _dp, _dp, _dp, _dp, C.c_void_p]),
     "hydro_gpu_device_count": (C.c_int, []),
     "hydro_gpu_calibrate": (C.c_int, [C.c_int, _dp, _dp]),
     "hydro_gpu_version": (C.c_char_p, []),
@@ -761,3 +763,36 @@ def ad_recon_forced(limiter, direction, gamma, dtA, wm, w0, wp, code):
     library().hydro_ad_recon_forced(limiter, direction, gamma, dtA, *[a.ctypes.data_as(_dp) for a in args],
                                     int(code), lo.ctypes.data_as(_dp), hi.ctypes.data_as(_dp), C.byref(nat))
     return lo, hi, nat.value
+
+
+def _fx_args(op, a, b):
+    a = np.ascontiguousarray(a, dtype=np.float64).ravel()
+    b = a if op == 1 else np.ascontiguousarray(b, dtype=np.float64).ravel()
+    if b.shape != a.shape:
+        raise ValueError("a and b must have the same size")
+    return a, b
+
+
+def fx_eval_host(op, a, b=None):
+    """Integer-pipe FP64 division (op 0: a / b) or square root (op 1:
+    sqrt(a)), host build: (results, fast-path flags)."""
+    a, b = _fx_args(op, a, b)
+    out = np.empty_like(a)
+    ok = np.zeros(a.shape, dtype=np.uint8)
+    library().hydro_fx_eval_host(int(op), a.size, a.ctypes.data_as(_dp), b.ctypes.data_as(_dp),
+                                 out.ctypes.data_as(_dp), ok.ctypes.data)
+    return out, ok.astype(bool)
+
+
+def gpu_fx_eval(op, a, b=None, device=0):
+    """The same on the GPU: (what the FP64 kernels compute, the hardware
+    operation, fast-path flags)."""
+    a, b = _fx_args(op, a, b)
+    fast, hw = np.empty_like(a), np.empty_like(a)
+    ok = np.zeros(a.shape, dtype=np.uint8)
+    rc = library().hydro_gpu_fx_eval(int(device), int(op), a.size, a.ctypes.data_as(_dp),
+                                     b.ctypes.data_as(_dp), fast.ctypes.data_as(_dp),
+                                     hw.ctypes.data_as(_dp), ok.ctypes.data)
+    if rc != 0:
+        raise HydroError(rc, "hydro_gpu_fx_eval failed (CUDA error)")
+    return fast, hw, ok.astype(bool)

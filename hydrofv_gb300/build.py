@@ -39,6 +39,7 @@ CUDA_SOURCES = [
     ("gpu/run1d.cu", ["--fmad=false"]),
     ("gpu/adjoint2d.cu", ["--fmad=false"]),
     ("gpu/ad_pointwise.cu", ["--fmad=false"]),
+    ("gpu/fx_check.cu", ["--fmad=false"]),
 ]
 C_SOURCES = [
     "host/error.c",

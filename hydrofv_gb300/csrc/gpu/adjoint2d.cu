@@ -572,7 +572,7 @@ __global__ void __launch_bounds__(kThreads) ad_recon_vjp_kernel(const AdGeom q, 
         if (!nx_ && !ny_) continue;
         double w0[4], a0, o[4] = { 0, 0, 0, 0 };
         load_w(q, s.W, r, c, w0, a0);
-        const double inv_rho = 1.0 / w0[0], inv_p = 1.0 / w0[3];
+        const double inv_rho = dv(1.0, w0[0]), inv_p = dv(1.0, w0[3]);
         if (nx_) {
             double wm[4], wp[4], lob[4], hib[4], ox[4], A[4], B[4];
             load_w4(q, s.W, r, c - 1, wm);

@@ -44,8 +44,8 @@ HD double limit_slope_partials(double a, double b, double &da, double &db, int &
     }
     if (LIM == LIM_VAN_LEER) {
         const double s = a + b + 1e-10;
-        da = (2.0 * b - d) / s;
-        db = (2.0 * a - d) / s;
+        da = dv(2.0 * b - d, s);
+        db = dv(2.0 * a - d, s);
         code = 1;
         return d;
     }
@@ -70,8 +70,8 @@ HD double limit_slope_partials(double a, double b, double &da, double &db, int &
 HD void sound_speed_vjp(double rho, double p, double a, double ab, double &rhob, double &pb)
 {
     if (ab == 0.0) return;
-    rhob -= ab * (0.5 * a / rho);
-    pb += ab * (0.5 * a / p);
+    rhob -= ab * dv(0.5 * a, rho);
+    pb += ab * dv(0.5 * a, p);
 }
 
 /* ------------------------------------------------------------- predictor */
@@ -140,8 +140,8 @@ HD int hllc_fwd(const GasConst<double> &c, double rl, double ul, double pl, doub
     s.qR = hllc_q(c, pr, s.ps);
     s.SL = ul - s.aL * s.qL;
     s.SR = ur + s.aR * s.qR;
-    s.Ss = (pr - pl + rl * ul * (s.SL - ul) - rr * ur * (s.SR - ur))
-         / (rl * (s.SL - ul) - rr * (s.SR - ur));
+    s.Ss = dv(pr - pl + rl * ul * (s.SL - ul) - rr * ur * (s.SR - ur),
+              rl * (s.SL - ul) - rr * (s.SR - ur));
     if (0.0 <= s.SL) s.region = 0;
     else if (s.SL <= 0.0 && 0.0 <= s.Ss) s.region = 1;
     else if (s.Ss <= 0.0 && 0.0 <= s.SR) s.region = 2;
@@ -228,8 +228,8 @@ HD int hllc_fwd_from_guess(const GasConst<double> &c, double rl, double ul, doub
     s.qR = hllc_q(c, pr, s.ps);
     s.SL = ul - s.aL * s.qL;
     s.SR = ur + s.aR * s.qR;
-    s.Ss = (pr - pl + rl * ul * (s.SL - ul) - rr * ur * (s.SR - ur))
-         / (rl * (s.SL - ul) - rr * (s.SR - ur));
+    s.Ss = dv(pr - pl + rl * ul * (s.SL - ul) - rr * ur * (s.SR - ur),
+              rl * (s.SL - ul) - rr * (s.SR - ur));
     if (0.0 <= s.SL) s.region = 0;
     else if (s.SL <= 0.0 && 0.0 <= s.Ss) s.region = 1;
     else if (s.Ss <= 0.0 && 0.0 <= s.SR) s.region = 2;
@@ -296,8 +296,8 @@ HD void hllc_vjp_core(const GasConst<double> &c, const double L[4], const double
      * formed once as a reciprocal (a derivative, not a bit-parity value). */
     const double rl = L[0], ul = L[1], vl = L[2], pl = L[3];
     const double rr = Rs[0], ur = Rs[1], vr = Rs[2], pr = Rs[3];
-    const double inv_rl = 1.0 / rl, inv_rr = 1.0 / rr, inv_pl = 1.0 / pl, inv_pr = 1.0 / pr;
-    const double inv_gm1 = 1.0 / c.gm1;
+    const double inv_rl = dv(1.0, rl), inv_rr = dv(1.0, rr), inv_pl = dv(1.0, pl), inv_pr = dv(1.0, pr);
+    const double inv_gm1 = dv(1.0, c.gm1);
     double rLb = 0, uLb = 0, vLb = 0, pLb = 0, rRb = 0, uRb = 0, vRb = 0, pRb = 0;
     double aLb = 0, aRb = 0;
     /* ---- region flux of the selected side K ---- */
@@ -317,9 +317,9 @@ HD void hllc_vjp_core(const GasConst<double> &c, const double L[4], const double
         const double S = left ? s.SL : s.SR;
         const double Ss = s.Ss;
         const double Smu = S - u, SmS = S - Ss;
-        const double inv_SmS = 1.0 / SmS;
+        const double inv_SmS = dv(1.0, SmS);
         const double D = rho * Smu;
-        const double inv_D = 1.0 / D;
+        const double inv_D = dv(1.0, D);
         const double rs = D * inv_SmS;
         const double pD = p * inv_D;
         const double Z = Ss + pD;
@@ -369,7 +369,7 @@ HD void hllc_vjp_core(const GasConst<double> &c, const double L[4], const double
     if (Ssb != 0.0) {
         const double dL = s.SL - ul, dR = s.SR - ur;
         const double Dd = rl * dL - rr * dR;
-        const double Nnb = Ssb / Dd;
+        const double Nnb = dv(Ssb, Dd);
         const double Ddb = -Nnb * s.Ss;
         pRb += Nnb;
         pLb -= Nnb;
@@ -390,12 +390,12 @@ HD void hllc_vjp_core(const GasConst<double> &c, const double L[4], const double
     const double qRb = SRb * s.aR;
     double psb = 0.0;
     if (s.ps > pl) {
-        const double t = qLb * (0.5 * c.q_coef) / s.qL * inv_pl;
+        const double t = dv(qLb * (0.5 * c.q_coef), s.qL) * inv_pl;
         psb += t;
         pLb -= t * s.ps * inv_pl;
     }
     if (s.ps > pr) {
-        const double t = qRb * (0.5 * c.q_coef) / s.qR * inv_pr;
+        const double t = dv(qRb * (0.5 * c.q_coef), s.qR) * inv_pr;
         psb += t;
         pRb -= t * s.ps * inv_pr;
     }
@@ -408,13 +408,13 @@ HD void hllc_vjp_core(const GasConst<double> &c, const double L[4], const double
     } else if (s.reg == PREG_TRRS) {
         const double zL = have_z ? z0 : pow(pl, c.half_gm1_g);
         const double zR = have_z ? z1 : pow(pr, c.half_gm1_g);
-        const double izL = 1.0 / zL, izR = 1.0 / zR;
+        const double izL = dv(1.0, zL), izR = dv(1.0, zR);
         const double num = s.aL + s.aR - c.half_gm1 * (ur - ul);
         const double den = s.aL * izL + s.aR * izR;
         /* pg = (num / den)^(1/hg): d pg = (pg / hg) (d num / num - d den / den) */
         const double k = pgb * c.g_half_gm1 * s.pg;
-        const double numb = k / num;
-        const double denb = -k / den;
+        const double numb = dv(k, num);
+        const double denb = dv(-k, den);
         aLb += numb + denb * izL;
         aRb += numb + denb * izR;
         uRb -= numb * c.half_gm1;
@@ -424,9 +424,9 @@ HD void hllc_vjp_core(const GasConst<double> &c, const double L[4], const double
         pRb -= denb * s.aR * izR * c.half_gm1_g * inv_pr;
     } else {
         const double BL = s.ppv + pl * c.gm1_gp1, BR = s.ppv + pr * c.gm1_gp1;
-        const double gL = have_z ? z0 : sqrt((2.0 / (c.gp1 * rl)) / BL);
-        const double gR = have_z ? z1 : sqrt((2.0 / (c.gp1 * rr)) / BR);
-        const double Nnb = pgb / (gL + gR);
+        const double gL = have_z ? z0 : sq(dv(dv(2.0, c.gp1 * rl), BL));
+        const double gR = have_z ? z1 : sq(dv(dv(2.0, c.gp1 * rr), BR));
+        const double Nnb = dv(pgb, gL + gR);
         const double Ddb = -Nnb * s.pg;
         const double gLb = Nnb * pl + Ddb, gRb = Nnb * pr + Ddb;
         pLb += Nnb * gL;
@@ -436,7 +436,7 @@ HD void hllc_vjp_core(const GasConst<double> &c, const double L[4], const double
         const double hL = 0.5 * gLb * gL, hR = 0.5 * gRb * gR;
         rLb -= hL * inv_rl;
         rRb -= hR * inv_rr;
-        const double BLb = -hL / BL, BRb = -hR / BR;
+        const double BLb = dv(-hL, BL), BRb = dv(-hR, BR);
         ppvb += BLb + BRb;
         pLb += BLb * c.gm1_gp1;
         pRb += BRb * c.gm1_gp1;
@@ -500,14 +500,14 @@ HD void recon_cell(int dir, R dtA, const R wm[4], const R w0[4], const R wp[4], 
     if (dir == 0) {
 #pragma unroll
         for (int q = 0; q < 4; q++) d[q] = limit_slope<LIM>(w0[q] - wm[q], wp[q] - w0[q]);
-        hancock_2d(dtA, dtA / w0[0], w0[0], w0[1], w0[2], w0[3], a0, d, d[1], lo, hi);
+        hancock_2d(dtA, dv(dtA, w0[0]), w0[0], w0[1], w0[2], w0[3], a0, d, d[1], lo, hi);
     } else {
         d[0] = limit_slope<LIM>(w0[0] - wm[0], wp[0] - w0[0]);
         const R dvx = limit_slope<LIM>(w0[1] - wm[1], wp[1] - w0[1]);
         d[1] = limit_slope<LIM>(w0[2] - wm[2], wp[2] - w0[2]);
         d[2] = dvx;
         d[3] = limit_slope<LIM>(w0[3] - wm[3], wp[3] - w0[3]);
-        hancock_2d(dtA, dtA / w0[0], w0[0], w0[2], w0[1], w0[3], a0, d, dvx, lo, hi);
+        hancock_2d(dtA, dv(dtA, w0[0]), w0[0], w0[2], w0[1], w0[3], a0, d, dvx, lo, hi);
     }
 }
 
@@ -589,7 +589,7 @@ HD double limit_slope_forced(double a, double b, int code)
 {
     if (code == 0) return 0.0;
     if (LIM == LIM_MINMOD) return (code == 1) ? a : b;
-    if (LIM == LIM_VAN_LEER) return 2.0 * a * b / (a + b + 1e-10);
+    if (LIM == LIM_VAN_LEER) return dv(2.0 * a * b, a + b + 1e-10);
     if (code == 1) return (a > 0.0) ? 0.5 * (a + b) : -(-0.5 * (a + b));
     return 2.0 * ((code == 2) ? a : b);
 }
@@ -602,10 +602,10 @@ HD void recon_cell_forced(int dir, double dtA, const double wm[4], const double 
 #pragma unroll
     for (int q = 0; q < 4; q++) d[q] = limit_slope_forced<LIM>(w0[q] - wm[q], wp[q] - w0[q], (code >> (2 * q)) & 3);
     if (dir == 0) {
-        hancock_2d(dtA, dtA / w0[0], w0[0], w0[1], w0[2], w0[3], a0, d, d[1], lo, hi);
+        hancock_2d(dtA, dv(dtA, w0[0]), w0[0], w0[1], w0[2], w0[3], a0, d, d[1], lo, hi);
     } else {
         const double ds[4] = { d[0], d[2], d[1], d[3] };
-        hancock_2d(dtA, dtA / w0[0], w0[0], w0[2], w0[1], w0[3], a0, ds, d[1], lo, hi);
+        hancock_2d(dtA, dv(dtA, w0[0]), w0[0], w0[2], w0[1], w0[3], a0, ds, d[1], lo, hi);
     }
 }
 
@@ -660,15 +660,15 @@ HD void hllc_flux_2d_forced(const GasConst<double> &c, double rl, double ul, dou
     if (reg == PREG_TRRS) pg = guess_p_trrs(c, ul, pl, aL, ur, pr, aR);
     else if (reg == PREG_TSRS) pg = guess_p_tsrs(c, rl, ul, pl, rr, ur, pr, ppv);
     const double ps = (code & 4) ? c.tol : pg;
-    const double qL = (code & 8) ? sqrt(1.0 + c.q_coef * (ps / pl - 1.0)) : 1.0;
-    const double qR = (code & 16) ? sqrt(1.0 + c.q_coef * (ps / pr - 1.0)) : 1.0;
+    const double qL = (code & 8) ? sq(1.0 + c.q_coef * (dv(ps, pl) - 1.0)) : 1.0;
+    const double qR = (code & 16) ? sq(1.0 + c.q_coef * (dv(ps, pr) - 1.0)) : 1.0;
     const double SL = ul - aL * qL;
     const double SR = ur + aR * qR;
-    const double Ss = (pr - pl + rl * ul * (SL - ul) - rr * ur * (SR - ur)) / (rl * (SL - ul) - rr * (SR - ur));
+    const double Ss = dv(pr - pl + rl * ul * (SL - ul) - rr * ur * (SR - ur), rl * (SL - ul) - rr * (SR - ur));
     const int region = (code >> 5) & 3;
     const bool left = region <= 1;
     const double rho = left ? rl : rr, u = left ? ul : ur, v = left ? vl : vr, p = left ? pl : pr;
-    const double E = rho * (0.5 * (u * u + v * v) + p / (rho * c.gm1));
+    const double E = rho * (0.5 * (u * u + v * v) + dv(p, rho * c.gm1));
     const double fm = rho * u;
     F[0] = fm;
     F[1] = fm * u + p;
@@ -676,8 +676,8 @@ HD void hllc_flux_2d_forced(const GasConst<double> &c, double rl, double ul, dou
     F[3] = u * (E + p);
     if (region == 1 || region == 2) {
         const double S = left ? SL : SR;
-        const double rs = rho * (S - u) / (S - Ss);
-        const double es = rs * (E / rho + (Ss - u) * (Ss + p / (rho * (S - u))));
+        const double rs = dv(rho * (S - u), S - Ss);
+        const double es = rs * (dv(E, rho) + (Ss - u) * (Ss + dv(p, rho * (S - u))));
         F[0] = fm + S * (rs - rho);
         F[1] = F[1] + S * (rs * Ss - rho * u);
         F[2] = F[2] + S * (rs * v - rho * v);
@@ -691,16 +691,16 @@ HD void hllc_flux_2d_forced(const GasConst<double> &c, double rl, double ul, dou
 HD void cons_to_prim_2d_vjp(const GasConst<double> &c, double vol, double m, double mx, double my,
                             const double wb[4], double Ub[4])
 {
-    const double w1 = mx / m, w2 = my / m;
+    const double w1 = dv(mx, m), w2 = dv(my, m);
     const double K = w1 * w1 + w2 * w2;
-    const double Pb = wb[3] * c.gm1 / vol;
+    const double Pb = dv(wb[3] * c.gm1, vol);
     Ub[3] += Pb;
-    double mb = -0.5 * K * Pb + wb[0] / vol;
+    double mb = -0.5 * K * Pb + dv(wb[0], vol);
     const double w1b = wb[1] - m * w1 * Pb;
     const double w2b = wb[2] - m * w2 * Pb;
-    Ub[1] += w1b / m;
-    Ub[2] += w2b / m;
-    mb += -(w1b * w1 + w2b * w2) / m;
+    Ub[1] += dv(w1b, m);
+    Ub[2] += dv(w2b, m);
+    mb += dv(-(w1b * w1 + w2b * w2), m);
     Ub[0] += mb;
 }
 
@@ -715,7 +715,7 @@ HD void prim_to_cons_2d_vjp(const GasConst<double> &c, double vol, const double 
     wb[0] += mb * vol + Ub[3] * vol * 0.5 * (u * u + v * v);
     wb[1] += Ub[1] * m + Ub[3] * vol * rho * u;
     wb[2] += Ub[2] * m + Ub[3] * vol * rho * v;
-    wb[3] += Ub[3] * vol / c.gm1;
+    wb[3] += dv(Ub[3] * vol, c.gm1);
 }
 
 /* The same conversion forward, templated for the tangent-linear state. */
@@ -726,7 +726,7 @@ HD void prim_to_cons_2d(const GasConst<R> &c, R vol, const R w[4], R U[4])
     U[0] = m;
     U[1] = m * w[1];
     U[2] = m * w[2];
-    U[3] = vol * (R(0.5) * w[0] * (w[1] * w[1] + w[2] * w[2]) + w[3] / c.gm1);
+    U[3] = vol * (R(0.5) * w[0] * (w[1] * w[1] + w[2] * w[2]) + dv(w[3], c.gm1));
 }
 
 }  // namespace hydro

@@ -1,0 +1,78 @@
+/*
+ * fx_check.cu -- evaluation entry points for the integer-pipe FP64 division
+ * and square root (fp64_int.cuh), used by the tests: the host build over
+ * arrays (checked on the CPU against the host's IEEE operations), and the
+ * device build next to the hardware operations on the GPU.
+ */
+#include <cuda_runtime.h>
+
+#include "fp64_int.cuh"
+#include "hydro_gpu.h"
+
+using namespace hydro;
+
+namespace {
+
+/* op 0: a / b, op 1: sqrt(a).  fast = the integer form where it applies
+ * (else the hardware result), hw = the hardware operation, ok = 1 where the
+ * integer form applied. */
+__global__ void fx_eval_kernel(int op, long long n, const double *a, const double *b,
+                               double *fast, double *hw, unsigned char *ok)
+{
+    const long long stride = (long long) gridDim.x * blockDim.x;
+    for (long long i = (long long) blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        bool k;
+        double f;
+        if (op == 0) {
+            f = fx::div_fast(a[i], b[i], k);
+            hw[i] = fx::div_hw(a[i], b[i]);
+            fast[i] = k ? f : dv(a[i], b[i]);
+        } else {
+            f = fx::sqrt_fast(a[i], k);
+            hw[i] = fx::sqrt_hw(a[i]);
+            fast[i] = k ? f : sq(a[i]);
+        }
+        ok[i] = k ? 1 : 0;
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+void hydro_fx_eval_host(int op, long long n, const double *a, const double *b, double *out,
+                        unsigned char *ok)
+{
+    for (long long i = 0; i < n; i++) {
+        bool k;
+        out[i] = (op == 0) ? fx::div_fast(a[i], b[i], k) : fx::sqrt_fast(a[i], k);
+        ok[i] = k ? 1 : 0;
+    }
+}
+
+int hydro_gpu_fx_eval(int device, int op, long long n, const double *a, const double *b,
+                      double *fast, double *hw, unsigned char *ok)
+{
+    if (n <= 0) return 0;
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) return (int) e;
+    const size_t nb = (size_t) n * sizeof(double);
+    char *slab = nullptr;
+    e = cudaMalloc(&slab, 4 * nb + (size_t) n);
+    if (e != cudaSuccess) return (int) e;
+    double *da = (double *) slab, *db = da + n, *df = db + n, *dh = df + n;
+    unsigned char *dk = (unsigned char *) (dh + n);
+    e = cudaMemcpy(da, a, nb, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(db, op == 0 ? b : a, nb, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        fx_eval_kernel<<<4 * 152, 256>>>(op, n, da, db, df, dh, dk);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(fast, df, nb, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(hw, dh, nb, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(ok, dk, (size_t) n, cudaMemcpyDeviceToHost);
+    cudaFree(slab);
+    return (int) e;
+}
+
+}  // extern "C"

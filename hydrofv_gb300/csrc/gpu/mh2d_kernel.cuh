@@ -323,7 +323,7 @@ __device__ __forceinline__ void mh2d_item(const Mh2dArgs<R> &a, Mh2dShared<R, NT
         d[1] = limit_slope<LIM>(vy - sm.ring[sb][2][u], sm.ring[st][2][u] - vy);
         d[2] = dvx;
         d[3] = limit_slope<LIM>(p - sm.ring[sb][3][u], sm.ring[st][3][u] - p);
-        hancock_2d(dtA_y, dtA_y / rho, rho, vy, vx, p, as, d, dvx, lo, hi);
+        hancock_2d(dtA_y, dv(dtA_y, rho), rho, vy, vx, p, as, d, dvx, lo, hi);
     };
 
     /* x reconstruction of slot tid in ring row s, (rho, u, v, p) order */
@@ -340,7 +340,7 @@ __device__ __forceinline__ void mh2d_item(const Mh2dArgs<R> &a, Mh2dShared<R, NT
         d[1] = limit_slope<LIM>(vx - sm.ring[s][1][u - 1], sm.ring[s][1][u + 1] - vx);
         d[2] = limit_slope<LIM>(vy - sm.ring[s][2][u - 1], sm.ring[s][2][u + 1] - vy);
         d[3] = limit_slope<LIM>(p - sm.ring[s][3][u - 1], sm.ring[s][3][u + 1] - p);
-        hancock_2d(dtA_x, dtA_x / rho, rho, vx, vy, p, as, d, d[1], lo, hi);
+        hancock_2d(dtA_x, dv(dtA_x, rho), rho, vx, vy, p, as, d, d[1], lo, hi);
     };
 
     /* ---- prologue: the faces below r_begin ---- */
@@ -441,7 +441,7 @@ __device__ __forceinline__ void mh2d_item(const Mh2dArgs<R> &a, Mh2dShared<R, NT
                 const R k3 = k2;
                 const R k4 = pf * (Un[2] + km);
                 Un[2] = Un[2] + km;
-                Un[3] = Un[3] + (k1 + R(2) * k2 + R(2) * k3 + k4) / R(6);
+                Un[3] = Un[3] + dv(k1 + R(2) * k2 + R(2) * k3 + k4, R(6));
 #pragma unroll
                 for (int q = 0; q < 4; q++) Uout[q][idx] = Un[q];
             }

@@ -26,6 +26,8 @@
 
 #include <math.h>
 #include <string.h>
+
+#include "fp64_int.cuh"
 #ifdef __cplusplus
 #include <cmath>
 using std::fabs;
@@ -115,7 +117,7 @@ HD GasConst<R> make_gas_const(double gamma, double tol)
 template <class R>
 HD R sound_speed(const GasConst<R> &c, R rho, R p)
 {
-    return sqrt(c.gamma * p / rho);
+    return sq(dv(c.gamma * p, rho));
 }
 
 template <int LIM, class R>
@@ -123,7 +125,7 @@ HD R limit_slope(R a, R b)
 {
     if (a * b <= R(0)) return R(0);
     if (LIM == LIM_MINMOD) return (fabs(a) < fabs(b)) ? a : b;
-    if (LIM == LIM_VAN_LEER) return R(2) * a * b / (a + b + R(1e-10));
+    if (LIM == LIM_VAN_LEER) return dv(R(2) * a * b, a + b + R(1e-10));
     if (a > R(0)) return fmin(R(0.5) * (a + b), R(2) * fmin(fabs(a), fabs(b)));
     return -fmin(R(-0.5) * (a + b), R(2) * fmin(fabs(a), fabs(b)));
 }
@@ -167,13 +169,13 @@ HD R guess_p(const GasConst<R> &c, R rho_L, R u_L, R p_L, R a_L,
     if (ratio_at_most_two(p_max, p_min) && (p_min <= ppv && ppv <= p_max)) {
         pg = ppv;
     } else if (ppv < p_min) {
-        pg = (a_L + a_R - c.half_gm1 * (u_R - u_L))
-           / (a_L / pow(p_L, c.half_gm1_g) + a_R / pow(p_R, c.half_gm1_g));
+        pg = dv(a_L + a_R - c.half_gm1 * (u_R - u_L),
+                dv(a_L, pow(p_L, c.half_gm1_g)) + dv(a_R, pow(p_R, c.half_gm1_g)));
         pg = pow(pg, c.g_half_gm1);
     } else {
-        const R gL = sqrt((R(2) / (c.gp1 * rho_L)) / (ppv + p_L * c.gm1_gp1));
-        const R gR = sqrt((R(2) / (c.gp1 * rho_R)) / (ppv + p_R * c.gm1_gp1));
-        pg = (gL * p_L + gR * p_R - (u_R - u_L)) / (gL + gR);
+        const R gL = sq(dv(dv(R(2), c.gp1 * rho_L), ppv + p_L * c.gm1_gp1));
+        const R gR = sq(dv(dv(R(2), c.gp1 * rho_R), ppv + p_R * c.gm1_gp1));
+        pg = dv(gL * p_L + gR * p_R - (u_R - u_L), gL + gR);
     }
     if (pg < c.tol) pg = c.tol;
     return pg;
@@ -239,7 +241,7 @@ template <class R>
 HD R hllc_q(const GasConst<R> &c, R p_X, R p_star)
 {
     if (p_star <= p_X) return R(1);
-    return sqrt(R(1) + c.q_coef * (p_star / p_X - R(1)));
+    return sq(R(1) + c.q_coef * (dv(p_star, p_X) - R(1)));
 }
 
 /*
@@ -275,7 +277,7 @@ HD int hllc_classify(const GasConst<R> &c, R rho_L, R u_L, R p_L, R rho_R, R u_R
     a_L = (rho_L > R(0)) ? sound_speed(c, rho_L, p_L) : R(0);
     a_R = (rho_R > R(0)) ? sound_speed(c, rho_R, p_R) : R(0);
     ppv = R(0);
-    if (rho_L <= R(0) || rho_R <= R(0) || ((a_L + a_R) * R(2) / c.gp1) <= (u_R - u_L))
+    if (rho_L <= R(0) || rho_R <= R(0) || dv((a_L + a_R) * R(2), c.gp1) <= (u_R - u_L))
         return PREG_VACUUM;
     const R p_min = (p_L > p_R) ? p_R : p_L;
     const R p_max = (p_L > p_R) ? p_L : p_R;
@@ -294,32 +296,32 @@ HD R guess_p_trrs_z(const GasConst<R> &c, R u_L, R p_L, R a_L, R u_R, R p_R, R a
 {
     zL = pow(p_L, c.half_gm1_g);
     zR = pow(p_R, c.half_gm1_g);
-    const R pg = (a_L + a_R - c.half_gm1 * (u_R - u_L)) / (a_L / zL + a_R / zR);
+    const R pg = dv(a_L + a_R - c.half_gm1 * (u_R - u_L), dv(a_L, zL) + dv(a_R, zR));
     return pow(pg, c.g_half_gm1);
 }
 
 template <class R>
 HD R guess_p_trrs(const GasConst<R> &c, R u_L, R p_L, R a_L, R u_R, R p_R, R a_R)
 {
-    const R pg = (a_L + a_R - c.half_gm1 * (u_R - u_L))
-               / (a_L / pow(p_L, c.half_gm1_g) + a_R / pow(p_R, c.half_gm1_g));
+    const R pg = dv(a_L + a_R - c.half_gm1 * (u_R - u_L),
+                    dv(a_L, pow(p_L, c.half_gm1_g)) + dv(a_R, pow(p_R, c.half_gm1_g)));
     return pow(pg, c.g_half_gm1);
 }
 
 template <class R>
 HD R guess_p_tsrs_g(const GasConst<R> &c, R rho_L, R u_L, R p_L, R rho_R, R u_R, R p_R, R ppv, R &gL, R &gR)
 {
-    gL = sqrt((R(2) / (c.gp1 * rho_L)) / (ppv + p_L * c.gm1_gp1));
-    gR = sqrt((R(2) / (c.gp1 * rho_R)) / (ppv + p_R * c.gm1_gp1));
-    return (gL * p_L + gR * p_R - (u_R - u_L)) / (gL + gR);
+    gL = sq(dv(dv(R(2), c.gp1 * rho_L), ppv + p_L * c.gm1_gp1));
+    gR = sq(dv(dv(R(2), c.gp1 * rho_R), ppv + p_R * c.gm1_gp1));
+    return dv(gL * p_L + gR * p_R - (u_R - u_L), gL + gR);
 }
 
 template <class R>
 HD R guess_p_tsrs(const GasConst<R> &c, R rho_L, R u_L, R p_L, R rho_R, R u_R, R p_R, R ppv)
 {
-    const R gL = sqrt((R(2) / (c.gp1 * rho_L)) / (ppv + p_L * c.gm1_gp1));
-    const R gR = sqrt((R(2) / (c.gp1 * rho_R)) / (ppv + p_R * c.gm1_gp1));
-    return (gL * p_L + gR * p_R - (u_R - u_L)) / (gL + gR);
+    const R gL = sq(dv(dv(R(2), c.gp1 * rho_L), ppv + p_L * c.gm1_gp1));
+    const R gR = sq(dv(dv(R(2), c.gp1 * rho_R), ppv + p_R * c.gm1_gp1));
+    return dv(gL * p_L + gR * p_R - (u_R - u_L), gL + gR);
 }
 
 /* Flux of the vacuum / vacuum-generation case (src/riemann_solver_hllc.c:249-287). */
@@ -345,8 +347,8 @@ HD int hllc_finish(const GasConst<R> &c, R rho_L, R u_L, R v_L, R p_L, R a_L,
     const R ps = (pg < c.tol) ? c.tol : pg;
     const R S_L = u_L - a_L * hllc_q(c, p_L, ps);
     const R S_R = u_R + a_R * hllc_q(c, p_R, ps);
-    const R S_s = (p_R - p_L + rho_L * u_L * (S_L - u_L) - rho_R * u_R * (S_R - u_R))
-                / (rho_L * (S_L - u_L) - rho_R * (S_R - u_R));
+    const R S_s = dv(p_R - p_L + rho_L * u_L * (S_L - u_L) - rho_R * u_R * (S_R - u_R),
+                     rho_L * (S_L - u_L) - rho_R * (S_R - u_R));
     int region;
     if (R(0) <= S_L) region = 0;
     else if (S_L <= R(0) && R(0) <= S_s) region = 1;
@@ -358,7 +360,7 @@ HD int hllc_finish(const GasConst<R> &c, R rho_L, R u_L, R v_L, R p_L, R a_L,
     const R u = left ? u_L : u_R;
     const R v = left ? v_L : v_R;
     const R p = left ? p_L : p_R;
-    const R E = rho * (R(0.5) * (u * u + v * v) + p / (rho * c.gm1));
+    const R E = rho * (R(0.5) * (u * u + v * v) + dv(p, rho * c.gm1));
     const R fm = rho * u;
     F[0] = fm;
     F[1] = fm * u + p;
@@ -366,8 +368,8 @@ HD int hllc_finish(const GasConst<R> &c, R rho_L, R u_L, R v_L, R p_L, R a_L,
     F[3] = u * (E + p);
     if (region == 1 || region == 2) {
         const R S = left ? S_L : S_R;
-        const R rs = rho * (S - u) / (S - S_s);
-        const R es = rs * (E / rho + (S_s - u) * (S_s + p / (rho * (S - u))));
+        const R rs = dv(rho * (S - u), S - S_s);
+        const R es = rs * (dv(E, rho) + (S_s - u) * (S_s + dv(p, rho * (S - u))));
         F[0] = fm + S * (rs - rho);
         F[1] = F[1] + S * (rs * S_s - rho * u);
         F[2] = F[2] + S * (rs * v - rho * v);
@@ -403,7 +405,7 @@ HD int hllc_flux_1d(const GasConst<R> &c, R rho_L, R u_L, R p_L, R rho_R, R u_R,
 {
     const R a_L = (rho_L > R(0)) ? sound_speed(c, rho_L, p_L) : R(0);
     const R a_R = (rho_R > R(0)) ? sound_speed(c, rho_R, p_R) : R(0);
-    if (rho_L <= R(0) || rho_R <= R(0) || ((a_L + a_R) * R(2) / c.gp1) <= (u_R - u_L)) {
+    if (rho_L <= R(0) || rho_R <= R(0) || dv((a_L + a_R) * R(2), c.gp1) <= (u_R - u_L)) {
         R s[4];
         solve_vacuum(c, rho_L, u_L, R(0), p_L, a_L, rho_R, u_R, R(0), p_R, a_R, R(0), s);
         const R E = s[0] * (R(0.5) * s[1] * s[1] + s[3] / (s[0] * c.gm1));
@@ -415,37 +417,37 @@ HD int hllc_flux_1d(const GasConst<R> &c, R rho_L, R u_L, R p_L, R rho_R, R u_R,
     const R ps = guess_p(c, rho_L, u_L, p_L, a_L, rho_R, u_R, p_R, a_R);
     const R S_L = u_L - a_L * hllc_q(c, p_L, ps);
     const R S_R = u_R + a_R * hllc_q(c, p_R, ps);
-    const R S_s = (p_R - p_L + rho_L * u_L * (S_L - u_L) - rho_R * u_R * (S_R - u_R))
-                / (rho_L * (S_L - u_L) - rho_R * (S_R - u_R));
+    const R S_s = dv(p_R - p_L + rho_L * u_L * (S_L - u_L) - rho_R * u_R * (S_R - u_R),
+                     rho_L * (S_L - u_L) - rho_R * (S_R - u_R));
     if (R(0) <= S_L) {
-        const R E = rho_L * (R(0.5) * u_L * u_L + p_L / (rho_L * c.gm1));
+        const R E = rho_L * (R(0.5) * u_L * u_L + dv(p_L, rho_L * c.gm1));
         F[0] = rho_L * u_L;
         F[1] = rho_L * u_L * u_L + p_L;
         F[2] = u_L * (E + p_L);
         return DEV_OK;
     }
     if (S_L <= R(0) && R(0) <= S_s) {
-        const R E = rho_L * (R(0.5) * u_L * u_L + p_L / (rho_L * c.gm1));
+        const R E = rho_L * (R(0.5) * u_L * u_L + dv(p_L, rho_L * c.gm1));
         const R fm = rho_L * u_L;
-        const R rs = rho_L * (S_L - u_L) / (S_L - S_s);
-        const R es = rs * (E / rho_L + (S_s - u_L) * (S_s + p_L / (rho_L * (S_L - u_L))));
+        const R rs = dv(rho_L * (S_L - u_L), S_L - S_s);
+        const R es = rs * (dv(E, rho_L) + (S_s - u_L) * (S_s + dv(p_L, rho_L * (S_L - u_L))));
         F[0] = fm + S_L * (rs - rho_L);
         F[1] = (fm * u_L + p_L) + S_L * (rs * S_s - rho_L * u_L);
         F[2] = u_L * (E + p_L) + S_L * (es - E);
         return DEV_OK;
     }
     if (S_s <= R(0) && R(0) <= S_R) {
-        const R E = rho_R * (R(0.5) * u_R * u_R + p_R / (rho_R * c.gm1));
+        const R E = rho_R * (R(0.5) * u_R * u_R + dv(p_R, rho_R * c.gm1));
         const R fm = rho_R * u_R;
-        const R rs = rho_R * (S_R - u_R) / (S_R - S_s);
-        const R es = rs * (E / rho_R + (S_s - u_R) * (S_s + p_R / (rho_R * (S_R - u_R))));
+        const R rs = dv(rho_R * (S_R - u_R), S_R - S_s);
+        const R es = rs * (dv(E, rho_R) + (S_s - u_R) * (S_s + dv(p_R, rho_R * (S_R - u_R))));
         F[0] = fm + S_R * (rs - rho_R);
         F[1] = (fm * u_R + p_R) + S_R * (rs * S_s - rho_R * u_R);
         F[2] = u_R * (E + p_R) + S_R * (es - E);
         return DEV_OK;
     }
     if (S_R <= R(0)) {
-        const R E = rho_R * (R(0.5) * u_R * u_R + p_R / (rho_R * c.gm1));
+        const R E = rho_R * (R(0.5) * u_R * u_R + dv(p_R, rho_R * c.gm1));
         F[0] = rho_R * u_R;
         F[1] = rho_R * u_R * u_R + p_R;
         F[2] = u_R * (E + p_R);
@@ -608,7 +610,7 @@ HD int exact_solve_1d(const GasConst<R> &c, R rho_L, R u_L, R p_L, R rho_R, R u_
 {
     const R a_L = (rho_L > R(0)) ? sound_speed(c, rho_L, p_L) : R(0);
     const R a_R = (rho_R > R(0)) ? sound_speed(c, rho_R, p_R) : R(0);
-    if (rho_L <= R(0) || rho_R <= R(0) || ((a_L + a_R) * R(2) / c.gp1) <= (u_R - u_L)) {
+    if (rho_L <= R(0) || rho_R <= R(0) || dv((a_L + a_R) * R(2), c.gp1) <= (u_R - u_L)) {
         R s[4];
         solve_vacuum(c, rho_L, u_L, R(0), p_L, a_L, rho_R, u_R, R(0), p_R, a_R, S, s);
         o[0] = s[0]; o[1] = s[1]; o[2] = s[3];
@@ -671,7 +673,7 @@ HD void hancock_1d(R dtA, R rho, R u, R p, R a, const R d[3], R lo[3], R hi[3])
     const R up = R(1) + dtA * u;
     const R um = R(1) - dtA * u;
     const R dr = dtA * rho;
-    const R drd = dtA / rho;
+    const R drd = dv(dtA, rho);
     lo[0] = rho + R(-0.5) * (up * d[0] + dr * d[1] + R(0));
     lo[1] = u + R(-0.5) * (R(0) + up * d[1] + drd * d[2]);
     lo[2] = p + R(-0.5) * (R(0) + dr * a * a * d[1] + up * d[2]);
@@ -686,10 +688,10 @@ HD void hancock_1d(R dtA, R rho, R u, R p, R a, const R d[3], R lo[3], R hi[3])
 template <class R>
 HD void cons_to_prim_2d(const GasConst<R> &c, R vol, R m, R mx, R my, R E, R w[4])
 {
-    w[0] = m / vol;
-    w[1] = mx / m;
-    w[2] = my / m;
-    w[3] = c.gm1 * (E - R(0.5) * m * (w[1] * w[1] + w[2] * w[2])) / vol;
+    w[0] = dv(m, vol);
+    w[1] = dv(mx, m);
+    w[2] = dv(my, m);
+    w[3] = dv(c.gm1 * (E - R(0.5) * m * (w[1] * w[1] + w[2] * w[2])), vol);
 }
 
 /* FP32 state: the same conversion, except that where the kinetic energy is
