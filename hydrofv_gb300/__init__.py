@@ -774,8 +774,9 @@ def _fx_args(op, a, b):
 
 
 def fx_eval_host(op, a, b=None):
-    """Integer-pipe FP64 division (op 0: a / b) or square root (op 1:
-    sqrt(a)), host build: (results, fast-path flags)."""
+    """Integer-pipe FP64 division (op 0: a / b), square root (op 1:
+    sqrt(a)) or power (op 2: pow(a, b)), host build: (results, fast-path
+    flags)."""
     a, b = _fx_args(op, a, b)
     out = np.empty_like(a)
     ok = np.zeros(a.shape, dtype=np.uint8)

@@ -30,6 +30,10 @@ INCLUDES = ["-I" + os.path.join(ROOT, "include"), "-I" + os.path.join(CSRC, "gpu
 # (source, extra nvcc flags)
 CUDA_SOURCES = [
     ("gpu/mh2d.cu", ["--fmad=false"]),
+    ("gpu/mh2d_lim_minmod.cu", ["--fmad=false"]),
+    ("gpu/mh2d_lim_vanleer.cu", ["--fmad=false"]),
+    ("gpu/mh2d_lim_mc.cu", ["--fmad=false"]),
+    ("gpu/mh2d_lim_first_order.cu", ["--fmad=false"]),
     ("gpu/mh2d_fp32.cu", []),
     ("gpu/runtime2d.cu", []),
     ("gpu/runtime_batch.cu", []),

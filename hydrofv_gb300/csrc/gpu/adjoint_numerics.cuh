@@ -195,8 +195,8 @@ HD void vacuum_fan_vjp(const GasConst<double> &c, bool right, double rho, double
 {
     const double k = (u - 0.0) * c.gm1 / (c.gp1 * a);
     const double t0 = right ? (c.two_gp1 + k) : (c.two_gp1 - k);
-    const double t = pow(t0, c.two_gm1);
-    const double tg = pow(t, c.gamma);
+    const double t = pw(t0, c.two_gm1);
+    const double tg = pw(t, c.gamma);
     rhob += ob[0] * t;
     const double tb = ob[0] * rho + ob[3] * p * c.gamma * tg / t;
     pb += ob[3] * tg;
@@ -406,8 +406,8 @@ HD void hllc_vjp_core(const GasConst<double> &c, const double L[4], const double
     if (s.reg == PREG_PVRS) {
         ppvb += pgb;
     } else if (s.reg == PREG_TRRS) {
-        const double zL = have_z ? z0 : pow(pl, c.half_gm1_g);
-        const double zR = have_z ? z1 : pow(pr, c.half_gm1_g);
+        const double zL = have_z ? z0 : pw(pl, c.half_gm1_g);
+        const double zR = have_z ? z1 : pw(pr, c.half_gm1_g);
         const double izL = dv(1.0, zL), izR = dv(1.0, zR);
         const double num = s.aL + s.aR - c.half_gm1 * (ur - ul);
         const double den = s.aL * izL + s.aR * izR;
@@ -623,18 +623,18 @@ HD void vacuum_flux_forced(const GasConst<double> &c, double rl, double ul, doub
             s[0] = rho; s[1] = u; s[2] = v; s[3] = p;
         } else if (right) {
             double tmp = c.two_gp1 + (u - 0.0) * c.gm1 / (c.gp1 * a);
-            tmp = pow(tmp, c.two_gm1);
+            tmp = pw(tmp, c.two_gm1);
             s[0] = rho * tmp;
             s[1] = (a + c.half_gm1 * u + 0.0) * 2.0 / c.gp1;
             s[2] = v;
-            s[3] = p * pow(tmp, c.gamma);
+            s[3] = p * pw(tmp, c.gamma);
         } else {
             double tmp = c.two_gp1 - (u - 0.0) * c.gm1 / (c.gp1 * a);
-            tmp = pow(tmp, c.two_gm1);
+            tmp = pw(tmp, c.two_gm1);
             s[0] = rho * tmp;
             s[1] = (-a + c.half_gm1 * u + 0.0) * 2.0 / c.gp1;
             s[2] = v;
-            s[3] = p * pow(tmp, c.gamma);
+            s[3] = p * pw(tmp, c.gamma);
         }
     }
     const double E = s[0] * (0.5 * (s[1] * s[1] + s[2] * s[2]) + s[3] / (s[0] * c.gm1));

@@ -21,6 +21,8 @@
 
 #include <math.h>
 
+#include "pow_int.cuh"
+
 #ifdef __CUDACC__
 #define DHD __host__ __device__ __forceinline__
 #else
@@ -43,8 +45,8 @@ DHD Dual operator-(Dual a) { return Dual(-a.v, -a.d); }
 DHD Dual operator*(Dual a, Dual b) { return Dual(a.v * b.v, a.d * b.v + a.v * b.d); }
 DHD Dual operator/(Dual a, Dual b)
 {
-    const double q = a.v / b.v;
-    return Dual(q, (a.d - q * b.d) / b.v);
+    const double q = dv(a.v, b.v);
+    return Dual(q, dv(a.d - q * b.d, b.v));
 }
 DHD Dual &operator+=(Dual &a, Dual b) { a = a + b; return a; }
 DHD Dual &operator-=(Dual &a, Dual b) { a = a - b; return a; }
@@ -58,8 +60,8 @@ DHD bool operator!=(Dual a, Dual b) { return a.v != b.v; }
 
 DHD Dual sqrt(Dual a)
 {
-    const double s = ::sqrt(a.v);
-    return Dual(s, a.d / (2.0 * s));
+    const double s = sq(a.v);
+    return Dual(s, dv(a.d, 2.0 * s));
 }
 
 DHD Dual fabs(Dual a) { return (a.v < 0.0) ? -a : a; }
@@ -69,8 +71,8 @@ DHD Dual fmin(Dual a, Dual b) { return (b.v < a.v) ? b : a; }
 /* x^y with a constant exponent: d = y * x^y / x * dx. */
 DHD Dual pow(Dual x, Dual y)
 {
-    const double p = ::pow(x.v, y.v);
-    return Dual(p, y.v * (p / x.v) * x.d);
+    const double p = pw(x.v, y.v);
+    return Dual(p, y.v * dv(p, x.v) * x.d);
 }
 
 }  // namespace hydro

@@ -7,13 +7,14 @@
 #include <cuda_runtime.h>
 
 #include "fp64_int.cuh"
+#include "pow_int.cuh"
 #include "hydro_gpu.h"
 
 using namespace hydro;
 
 namespace {
 
-/* op 0: a / b, op 1: sqrt(a).  fast = the integer form where it applies
+/* op 0: a / b, op 1: sqrt(a), op 2: pow(a, b).  fast = the integer form where it applies
  * (else the hardware result), hw = the hardware operation, ok = 1 where the
  * integer form applied. */
 __global__ void fx_eval_kernel(int op, long long n, const double *a, const double *b,
@@ -27,10 +28,14 @@ __global__ void fx_eval_kernel(int op, long long n, const double *a, const doubl
             f = fx::div_fast(a[i], b[i], k);
             hw[i] = fx::div_hw(a[i], b[i]);
             fast[i] = k ? f : dv(a[i], b[i]);
-        } else {
+        } else if (op == 1) {
             f = fx::sqrt_fast(a[i], k);
             hw[i] = fx::sqrt_hw(a[i]);
             fast[i] = k ? f : sq(a[i]);
+        } else {
+            f = fx::pow_fast(a[i], b[i], k);
+            hw[i] = fx::pow_hw(a[i], b[i]);
+            fast[i] = k ? f : pw(a[i], b[i]);
         }
         ok[i] = k ? 1 : 0;
     }
@@ -45,7 +50,8 @@ void hydro_fx_eval_host(int op, long long n, const double *a, const double *b, d
 {
     for (long long i = 0; i < n; i++) {
         bool k;
-        out[i] = (op == 0) ? fx::div_fast(a[i], b[i], k) : fx::sqrt_fast(a[i], k);
+        out[i] = (op == 0) ? fx::div_fast(a[i], b[i], k)
+               : (op == 1) ? fx::sqrt_fast(a[i], k) : fx::pow_fast(a[i], b[i], k);
         ok[i] = k ? 1 : 0;
     }
 }
@@ -63,7 +69,7 @@ int hydro_gpu_fx_eval(int device, int op, long long n, const double *a, const do
     double *da = (double *) slab, *db = da + n, *df = db + n, *dh = df + n;
     unsigned char *dk = (unsigned char *) (dh + n);
     e = cudaMemcpy(da, a, nb, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemcpy(db, op == 0 ? b : a, nb, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(db, op == 1 ? a : b, nb, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) {
         fx_eval_kernel<<<4 * 152, 256>>>(op, n, da, db, df, dh, dk);
         e = cudaGetLastError();

@@ -9,10 +9,14 @@
  * of the total energy (cons_to_prim_2d_guarded) and for the compensated
  * conserved totals.
  */
-#include "mh2d_launch.cuh"
+#include "mh2d_lim.cuh"
 
 namespace hydro {
 
+HYDRO_MH2D_INSTANTIATE(float, LIM_MINMOD, 0)
+HYDRO_MH2D_INSTANTIATE(float, LIM_MINMOD, 1)
+HYDRO_MH2D_INSTANTIATE(float, LIM_VAN_LEER, 0)
+HYDRO_MH2D_INSTANTIATE(float, LIM_MC, 0)
 template int mh2d_resident_ctas<float>(int, int, int);
 template cudaError_t mh2d_launch_batch_step<float>(const Mh2dBatchArgs<float> &, int, int, int, cudaStream_t);
 template cudaError_t mh2d_launch_step<float>(const Mh2dArgs<float> &, int, cudaStream_t);

@@ -13,7 +13,8 @@
  *                           with Neumaier compensation (drift diagnostics);
  *   convert_kernel          FP64 <-> FP32 copies for the FP32 state form.
  *
- * Included by mh2d.cu (FP64, --fmad=false) and mh2d_fp32.cu (FP32).
+ * Included by mh2d.cu (FP64, --fmad=false), the per-limiter FP64 units
+ * mh2d_lim_*.cu and mh2d_fp32.cu (FP32).
  */
 #ifndef HYDRO_GPU_MH2D_LAUNCH_CUH
 #define HYDRO_GPU_MH2D_LAUNCH_CUH
@@ -129,26 +130,31 @@ __global__ void mh2d_ghost_sound_speed_kernel(const Mh2dArgs<R> a, int buf, int 
 
 /* ------------------------------------------------------------- launchers */
 
+/*
+ * Per-limiter launchers.  Their definitions (mh2d_lim.cuh) are explicitly
+ * instantiated in one translation unit per (precision, limiter) --
+ * mh2d_lim_{minmod,vanleer,mc}.cu for FP64, mh2d_fp32.cu for FP32 -- so that
+ * the step kernels of the three limiters compile in parallel.
+ */
 template <class R, int LIM, int FIRST_ORDER>
-static cudaError_t launch_step_lim(const Mh2dArgs<R> &a, int grid, cudaStream_t s)
-{
-    if (a.gravity != 0.0)
-        mh2d_step_kernel<R, LIM, MH2D_THREADS, FIRST_ORDER, false, true><<<grid, MH2D_THREADS, 0, s>>>(a);
-    else
-        mh2d_step_kernel<R, LIM, MH2D_THREADS, FIRST_ORDER><<<grid, MH2D_THREADS, 0, s>>>(a);
-    return cudaGetLastError();
-}
+cudaError_t mh2d_launch_step_lim(const Mh2dArgs<R> &a, int grid, cudaStream_t s);
+template <class R, int LIM>
+cudaError_t mh2d_launch_tape_lim(const Mh2dArgs<R> &a, int grid, cudaStream_t s);
+template <class R, int LIM, int FIRST_ORDER>
+cudaError_t mh2d_launch_batch_lim(const Mh2dBatchArgs<R> &b, int grid, cudaStream_t s);
+template <class R, int LIM, int FIRST_ORDER>
+cudaError_t mh2d_step_occupancy(int *per_sm);
 
 template <class R>
 cudaError_t mh2d_launch_step(const Mh2dArgs<R> &a, int limiter, cudaStream_t s)
 {
     const int n_items = ((a.nx + a.strip_w - 1) / a.strip_w) * ((a.ny + a.chunk_h - 1) / a.chunk_h);
     const int grid = (a.grid_ctas > 0 && a.grid_ctas < n_items) ? a.grid_ctas : n_items;
-    if (a.first_order) return launch_step_lim<R, LIM_MINMOD, 1>(a, grid, s);
+    if (a.first_order) return mh2d_launch_step_lim<R, LIM_MINMOD, 1>(a, grid, s);
     switch (limiter) {
-    case LIM_MINMOD: return launch_step_lim<R, LIM_MINMOD, 0>(a, grid, s);
-    case LIM_VAN_LEER: return launch_step_lim<R, LIM_VAN_LEER, 0>(a, grid, s);
-    default: return launch_step_lim<R, LIM_MC, 0>(a, grid, s);
+    case LIM_MINMOD: return mh2d_launch_step_lim<R, LIM_MINMOD, 0>(a, grid, s);
+    case LIM_VAN_LEER: return mh2d_launch_step_lim<R, LIM_VAN_LEER, 0>(a, grid, s);
+    default: return mh2d_launch_step_lim<R, LIM_MC, 0>(a, grid, s);
     }
 }
 
@@ -159,11 +165,10 @@ cudaError_t mh2d_launch_step_tape(const Mh2dArgs<R> &a, int limiter, cudaStream_
     const int n_items = ((a.nx + a.strip_w - 1) / a.strip_w) * ((a.ny + a.chunk_h - 1) / a.chunk_h);
     const int grid = (a.grid_ctas > 0 && a.grid_ctas < n_items) ? a.grid_ctas : n_items;
     switch (limiter) {
-    case LIM_MINMOD: mh2d_step_kernel<R, LIM_MINMOD, MH2D_THREADS, 0, true><<<grid, MH2D_THREADS, 0, s>>>(a); break;
-    case LIM_VAN_LEER: mh2d_step_kernel<R, LIM_VAN_LEER, MH2D_THREADS, 0, true><<<grid, MH2D_THREADS, 0, s>>>(a); break;
-    default: mh2d_step_kernel<R, LIM_MC, MH2D_THREADS, 0, true><<<grid, MH2D_THREADS, 0, s>>>(a); break;
+    case LIM_MINMOD: return mh2d_launch_tape_lim<R, LIM_MINMOD>(a, grid, s);
+    case LIM_VAN_LEER: return mh2d_launch_tape_lim<R, LIM_VAN_LEER>(a, grid, s);
+    default: return mh2d_launch_tape_lim<R, LIM_MC>(a, grid, s);
     }
-    return cudaGetLastError();
 }
 
 template <class R>
@@ -194,22 +199,15 @@ cudaError_t mh2d_launch_materialize(const Mh2dArgs<R> &a, int buf, R *const out[
     return cudaGetLastError();
 }
 
-template <class R, int LIM, int FIRST_ORDER>
-static cudaError_t launch_batch_lim(const Mh2dBatchArgs<R> &b, int grid, cudaStream_t s)
-{
-    mh2d_batch_step_kernel<R, LIM, MH2D_THREADS, FIRST_ORDER><<<grid, MH2D_THREADS, 0, s>>>(b);
-    return cudaGetLastError();
-}
-
 template <class R>
 cudaError_t mh2d_launch_batch_step(const Mh2dBatchArgs<R> &b, int limiter, int first_order, int grid,
                                    cudaStream_t s)
 {
-    if (first_order) return launch_batch_lim<R, LIM_MINMOD, 1>(b, grid, s);
+    if (first_order) return mh2d_launch_batch_lim<R, LIM_MINMOD, 1>(b, grid, s);
     switch (limiter) {
-    case LIM_MINMOD: return launch_batch_lim<R, LIM_MINMOD, 0>(b, grid, s);
-    case LIM_VAN_LEER: return launch_batch_lim<R, LIM_VAN_LEER, 0>(b, grid, s);
-    default: return launch_batch_lim<R, LIM_MC, 0>(b, grid, s);
+    case LIM_MINMOD: return mh2d_launch_batch_lim<R, LIM_MINMOD, 0>(b, grid, s);
+    case LIM_VAN_LEER: return mh2d_launch_batch_lim<R, LIM_VAN_LEER, 0>(b, grid, s);
+    default: return mh2d_launch_batch_lim<R, LIM_MC, 0>(b, grid, s);
     }
 }
 
@@ -219,14 +217,10 @@ int mh2d_resident_ctas(int limiter, int first_order, int device)
 {
     int per_sm = 0, sms = 0;
     cudaError_t e;
-    if (first_order)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mh2d_step_kernel<R, LIM_MINMOD, MH2D_THREADS, 1>, MH2D_THREADS, 0);
-    else if (limiter == LIM_MINMOD)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mh2d_step_kernel<R, LIM_MINMOD, MH2D_THREADS, 0>, MH2D_THREADS, 0);
-    else if (limiter == LIM_VAN_LEER)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mh2d_step_kernel<R, LIM_VAN_LEER, MH2D_THREADS, 0>, MH2D_THREADS, 0);
-    else
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mh2d_step_kernel<R, LIM_MC, MH2D_THREADS, 0>, MH2D_THREADS, 0);
+    if (first_order) e = mh2d_step_occupancy<R, LIM_MINMOD, 1>(&per_sm);
+    else if (limiter == LIM_MINMOD) e = mh2d_step_occupancy<R, LIM_MINMOD, 0>(&per_sm);
+    else if (limiter == LIM_VAN_LEER) e = mh2d_step_occupancy<R, LIM_VAN_LEER, 0>(&per_sm);
+    else e = mh2d_step_occupancy<R, LIM_MC, 0>(&per_sm);
     if (e != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess)
         return 0;
     return per_sm * sms;

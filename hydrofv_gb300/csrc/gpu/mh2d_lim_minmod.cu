@@ -1,0 +1,15 @@
+/*
+ * mh2d_lim_minmod.cu -- FP64 step kernels with the minmod limiter: single grid
+ * (with and without gravity), adjoint tape and batched forms.
+ *
+ * Compiled with --fmad=false: the FP64 path must issue the same IEEE
+ * operations as the reference CPU code, which never contracts a*b+c.
+ */
+#include "mh2d_lim.cuh"
+
+namespace hydro {
+
+HYDRO_MH2D_INSTANTIATE(double, LIM_MINMOD, 0)
+template cudaError_t mh2d_launch_tape_lim<double, LIM_MINMOD>(const Mh2dArgs<double> &, int, cudaStream_t);
+
+}  // namespace hydro

@@ -28,6 +28,7 @@
 #include <string.h>
 
 #include "fp64_int.cuh"
+#include "pow_int.cuh"
 #ifdef __cplusplus
 #include <cmath>
 using std::fabs;
@@ -170,8 +171,8 @@ HD R guess_p(const GasConst<R> &c, R rho_L, R u_L, R p_L, R a_L,
         pg = ppv;
     } else if (ppv < p_min) {
         pg = dv(a_L + a_R - c.half_gm1 * (u_R - u_L),
-                dv(a_L, pow(p_L, c.half_gm1_g)) + dv(a_R, pow(p_R, c.half_gm1_g)));
-        pg = pow(pg, c.g_half_gm1);
+                dv(a_L, pw(p_L, c.half_gm1_g)) + dv(a_R, pw(p_R, c.half_gm1_g)));
+        pg = pw(pg, c.g_half_gm1);
     } else {
         const R gL = sq(dv(dv(R(2), c.gp1 * rho_L), ppv + p_L * c.gm1_gp1));
         const R gR = sq(dv(dv(R(2), c.gp1 * rho_R), ppv + p_R * c.gm1_gp1));
@@ -190,11 +191,11 @@ HD void sample_right_vacuum(const GasConst<R> &c, R rho, R u, R v, R p, R a, R S
     const R front = u + R(2) * a / c.gm1;
     if (S < front) {
         R tmp = c.two_gp1 + (u - S) * c.gm1 / (c.gp1 * a);
-        tmp = pow(tmp, c.two_gm1);
+        tmp = pw(tmp, c.two_gm1);
         o[0] = rho * tmp;
         o[1] = (a + c.half_gm1 * u + S) * R(2) / c.gp1;
         o[2] = v;
-        o[3] = p * pow(tmp, c.gamma);
+        o[3] = p * pw(tmp, c.gamma);
     } else {
         o[0] = R(0); o[1] = R(0); o[2] = R(0); o[3] = R(0);
     }
@@ -207,11 +208,11 @@ HD void sample_left_vacuum(const GasConst<R> &c, R rho, R u, R v, R p, R a, R S,
     const R front = u - R(2) * a / c.gm1;
     if (S > front) {
         R tmp = c.two_gp1 - (u - S) * c.gm1 / (c.gp1 * a);
-        tmp = pow(tmp, c.two_gm1);
+        tmp = pw(tmp, c.two_gm1);
         o[0] = rho * tmp;
         o[1] = (-a + c.half_gm1 * u + S) * R(2) / c.gp1;
         o[2] = v;
-        o[3] = p * pow(tmp, c.gamma);
+        o[3] = p * pw(tmp, c.gamma);
     } else {
         o[0] = R(0); o[1] = R(0); o[2] = R(0); o[3] = R(0);
     }
@@ -294,18 +295,18 @@ HD int hllc_classify(const GasConst<R> &c, R rho_L, R u_L, R p_L, R rho_R, R u_R
 template <class R>
 HD R guess_p_trrs_z(const GasConst<R> &c, R u_L, R p_L, R a_L, R u_R, R p_R, R a_R, R &zL, R &zR)
 {
-    zL = pow(p_L, c.half_gm1_g);
-    zR = pow(p_R, c.half_gm1_g);
+    zL = pw(p_L, c.half_gm1_g);
+    zR = pw(p_R, c.half_gm1_g);
     const R pg = dv(a_L + a_R - c.half_gm1 * (u_R - u_L), dv(a_L, zL) + dv(a_R, zR));
-    return pow(pg, c.g_half_gm1);
+    return pw(pg, c.g_half_gm1);
 }
 
 template <class R>
 HD R guess_p_trrs(const GasConst<R> &c, R u_L, R p_L, R a_L, R u_R, R p_R, R a_R)
 {
     const R pg = dv(a_L + a_R - c.half_gm1 * (u_R - u_L),
-                    dv(a_L, pow(p_L, c.half_gm1_g)) + dv(a_R, pow(p_R, c.half_gm1_g)));
-    return pow(pg, c.g_half_gm1);
+                    dv(a_L, pw(p_L, c.half_gm1_g)) + dv(a_R, pw(p_R, c.half_gm1_g)));
+    return pw(pg, c.g_half_gm1);
 }
 
 template <class R>
@@ -466,7 +467,7 @@ HD R exact_fK(const GasConst<R> &c, R rho, R p, R a, R ps)
         const R B = p * c.gm1_gp1;
         return (ps - p) * sqrt(A / (ps + B));
     }
-    return R(2) * a * (pow((ps / p), c.gm1_2g) - R(1)) / c.gm1;
+    return R(2) * a * (pw((ps / p), c.gm1_2g) - R(1)) / c.gm1;
 }
 
 /* Derivative; the shock branch's (B - p*) follows the reference
@@ -479,7 +480,7 @@ HD R exact_dfK(const GasConst<R> &c, R rho, R p, R a, R ps)
         const R B = p * c.gm1_gp1;
         return (R(1) - R(0.5) * (ps - p) / (B - ps)) * sqrt(A / (B + ps));
     }
-    return pow(ps / p, c.neg_gp1_2g) / (p * a);
+    return pw(ps / p, c.neg_gp1_2g) / (p * a);
 }
 
 template <class R>
@@ -565,15 +566,15 @@ HD void exact_sample(const GasConst<R> &c, R rho_L, R u_L, R p_L, R a_L,
         }
         const R SH = u_L - a_L;
         if (S < SH) { o[0] = rho_L; o[1] = u_L; o[2] = p_L; return; }
-        const R as = a_L * pow(ps / p_L, c.gm1_2g);
+        const R as = a_L * pw(ps / p_L, c.gm1_2g);
         if (S < us - as) {
-            const R cm = pow((c.two_gp1 + (u_L - S) * (c.gm1 / (a_L * c.gp1))), c.two_gm1);
+            const R cm = pw((c.two_gp1 + (u_L - S) * (c.gm1 / (a_L * c.gp1))), c.two_gm1);
             o[0] = rho_L * cm;
             o[1] = c.two_gp1 * (a_L + R(0.5) * u_L * c.gm1 + S);
-            o[2] = p_L * pow(cm, c.gamma);
+            o[2] = p_L * pw(cm, c.gamma);
             return;
         }
-        o[0] = rho_L * pow(ps / p_L, c.inv_g);
+        o[0] = rho_L * pw(ps / p_L, c.inv_g);
         o[1] = us;
         o[2] = ps;
         return;
@@ -590,15 +591,15 @@ HD void exact_sample(const GasConst<R> &c, R rho_L, R u_L, R p_L, R a_L,
     }
     const R SH = u_R + a_R;
     if (S > SH) { o[0] = rho_R; o[1] = u_R; o[2] = p_R; return; }
-    const R as = a_R * pow(ps / p_R, c.gm1_2g);
+    const R as = a_R * pw(ps / p_R, c.gm1_2g);
     if (S > us + as) {
-        const R cm = pow((c.two_gp1 - (u_R - S) * c.gm1 / (a_R * c.gp1)), c.two_gm1);
+        const R cm = pw((c.two_gp1 - (u_R - S) * c.gm1 / (a_R * c.gp1)), c.two_gm1);
         o[0] = rho_R * cm;
         o[1] = c.two_gp1 * (-a_R + R(0.5) * u_R * c.gm1 + S);
-        o[2] = p_R * pow(cm, c.gamma);
+        o[2] = p_R * pw(cm, c.gamma);
         return;
     }
-    o[0] = rho_R * pow(ps / p_R, c.inv_g);
+    o[0] = rho_R * pw(ps / p_R, c.inv_g);
     o[1] = us;
     o[2] = ps;
 }

@@ -337,9 +337,9 @@ void hydro_ad_recon_forced(int limiter, int dir, double gamma, double dtA, const
                            const double w0[4], const double wp[4], int code, double lo[4],
                            double hi[4], int *natural_code);
 
-/* The integer-pipe FP64 division (op 0: a[i] / b[i]) and square root
- * (op 1: sqrt(a[i])) the FP64 kernels use in place of the FP64-pipe
- * sequences.  Host build: out[i] = the integer form, ok[i] = 1 where its
+/* The integer-pipe FP64 division (op 0: a[i] / b[i]), square root
+ * (op 1: sqrt(a[i])) and power (op 2: pow(a[i], b[i])) the FP64 kernels use
+ * in place of the FP64-pipe sequences.  Host build: out[i] = the integer form, ok[i] = 1 where its
  * fast path applied (elsewhere out[i] is meaningless).  Device build:
  * fast[i] = what the kernels compute, hw[i] = the hardware operation,
  * ok[i] as above; returns a cudaError_t. */

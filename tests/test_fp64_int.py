@@ -174,3 +174,99 @@ def test_gpu_sqrt_is_bitwise_ieee():
     assert _same_bits(fast, hw).all()
     assert _same_bits(hw, np.sqrt(np.where(x < 0, np.nan, x))).all()
     assert ok[:1 << 22].all()
+
+
+# ---------------------------------------------------------------- pow
+
+# exponents the solvers use: (g-1)/2g, 2g/(g-1), 2/(g-1), g, 1/g, (g-1)/2g,
+# -(g+1)/2g for g = 1.4 and 5/3
+SOLVER_EXPONENTS = [0.2 / 1.4, 1.4 / 0.2, 2 / 0.4, 1.4, 1 / 1.4, 0.4 / 2.8, -2.4 / 2.8,
+                    (1 / 3) / (5 / 3), (5 / 3) / (1 / 3), 2 / (2 / 3), 5 / 3, 0.6, -(8 / 3) / (10 / 3)]
+
+
+def _correctly_rounded_pow(x, y):
+    mp = pytest.importorskip("mpmath")
+    mp.mp.prec = 200
+    return np.array([float(mp.power(mp.mpf(a), mp.mpf(b))) for a, b in zip(x, y)])
+
+
+def test_host_pow_is_correctly_rounded_on_solver_exponents():
+    rng = np.random.default_rng(11)
+    x = np.exp(rng.uniform(-12, 12, 1500 * len(SOLVER_EXPONENTS)))
+    y = np.repeat(SOLVER_EXPONENTS, 1500)
+    out, ok = h.fx_eval_host(2, x, y)
+    assert ok.all()
+    assert np.array_equal(out.view(np.uint64), _correctly_rounded_pow(x, y).view(np.uint64))
+
+
+def test_host_pow_is_correctly_rounded_on_wide_operands():
+    rng = np.random.default_rng(12)
+    x = np.concatenate([np.exp(rng.uniform(-700, 700, 6000)), rng.uniform(0.5, 2.0, 6000),
+                        1.0 + rng.uniform(-1e-9, 1e-9, 2000)])
+    y = np.concatenate([rng.uniform(-1, 1, 6000), rng.uniform(-40, 40, 6000), rng.uniform(-500, 500, 2000)])
+    out, ok = h.fx_eval_host(2, x, y)
+    assert ok.mean() > 0.99
+    ref = _correctly_rounded_pow(x[ok], y[ok])
+    assert np.array_equal(out[ok].view(np.uint64), ref.view(np.uint64))
+
+
+def test_host_pow_table_boundaries_and_exact_results():
+    x = np.array([1.0 + k / 128 for k in range(129)] + [np.nextafter(1.0 + k / 128, 0) for k in range(1, 129)]
+                 + [1.0 + (2 * k + 1) / 256 for k in range(128)] + [np.nextafter(1.0, 2.0), np.nextafter(1.0, 0.0)])
+    for yv in (0.2, 7.0, -3.5, 0.5, 100.0, -300.0, 511.0):
+        y = np.full(x.size, yv)
+        out, ok = h.fx_eval_host(2, x, y)
+        with np.errstate(all="ignore"):
+            normal = np.abs(np.log2(x) * yv) < 1020      # results that stay normal
+        assert ok[normal].mean() > 0.95 and not ok[~normal].any()   # short mantissas: midpoints
+        ref = _correctly_rounded_pow(x[ok], y[ok])
+        assert np.array_equal(out[ok].view(np.uint64), ref.view(np.uint64))
+    # exact powers come out exact
+    out, ok = h.fx_eval_host(2, np.array([4.0, 2.0, 9.0, 0.25, 1024.0, 1.0]), np.array([0.5, 10.0, 0.5, -2.0, 0.1, 123.4]))
+    assert ok.all() and np.array_equal(out, [2.0, 1024.0, 3.0, 16.0, 2.0, 1.0])
+
+
+def test_host_pow_agrees_with_the_c_library_pow():
+    """glibc's pow (what the reference calls) is correctly rounded in all but
+    a small fraction of cases; where it differs, by one ulp."""
+    import ctypes
+    import ctypes.util
+    libm = ctypes.CDLL(ctypes.util.find_library("m"))
+    libm.pow.restype = ctypes.c_double
+    libm.pow.argtypes = [ctypes.c_double, ctypes.c_double]
+    rng = np.random.default_rng(13)
+    x = np.exp(rng.uniform(-6, 6, 4000 * len(SOLVER_EXPONENTS)))
+    y = np.repeat(SOLVER_EXPONENTS, 4000)
+    out, ok = h.fx_eval_host(2, x, y)
+    assert ok.all()
+    ref = np.array([libm.pow(a, b) for a, b in zip(x, y)])
+    d = np.abs(out.view(np.int64) - ref.view(np.int64))
+    assert d.max() <= 1
+    assert (d != 0).mean() < 5e-3
+
+
+def test_host_pow_special_operands_take_the_fallback():
+    x = np.array([0.0, -1.0, np.inf, np.nan, 5e-324, 2.0, 2.0, 2.0, 2.0, 1e300, 1e-300, 2.0, 2.0])
+    y = np.array([2.0, 2.0, 2.0, 2.0, 2.0, 0.0, 512.0, 1023.9, -1022.5, 2.0, 2.0, np.nan, 1e-320])
+    _, ok = h.fx_eval_host(2, x, y)
+    assert not ok.any()
+
+
+@pytest.mark.gpu
+def test_gpu_pow_matches_the_host_build_bitwise():
+    """The device build is the same integer algorithm (no seeds): bit-identical
+    to the host build wherever its fast path applies; elsewhere it is the
+    hardware pow."""
+    rng = np.random.default_rng(14)
+    x = np.concatenate([np.exp(rng.uniform(-12, 12, 1 << 21)), np.exp(rng.uniform(-700, 700, 1 << 20)),
+                        np.array([0.0, -1.0, np.inf, np.nan, 5e-324, 2.0, 2.0, 1e300])])
+    y = np.concatenate([rng.choice(SOLVER_EXPONENTS, 1 << 21), rng.uniform(-1, 1, 1 << 20),
+                        np.array([2.0, 2.0, 2.0, 2.0, 2.0, 0.0, 512.0, 2.0])])
+    fast, hw, ok = h.gpu_fx_eval(2, x, y)
+    host, hok = h.fx_eval_host(2, x, y)
+    assert np.array_equal(ok, hok)
+    assert np.array_equal(fast[ok].view(np.uint64), host[ok].view(np.uint64))
+    assert _same_bits(fast[~ok], hw[~ok]).all()
+    # the hardware pow is within a few ulps of the correctly rounded result
+    d = np.abs(fast[ok].view(np.int64) - hw[ok].view(np.int64))
+    assert d.max() <= 4
