@@ -169,6 +169,15 @@ struct Mh2dShared {
     double red[2][NT / 32];
 };
 
+/* The vacuum / vacuum-generation flux, out of line: rare, and kept out of
+ * the finish loop's code. */
+template <class R>
+__device__ __noinline__ void vacuum_flux_dev(const GasConst<R> &c, R rl, R ul, R vl, R pl, R al,
+                                             R rr, R ur, R vr, R pr, R ar, R F[4])
+{
+    hllc_vacuum_flux(c, rl, ul, vl, pl, al, rr, ur, vr, pr, ar, F);
+}
+
 /*
  * Solve faces 0..nF-1 of the batch in sm.FL / sm.FR (normal velocity in
  * slot 1) with the HLLC flux, as three dense passes over the CTA:
@@ -235,7 +244,7 @@ __device__ __forceinline__ int solve_faces(Mh2dShared<R, NT> &sm, const GasConst
             *tc.field(f, TAPE_REG) = (R) sm.reg[f];
         }
         if (sm.reg[f] == PREG_VACUUM) {
-            hllc_vacuum_flux(gas, rl, ul, vl, pl, sm.aL[f], rr, ur, vr, pr, sm.aR[f], F);
+            vacuum_flux_dev(gas, rl, ul, vl, pl, sm.aL[f], rr, ur, vr, pr, sm.aR[f], F);
         } else {
             const int rc = hllc_finish(gas, rl, ul, vl, pl, sm.aL[f], rr, ur, vr, pr, sm.aR[f],
                                        sm.pg[f], F);

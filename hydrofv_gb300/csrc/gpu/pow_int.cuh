@@ -165,6 +165,15 @@ FXHD double pow_fast(double x, double y, bool &ok)
 
 #if defined(__CUDACC__)
 static __device__ __noinline__ double pow_hw(double x, double y) { return pow(x, y); }
+
+/* The device pow, out of line (one copy per kernel instead of one per call
+ * site), like the divide and square root of fp64_int.cuh. */
+static __device__ __noinline__ double pow_dev(double x, double y)
+{
+    bool ok;
+    const double r = pow_fast(x, y, ok);
+    return ok ? r : pow_hw(x, y);
+}
 #endif
 
 }  // namespace fx
@@ -178,9 +187,7 @@ FXHD R pw(R x, R y) { return pow(x, y); }
 FXHD double pw(double x, double y)
 {
 #if defined(__CUDA_ARCH__)
-    bool ok;
-    const double r = fx::pow_fast(x, y, ok);
-    return ok ? r : fx::pow_hw(x, y);
+    return fx::pow_dev(x, y);
 #else
     return pow(x, y);
 #endif
