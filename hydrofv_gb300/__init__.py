@@ -766,6 +766,7 @@ def ad_recon_forced(limiter, direction, gamma, dtA, wm, w0, wp, code):
 
 
 def _fx_args(op, a, b):
+    """Operands of the fx evaluations (op 1, sqrt, takes a alone)."""
     a = np.ascontiguousarray(a, dtype=np.float64).ravel()
     b = a if op == 1 else np.ascontiguousarray(b, dtype=np.float64).ravel()
     if b.shape != a.shape:

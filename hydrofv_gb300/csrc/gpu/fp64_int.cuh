@@ -222,6 +222,25 @@ FXHD double sqrt_fast(double x, bool &ok)
     return from_bits(res);
 }
 
+/*
+ * The limiter's sign test a * b <= 0 decided on the bits where that is exact
+ * without the multiply: 1 (true), 0 (false), or -1 when it is not decided
+ * here (a NaN or infinite operand, a subnormal one, or a product of normal
+ * operands small enough to underflow to zero: the caller evaluates the FP64
+ * expression).  A zero times a finite operand is a signed zero (true);
+ * otherwise the product's sign is the XOR of the signs, and for
+ * ea + eb >= 973 the product is at least 2^-1074 in magnitude.
+ */
+FXHD int product_nonpositive(u64 ua, u64 ub)
+{
+    const u64 aa = ua & ~SIGN, ab = ub & ~SIGN;
+    const unsigned ea = (unsigned) (aa >> 52), eb = (unsigned) (ab >> 52);
+    if (ea == 0x7ffu || eb == 0x7ffu) return -1;
+    if (aa == 0ull || ab == 0ull) return 1;
+    if (ea == 0u || eb == 0u || ea + eb < 973u) return -1;
+    return (int) ((ua ^ ub) >> 63);
+}
+
 #if defined(__CUDACC__)
 /* Hardware operations for the cases the fast paths leave out; kept out of
  * line so that the fast path's call sites stay small. */

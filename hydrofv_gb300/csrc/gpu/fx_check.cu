@@ -8,6 +8,7 @@
 
 #include "fp64_int.cuh"
 #include "pow_int.cuh"
+#include "numerics.cuh"
 #include "hydro_gpu.h"
 
 using namespace hydro;
@@ -16,7 +17,9 @@ namespace {
 
 /* op 0: a / b, op 1: sqrt(a), op 2: pow(a, b).  fast = the integer form where it applies
  * (else the hardware result), hw = the hardware operation, ok = 1 where the
- * integer form applied. */
+ * integer form applied.  op 3, 4, 5: the minmod, van Leer and MC slope
+ * limiters L(a, b) as the kernels evaluate them (fast = hw; ok = 1 where the
+ * sign test was decided on the bits). */
 __global__ void fx_eval_kernel(int op, long long n, const double *a, const double *b,
                                double *fast, double *hw, unsigned char *ok)
 {
@@ -32,10 +35,16 @@ __global__ void fx_eval_kernel(int op, long long n, const double *a, const doubl
             f = fx::sqrt_fast(a[i], k);
             hw[i] = fx::sqrt_hw(a[i]);
             fast[i] = k ? f : sq(a[i]);
-        } else {
+        } else if (op == 2) {
             f = fx::pow_fast(a[i], b[i], k);
             hw[i] = fx::pow_hw(a[i], b[i]);
             fast[i] = k ? f : pw(a[i], b[i]);
+        } else {
+            k = fx::product_nonpositive(fx::bits(a[i]), fx::bits(b[i])) >= 0;
+            f = (op == 3) ? limit_slope<LIM_MINMOD>(a[i], b[i])
+              : (op == 4) ? limit_slope<LIM_VAN_LEER>(a[i], b[i]) : limit_slope<LIM_MC>(a[i], b[i]);
+            fast[i] = f;
+            hw[i] = f;
         }
         ok[i] = k ? 1 : 0;
     }
@@ -49,9 +58,18 @@ void hydro_fx_eval_host(int op, long long n, const double *a, const double *b, d
                         unsigned char *ok)
 {
     for (long long i = 0; i < n; i++) {
-        bool k;
-        out[i] = (op == 0) ? fx::div_fast(a[i], b[i], k)
-               : (op == 1) ? fx::sqrt_fast(a[i], k) : fx::pow_fast(a[i], b[i], k);
+        bool k = true;
+        if (op <= 2) {
+            out[i] = (op == 0) ? fx::div_fast(a[i], b[i], k)
+                   : (op == 1) ? fx::sqrt_fast(a[i], k) : fx::pow_fast(a[i], b[i], k);
+        } else if (op == 6) {
+            /* the bit-level sign test itself: out = 1, 0 or -1 */
+            out[i] = (double) fx::product_nonpositive(fx::bits(a[i]), fx::bits(b[i]));
+        } else {
+            /* host builds evaluate the limiters' FP64 expressions */
+            out[i] = (op == 3) ? limit_slope<LIM_MINMOD>(a[i], b[i])
+                   : (op == 4) ? limit_slope<LIM_VAN_LEER>(a[i], b[i]) : limit_slope<LIM_MC>(a[i], b[i]);
+        }
         ok[i] = k ? 1 : 0;
     }
 }
@@ -69,6 +87,7 @@ int hydro_gpu_fx_eval(int device, int op, long long n, const double *a, const do
     double *da = (double *) slab, *db = da + n, *df = db + n, *dh = df + n;
     unsigned char *dk = (unsigned char *) (dh + n);
     e = cudaMemcpy(da, a, nb, cudaMemcpyHostToDevice);
+    if (op < 0 || op > 5) e = cudaErrorInvalidValue;
     if (e == cudaSuccess) e = cudaMemcpy(db, op == 1 ? a : b, nb, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) {
         fx_eval_kernel<<<4 * 152, 256>>>(op, n, da, db, df, dh, dk);

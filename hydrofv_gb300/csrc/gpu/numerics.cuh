@@ -31,6 +31,7 @@
 #include "pow_int.cuh"
 #ifdef __cplusplus
 #include <cmath>
+#include <type_traits>
 using std::fabs;
 using std::fmin;
 using std::pow;
@@ -121,9 +122,32 @@ HD R sound_speed(const GasConst<R> &c, R rho, R p)
     return sq(dv(c.gamma * p, rho));
 }
 
+/*
+ * On the device, for double, the sign test and the minima are decided on the
+ * bits (fx::product_nonpositive; the minimum of two positive doubles is the
+ * minimum of their bit patterns), leaving the FP64 pipe a + b and the two
+ * scalings.  The results are those of the expressions below bit for bit;
+ * operands the bit test does not decide take the expressions themselves.
+ */
 template <int LIM, class R>
 HD R limit_slope(R a, R b)
 {
+#if defined(__CUDA_ARCH__)
+    if constexpr (std::is_same<R, double>::value) {
+        const fx::u64 ua = fx::bits(a), ub = fx::bits(b);
+        const int t = fx::product_nonpositive(ua, ub);
+        if (t > 0) return R(0);
+        if (t == 0) {
+            const fx::u64 aa = ua & ~fx::SIGN, ab = ub & ~fx::SIGN;
+            if (LIM == LIM_MINMOD) return (aa < ab) ? a : b;
+            if (LIM == LIM_VAN_LEER) return dv(R(2) * a * b, a + b + R(1e-10));
+            const double two_m = 2.0 * fx::from_bits(aa < ab ? aa : ab);     /* 2 fmin(|a|, |b|) */
+            const double avg = ((ua >> 63) ? -0.5 : 0.5) * (a + b);           /* > 0 */
+            const fx::u64 ua2 = fx::bits(avg), ut = fx::bits(two_m);
+            return fx::from_bits((ua2 < ut ? ua2 : ut) | (ua & fx::SIGN));  /* +-fmin(avg, two_m) */
+        }
+    }
+#endif
     if (a * b <= R(0)) return R(0);
     if (LIM == LIM_MINMOD) return (fabs(a) < fabs(b)) ? a : b;
     if (LIM == LIM_VAN_LEER) return dv(R(2) * a * b, a + b + R(1e-10));

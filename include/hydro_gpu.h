@@ -339,7 +339,10 @@ void hydro_ad_recon_forced(int limiter, int dir, double gamma, double dtA, const
 
 /* The integer-pipe FP64 division (op 0: a[i] / b[i]), square root
  * (op 1: sqrt(a[i])) and power (op 2: pow(a[i], b[i])) the FP64 kernels use
- * in place of the FP64-pipe sequences.  Host build: out[i] = the integer form, ok[i] = 1 where its
+ * in place of the FP64-pipe sequences; op 3, 4, 5: the minmod, van Leer and
+ * MC limiters L(a[i], b[i]) (host: the FP64 expressions; device: as the
+ * kernels evaluate them, ok[i] = 1 where the sign test was decided on the
+ * bits); op 6 (host only): that sign test itself (1, 0 or -1).  Host build: out[i] = the integer form, ok[i] = 1 where its
  * fast path applied (elsewhere out[i] is meaningless).  Device build:
  * fast[i] = what the kernels compute, hw[i] = the hardware operation,
  * ok[i] as above; returns a cudaError_t. */

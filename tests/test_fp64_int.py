@@ -270,3 +270,43 @@ def test_gpu_pow_matches_the_host_build_bitwise():
     # the hardware pow is within a few ulps of the correctly rounded result
     d = np.abs(fast[ok].view(np.int64) - hw[ok].view(np.int64))
     assert d.max() <= 4
+
+
+# ---------------------------------------------------------------- limiters
+
+def _slope_pairs(rng, n):
+    """Slope pairs: same and opposite signs over a wide range, ties, zeros of
+    both signs, infinities, NaN, subnormals and products near underflow."""
+    a = rng.normal(size=n) * 10.0 ** rng.uniform(-30, 30, n)
+    b = rng.normal(size=n) * 10.0 ** rng.uniform(-30, 30, n)
+    b[: n // 8] = a[: n // 8] * rng.choice([1.0, 2.0, 0.5, -1.0], n // 8)        # ties and MC kinks
+    sp = np.array([0.0, -0.0, np.inf, -np.inf, np.nan, 5e-324, -2e-310, 1e-160, -3e-170, 1e300, 2.0])
+    a = np.concatenate([a, np.repeat(sp, sp.size)])
+    b = np.concatenate([b, np.tile(sp, sp.size)])
+    return a, b
+
+
+def test_host_bit_sign_test_matches_the_product():
+    rng = np.random.default_rng(21)
+    a, b = _slope_pairs(rng, 200000)
+    t, _ = h.fx_eval_host(6, a, b)
+    with np.errstate(all="ignore"):
+        ref = a * b <= 0.0
+    decided = t >= 0
+    assert np.array_equal(t[decided] == 1, ref[decided])
+    assert decided[:200000].mean() > 0.99
+    finite = np.isfinite(a) & np.isfinite(b)
+    assert not decided[~finite & ((a != 0) | ~np.isfinite(b)) & ((b != 0) | ~np.isfinite(a))].any()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("op", [3, 4, 5], ids=["minmod", "van_leer", "mc"])
+def test_gpu_limiters_match_the_fp64_expressions(op):
+    """The device limiters decide the sign test and the minima on the bits;
+    the results are the host build's FP64 expressions bit for bit."""
+    rng = np.random.default_rng(22 + op)
+    a, b = _slope_pairs(rng, 1 << 21)
+    fast, _, ok = h.gpu_fx_eval(op, a, b)
+    host, _ = h.fx_eval_host(op, a, b)
+    assert _same_bits(fast, host).all()
+    assert ok[: 1 << 21].mean() > 0.99
