@@ -241,6 +241,11 @@ FXHD int product_nonpositive(u64 ua, u64 ub)
     return (int) ((ua ^ ub) >> 63);
 }
 
+/* Ordered key of a non-NaN double's bits: monotone in the value, with +0
+ * and -0 equal. */
+FXHD i64 okey(u64 b) { return (i64) b >= 0 ? (i64) b : -(i64) (b & ~SIGN); }
+FXHD bool nan_bits(u64 b) { return (b & ~SIGN) > 0x7ff0000000000000ull; }
+
 #if defined(__CUDACC__)
 /* Hardware operations for the cases the fast paths leave out; kept out of
  * line so that the fast path's call sites stay small. */
@@ -292,6 +297,35 @@ FXHD double sq(double x)
     return fx::sqrt_dev(x);
 #else
     return sqrt(x);
+#endif
+}
+
+/* Ordered comparisons as the kernels evaluate them: IEEE semantics (false
+ * when either operand is NaN, +0 == -0), on the integer pipes for double on
+ * the device. */
+template <class R>
+FXHD bool lt(R a, R b) { return a < b; }
+
+template <class R>
+FXHD bool le(R a, R b) { return a <= b; }
+
+FXHD bool lt(double a, double b)
+{
+#if defined(__CUDA_ARCH__)
+    const fx::u64 ua = fx::bits(a), ub = fx::bits(b);
+    return !fx::nan_bits(ua) && !fx::nan_bits(ub) && fx::okey(ua) < fx::okey(ub);
+#else
+    return a < b;
+#endif
+}
+
+FXHD bool le(double a, double b)
+{
+#if defined(__CUDA_ARCH__)
+    const fx::u64 ua = fx::bits(a), ub = fx::bits(b);
+    return !fx::nan_bits(ua) && !fx::nan_bits(ub) && fx::okey(ua) <= fx::okey(ub);
+#else
+    return a <= b;
 #endif
 }
 

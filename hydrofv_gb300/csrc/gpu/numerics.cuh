@@ -178,7 +178,7 @@ HD R limit_slope_rt(int lim, R a, R b)
 template <class R>
 HD bool ratio_at_most_two(R p_max, R p_min)
 {
-    if (p_min > R(0)) return p_max <= R(2) * p_min;
+    if (lt(R(0), p_min)) return le(p_max, R(2) * p_min);
     return p_max / p_min <= R(2);
 }
 
@@ -265,7 +265,7 @@ HD void solve_vacuum(const GasConst<R> &c,
 template <class R>
 HD R hllc_q(const GasConst<R> &c, R p_X, R p_star)
 {
-    if (p_star <= p_X) return R(1);
+    if (le(p_star, p_X)) return R(1);
     return sq(R(1) + c.q_coef * (dv(p_star, p_X) - R(1)));
 }
 
@@ -299,16 +299,17 @@ template <class R>
 HD int hllc_classify(const GasConst<R> &c, R rho_L, R u_L, R p_L, R rho_R, R u_R, R p_R,
                      R &a_L, R &a_R, R &ppv)
 {
-    a_L = (rho_L > R(0)) ? sound_speed(c, rho_L, p_L) : R(0);
-    a_R = (rho_R > R(0)) ? sound_speed(c, rho_R, p_R) : R(0);
+    a_L = lt(R(0), rho_L) ? sound_speed(c, rho_L, p_L) : R(0);
+    a_R = lt(R(0), rho_R) ? sound_speed(c, rho_R, p_R) : R(0);
     ppv = R(0);
-    if (rho_L <= R(0) || rho_R <= R(0) || dv((a_L + a_R) * R(2), c.gp1) <= (u_R - u_L))
+    if (le(rho_L, R(0)) || le(rho_R, R(0)) || le(dv((a_L + a_R) * R(2), c.gp1), u_R - u_L))
         return PREG_VACUUM;
-    const R p_min = (p_L > p_R) ? p_R : p_L;
-    const R p_max = (p_L > p_R) ? p_L : p_R;
+    const bool l_above = lt(p_R, p_L);
+    const R p_min = l_above ? p_R : p_L;
+    const R p_max = l_above ? p_L : p_R;
     ppv = R(0.5) * (p_L + p_R) - R(0.125) * (u_R - u_L) * (rho_L + rho_R) * (a_L + a_R);
-    if (ratio_at_most_two(p_max, p_min) && (p_min <= ppv && ppv <= p_max)) return PREG_PVRS;
-    if (ppv < p_min) return PREG_TRRS;
+    if (ratio_at_most_two(p_max, p_min) && (le(p_min, ppv) && le(ppv, p_max))) return PREG_PVRS;
+    if (lt(ppv, p_min)) return PREG_TRRS;
     return PREG_TSRS;
 }
 
@@ -369,16 +370,16 @@ template <class R>
 HD int hllc_finish(const GasConst<R> &c, R rho_L, R u_L, R v_L, R p_L, R a_L,
                    R rho_R, R u_R, R v_R, R p_R, R a_R, R pg, R F[4])
 {
-    const R ps = (pg < c.tol) ? c.tol : pg;
+    const R ps = lt(pg, c.tol) ? c.tol : pg;
     const R S_L = u_L - a_L * hllc_q(c, p_L, ps);
     const R S_R = u_R + a_R * hllc_q(c, p_R, ps);
     const R S_s = dv(p_R - p_L + rho_L * u_L * (S_L - u_L) - rho_R * u_R * (S_R - u_R),
                      rho_L * (S_L - u_L) - rho_R * (S_R - u_R));
     int region;
-    if (R(0) <= S_L) region = 0;
-    else if (S_L <= R(0) && R(0) <= S_s) region = 1;
-    else if (S_s <= R(0) && R(0) <= S_R) region = 2;
-    else if (S_R <= R(0)) region = 3;
+    if (le(R(0), S_L)) region = 0;
+    else if (le(S_L, R(0)) && le(R(0), S_s)) region = 1;
+    else if (le(S_s, R(0)) && le(R(0), S_R)) region = 2;
+    else if (le(S_R, R(0))) region = 3;
     else return DEV_ERR_HLLC_WAVE_SPEED;
     const bool left = region <= 1;
     const R rho = left ? rho_L : rho_R;
