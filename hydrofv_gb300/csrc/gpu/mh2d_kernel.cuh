@@ -28,9 +28,9 @@
  *
  * The update is a gather in the reference's accumulation order
  * U += F_{i-1/2}; U -= F_{i+1/2}; U += G_{j-1/2}; U -= G_{j+1/2}, each term
- * (flux*dt)*area, so no atomics and no scatter races.  The first ghost layer
- * receives its one-sided update too (the reference updates it and the "none"
- * boundary reads it back).  The epilogue converts the new U to W, stores both
+ * (flux*dt)*area (formed once per face), so no atomics and no scatter
+ * races.  The first ghost layer receives its one-sided update too (the
+ * reference updates it and the "none" boundary reads it back).  The epilogue converts the new U to W, stores both
  * and folds a+|u|, a+|v| into CTA maxima that become the next step's dt.
  *
  * Both the state and W are double-buffered (step n reads buffer n&1 and
@@ -185,11 +185,16 @@ __device__ __noinline__ void vacuum_flux_dev(const GasConst<R> &c, R rl, R ul, R
  * on compacted lists (two-rarefaction: three pow; two-shock: five divides
  * and two square roots), and the finish (wave speeds, S*, region flux).
  * Compaction keeps lanes busy where neighbouring faces fall into different
- * regimes, which the one-face-per-thread form serialises.  The flux
- * replaces the left state in sm.FL.  Ends with a barrier.
+ * regimes, which the one-face-per-thread form serialises.  The face's
+ * update term (flux * dt) * area replaces the left state in sm.FL: faces
+ * [0, nXf) are x faces (area Ax), the rest y faces (Ay).  Both cells of a
+ * face add or subtract this one product, so it is formed once per face; the
+ * reference forms the same product for each cell (identical bits).  Ends
+ * with a barrier.
  */
 template <class R, int NT, bool TAPE = false>
 __device__ __forceinline__ int solve_faces(Mh2dShared<R, NT> &sm, const GasConst<R> &gas, int nF,
+                                           int nXf, R dtr, R Ax, R Ay,
                                            const TapeCtx<R> &tc = TapeCtx<R>{})
 {
     const int tid = threadIdx.x;
@@ -250,8 +255,9 @@ __device__ __forceinline__ int solve_faces(Mh2dShared<R, NT> &sm, const GasConst
                                        sm.pg[f], F);
             if (rc) err = rc;
         }
+        const R A = (f < nXf) ? Ax : Ay;
 #pragma unroll
-        for (int q = 0; q < 4; q++) sm.FL[q][f] = F[q];
+        for (int q = 0; q < 4; q++) sm.FL[q][f] = (F[q] * dtr) * A;
     }
     __syncthreads();
     return err;
@@ -374,9 +380,9 @@ __device__ __forceinline__ void mh2d_item(const Mh2dArgs<R> &a, Mh2dShared<R, NT
         int rc;
         if constexpr (TAPE) {
             const TapeCtx<R> tc{ a.tape, a.tape_plane, a.pitch, 0, -1, r_begin - 1, c0 };
-            rc = solve_faces<R, NT, true>(sm, a.gas, sw, tc);
+            rc = solve_faces<R, NT, true>(sm, a.gas, sw, 0, dtr, Ax, Ay, tc);
         } else {
-            rc = solve_faces<R, NT>(sm, a.gas, sw);
+            rc = solve_faces<R, NT>(sm, a.gas, sw, 0, dtr, Ax, Ay);
         }
         if (rc) err = rc;
     }
@@ -417,9 +423,9 @@ __device__ __forceinline__ void mh2d_item(const Mh2dArgs<R> &a, Mh2dShared<R, NT
             int rc;
             if constexpr (TAPE) {
                 const TapeCtx<R> tc{ a.tape, a.tape_plane, a.pitch, nX, r, r, c0 };
-                rc = solve_faces<R, NT, true>(sm, a.gas, nX + sw, tc);
+                rc = solve_faces<R, NT, true>(sm, a.gas, nX + sw, nX, dtr, Ax, Ay, tc);
             } else {
-                rc = solve_faces<R, NT>(sm, a.gas, nX + sw);
+                rc = solve_faces<R, NT>(sm, a.gas, nX + sw, nX, dtr, Ax, Ay);
             }
             if (rc) err = rc;
         }
@@ -434,10 +440,10 @@ __device__ __forceinline__ void mh2d_item(const Mh2dArgs<R> &a, Mh2dShared<R, NT
 #pragma unroll
             for (int q = 0; q < 4; q++) {
                 R v = Uin[q][idx];
-                v = v + (sm.FL[q][tid - 1] * dtr) * Ax;
-                v = v - (sm.FL[q][tid] * dtr) * Ax;
-                v = v + (gbot[ymap[q]] * dtr) * Ay;
-                v = v - (gtop[ymap[q]] * dtr) * Ay;
+                v = v + sm.FL[q][tid - 1];
+                v = v - sm.FL[q][tid];
+                v = v + gbot[ymap[q]];
+                v = v - gtop[ymap[q]];
                 Un[q] = v;
                 if constexpr (!GRAV) Uout[q][idx] = v;
             }
@@ -470,13 +476,13 @@ __device__ __forceinline__ void mh2d_item(const Mh2dArgs<R> &a, Mh2dShared<R, NT
                 const long long gi = idx - a.pitch;
 #pragma unroll
                 for (int q = 0; q < 4; q++)
-                    Uout[q][gi] = Uin[q][gi] - (gbot[ymap[q]] * dtr) * Ay;
+                    Uout[q][gi] = Uin[q][gi] - gbot[ymap[q]];
             }
             if (r == g + ny - 1) {
                 const long long gi = idx + a.pitch;
 #pragma unroll
                 for (int q = 0; q < 4; q++)
-                    Uout[q][gi] = Uin[q][gi] + (gtop[ymap[q]] * dtr) * Ay;
+                    Uout[q][gi] = Uin[q][gi] + gtop[ymap[q]];
             }
 #pragma unroll
             for (int q = 0; q < 4; q++) { ytop[q] = nhi[q]; gbot[q] = gtop[q]; }
@@ -485,12 +491,12 @@ __device__ __forceinline__ void mh2d_item(const Mh2dArgs<R> &a, Mh2dShared<R, NT
         if (ghost_xmin) {
             const long long gi = rowbase + col;
 #pragma unroll
-            for (int q = 0; q < 4; q++) Uout[q][gi] = Uin[q][gi] - (sm.FL[q][0] * dtr) * Ax;
+            for (int q = 0; q < 4; q++) Uout[q][gi] = Uin[q][gi] - sm.FL[q][0];
         }
         if (ghost_xmax) {
             const long long gi = rowbase + col;
 #pragma unroll
-            for (int q = 0; q < 4; q++) Uout[q][gi] = Uin[q][gi] + (sm.FL[q][sw] * dtr) * Ax;
+            for (int q = 0; q < 4; q++) Uout[q][gi] = Uin[q][gi] + sm.FL[q][sw];
         }
         __syncthreads();
     }
