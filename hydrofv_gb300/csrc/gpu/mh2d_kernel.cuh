@@ -185,12 +185,14 @@ __device__ __noinline__ void vacuum_flux_dev(const GasConst<R> &c, R rl, R ul, R
  * on compacted lists (two-rarefaction: three pow; two-shock: five divides
  * and two square roots), and the finish (wave speeds, S*, region flux).
  * Compaction keeps lanes busy where neighbouring faces fall into different
- * regimes, which the one-face-per-thread form serialises.  The face's
- * update term (flux * dt) * area replaces the left state in sm.FL: faces
- * [0, nXf) are x faces (area Ax), the rest y faces (Ay).  Both cells of a
- * face add or subtract this one product, so it is formed once per face; the
- * reference forms the same product for each cell (identical bits).  Ends
- * with a barrier.
+ * regimes, which the one-face-per-thread form serialises.  FP64: the
+ * face's update term (flux * dt) * area replaces the left state in sm.FL
+ * (faces [0, nXf) are x faces, area Ax, the rest y faces, Ay).  Both cells
+ * of a face add or subtract this one product, so it is formed once per face;
+ * the reference forms the same product for each cell (identical bits).
+ * FP32: the flux itself, and each cell forms U + (F dt) A, which the FP32
+ * build (contraction allowed) fuses; the point blast at 8192^2 needs that
+ * accuracy near its vacuum.  Ends with a barrier.
  */
 template <class R, int NT, bool TAPE = false>
 __device__ __forceinline__ int solve_faces(Mh2dShared<R, NT> &sm, const GasConst<R> &gas, int nF,
@@ -255,9 +257,14 @@ __device__ __forceinline__ int solve_faces(Mh2dShared<R, NT> &sm, const GasConst
                                        sm.pg[f], F);
             if (rc) err = rc;
         }
-        const R A = (f < nXf) ? Ax : Ay;
+        if constexpr (sizeof(R) == 8) {
+            const R A = (f < nXf) ? Ax : Ay;
 #pragma unroll
-        for (int q = 0; q < 4; q++) sm.FL[q][f] = (F[q] * dtr) * A;
+            for (int q = 0; q < 4; q++) sm.FL[q][f] = (F[q] * dtr) * A;
+        } else {
+#pragma unroll
+            for (int q = 0; q < 4; q++) sm.FL[q][f] = F[q];
+        }
     }
     __syncthreads();
     return err;
@@ -274,6 +281,12 @@ __device__ __forceinline__ void mh2d_item(const Mh2dArgs<R> &a, Mh2dShared<R, NT
                                           int &err)
 {
     const R dtr = (R) dt;
+    /* a face's update term from what solve_faces left in sm.FL: FP64 stores
+     * the term itself, FP32 the flux */
+    auto upd = [&](R v, R area) -> R {
+        if constexpr (sizeof(R) == 8) return v;
+        else return (v * dtr) * area;
+    };
     const R dtA_x = (R) (dt * a.area_x / a.vol);
     const R dtA_y = (R) (dt * a.area_y / a.vol);
     const R Ax = (R) a.area_x, Ay = (R) a.area_y;
@@ -440,10 +453,17 @@ __device__ __forceinline__ void mh2d_item(const Mh2dArgs<R> &a, Mh2dShared<R, NT
 #pragma unroll
             for (int q = 0; q < 4; q++) {
                 R v = Uin[q][idx];
-                v = v + sm.FL[q][tid - 1];
-                v = v - sm.FL[q][tid];
-                v = v + gbot[ymap[q]];
-                v = v - gtop[ymap[q]];
+                if constexpr (sizeof(R) == 8) {
+                    v = v + sm.FL[q][tid - 1];
+                    v = v - sm.FL[q][tid];
+                    v = v + gbot[ymap[q]];
+                    v = v - gtop[ymap[q]];
+                } else {
+                    v = v + (sm.FL[q][tid - 1] * dtr) * Ax;
+                    v = v - (sm.FL[q][tid] * dtr) * Ax;
+                    v = v + (gbot[ymap[q]] * dtr) * Ay;
+                    v = v - (gtop[ymap[q]] * dtr) * Ay;
+                }
                 Un[q] = v;
                 if constexpr (!GRAV) Uout[q][idx] = v;
             }
@@ -476,13 +496,13 @@ __device__ __forceinline__ void mh2d_item(const Mh2dArgs<R> &a, Mh2dShared<R, NT
                 const long long gi = idx - a.pitch;
 #pragma unroll
                 for (int q = 0; q < 4; q++)
-                    Uout[q][gi] = Uin[q][gi] - gbot[ymap[q]];
+                    Uout[q][gi] = Uin[q][gi] - upd(gbot[ymap[q]], Ay);
             }
             if (r == g + ny - 1) {
                 const long long gi = idx + a.pitch;
 #pragma unroll
                 for (int q = 0; q < 4; q++)
-                    Uout[q][gi] = Uin[q][gi] + gtop[ymap[q]];
+                    Uout[q][gi] = Uin[q][gi] + upd(gtop[ymap[q]], Ay);
             }
 #pragma unroll
             for (int q = 0; q < 4; q++) { ytop[q] = nhi[q]; gbot[q] = gtop[q]; }
@@ -491,12 +511,12 @@ __device__ __forceinline__ void mh2d_item(const Mh2dArgs<R> &a, Mh2dShared<R, NT
         if (ghost_xmin) {
             const long long gi = rowbase + col;
 #pragma unroll
-            for (int q = 0; q < 4; q++) Uout[q][gi] = Uin[q][gi] - sm.FL[q][0];
+            for (int q = 0; q < 4; q++) Uout[q][gi] = Uin[q][gi] - upd(sm.FL[q][0], Ax);
         }
         if (ghost_xmax) {
             const long long gi = rowbase + col;
 #pragma unroll
-            for (int q = 0; q < 4; q++) Uout[q][gi] = Uin[q][gi] + sm.FL[q][sw];
+            for (int q = 0; q < 4; q++) Uout[q][gi] = Uin[q][gi] + upd(sm.FL[q][sw], Ax);
         }
         __syncthreads();
     }
