@@ -300,6 +300,37 @@ FXHD double sq(double x)
 #endif
 }
 
+/* x + 0.0 and 0.0 - x as the kernels evaluate them (the reference's literal
+ * "+ 0.0" terms, which only turn -0.0 into +0.0).  On the device, for
+ * double, a compare and select on the bits: x + 0.0 is x except that -0.0
+ * becomes +0.0, and 0.0 - x is -x except that both zeros give +0.0.  A NaN
+ * stays a NaN (its payload bits are not canonicalised as an FP64 add would). */
+template <class R>
+FXHD R add_zero(R x) { return x + R(0); }
+
+template <class R>
+FXHD R zero_minus(R x) { return R(0) - x; }
+
+FXHD double add_zero(double x)
+{
+#if defined(__CUDA_ARCH__)
+    const fx::u64 u = fx::bits(x);
+    return fx::from_bits(u == fx::SIGN ? 0ull : u);
+#else
+    return x + 0.0;
+#endif
+}
+
+FXHD double zero_minus(double x)
+{
+#if defined(__CUDA_ARCH__)
+    const fx::u64 u = fx::bits(x);
+    return fx::from_bits((u << 1) == 0ull ? 0ull : (u ^ fx::SIGN));
+#else
+    return 0.0 - x;
+#endif
+}
+
 /* Ordered comparisons as the kernels evaluate them: IEEE semantics (false
  * when either operand is NaN, +0 == -0), on the integer pipes for double on
  * the device. */

@@ -682,14 +682,16 @@ HD void hancock_2d(R dtA, R dtA_rho, R rho, R n, R t, R p, R a,
     const R um = R(1) - dtA * n;
     const R dr = dtA * rho;
     const R draa = dr * a * a * d[1];
-    lo[0] = rho + R(-0.5) * (up * d[0] + dr * d_rho_vel + R(0) + R(0));
-    lo[1] = n + R(-0.5) * (R(0) + up * d[1] + R(0) + dtA_rho * d[3]);
-    lo[2] = t + R(-0.5) * (R(0) + R(0) + up * d[2] + R(0));
-    lo[3] = p + R(-0.5) * (R(0) + draa + R(0) + up * d[3]);
-    hi[0] = rho + R(0.5) * (um * d[0] - dr * d_rho_vel + R(0) + R(0));
-    hi[1] = n + R(0.5) * (R(0) + um * d[1] + R(0) - dtA_rho * d[3]);
-    hi[2] = t + R(0.5) * (R(0) + R(0) + um * d[2] + R(0));
-    hi[3] = p + R(0.5) * (R(0) + R(0) - draa + um * d[3]);
+    /* ((0 + 0) + y) + 0 == add_zero(y) and (0 + 0) - y == zero_minus(y): the
+     * zero terms in closed form, the same values (x + 0 is idempotent) */
+    lo[0] = rho + R(-0.5) * add_zero(up * d[0] + dr * d_rho_vel);
+    lo[1] = n + R(-0.5) * (add_zero(up * d[1]) + dtA_rho * d[3]);
+    lo[2] = t + R(-0.5) * add_zero(up * d[2]);
+    lo[3] = p + R(-0.5) * (add_zero(draa) + up * d[3]);
+    hi[0] = rho + R(0.5) * add_zero(um * d[0] - dr * d_rho_vel);
+    hi[1] = n + R(0.5) * (add_zero(um * d[1]) - dtA_rho * d[3]);
+    hi[2] = t + R(0.5) * add_zero(um * d[2]);
+    hi[3] = p + R(0.5) * (zero_minus(draa) + um * d[3]);
 }
 
 /* 1D predictor (src/integrator_muscl_hancock.c:185-246). */
