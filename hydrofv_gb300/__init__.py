@@ -339,26 +339,30 @@ def _set_custom(bcp, custom_bc, keep):
             setattr(bcp, "set_boundary_condition_cartesian_2d_" + side, C.cast(cb, C.c_void_p).value)
 
 
-def run_2d(nx: int, ny: int, g: int, bounds, gamma: float, W: np.ndarray, U: np.ndarray,
-           bc=("periodic",) * 4, integrator="muscl_hancock_2d",
-           riemann_solver="riemann_solver_hllc", slope_limiter="monotonized_central",
-           cfl=0.8, tf=1.0, max_steps=-1, options: HydroGpuOptions | None = None,
-           storing: dict | None = None, gravity: float = 0.0, custom_bc=None) -> RunResult:
-    """Run a 2D problem through hydro_gpu_launch_simulation.  W and U are
-    (4, ny+2g, nx+2g) float64 arrays (rho,u,v,p / mass,mom_x,mom_y,energy).
+class Simulation2D:
+    """A 2D problem held in the reference's structs -- a System allocated by
+    system_init with the padded W and U in its host arrays, and the boundary,
+    integrator, storing, settings and simulation parameters -- launched
+    through the drop-in entry point, hydro_gpu_launch_simulation (the host
+    arrays in and out, host<->device copies inside the call).  W and U are
+    (4, ny+2g, nx+2g) float64 arrays (rho,u,v,p / mass,mom_x,mom_y,energy);
     gravity sets System.gravity; custom_bc gives a problems.BcCallback per
     side whose boundary name is "custom"."""
-    lib = library()
-    h = _SystemHandle(lib, "cartesian_2d", nx, ny, g, bounds, gamma)
-    h.s.gravity = gravity
-    try:
-        for dst, src in zip(h.fields(W2), W):
-            dst[:] = np.ascontiguousarray(src, dtype=np.float64).reshape(-1)
-        for dst, src in zip(h.fields(U2), U):
-            dst[:] = np.ascontiguousarray(src, dtype=np.float64).reshape(-1)
+
+    def __init__(self, nx: int, ny: int, g: int, bounds, gamma: float, W: np.ndarray, U: np.ndarray,
+                 bc=("periodic",) * 4, integrator="muscl_hancock_2d",
+                 riemann_solver="riemann_solver_hllc", slope_limiter="monotonized_central",
+                 cfl=0.8, tf=1.0, max_steps=-1, options: HydroGpuOptions | None = None,
+                 storing: dict | None = None, gravity: float = 0.0, custom_bc=None):
+        lib = self.lib = library()
+        self.h = _SystemHandle(lib, "cartesian_2d", nx, ny, g, bounds, gamma)
+        self.h.s.gravity = gravity
+        self._W0, self._U0 = W, U
+        self.load(W, U)
         keep: list = []
-        bcp, ip = _params(lib, bc, integrator, riemann_solver, slope_limiter, cfl, keep)
-        _set_custom(bcp, custom_bc, keep)
+        self._keep = keep
+        self.bcp, self.ip = _params(lib, bc, integrator, riemann_solver, slope_limiter, cfl, keep)
+        _set_custom(self.bcp, custom_bc, keep)
         sp = lib.get_new_storing_param()
         if storing:
             sp.is_storing = True
@@ -367,21 +371,58 @@ def run_2d(nx: int, ny: int, g: int, bounds, gamma: float, W: np.ndarray, U: np.
             d = storing["output_dir"].encode()
             keep.append(d)
             sp.output_dir = d
-        settings = Settings(0, True)
-        simp = SimulationParam(tf)
-        st = SimulationStatus(0, 0.0, 0.0)
-        opt = options if options is not None else lib.hydro_gpu_default_options()
+        self.sp = sp
+        self.settings = Settings(0, True)
+        self.simp = SimulationParam(tf)
+        self.opt = options if options is not None else lib.hydro_gpu_default_options()
         if max_steps is not None and max_steps >= 0:
-            opt.max_steps = max_steps
+            self.opt.max_steps = max_steps
+
+    def load(self, W: np.ndarray, U: np.ndarray) -> None:
+        """Copy a padded state into the System's host arrays."""
+        for dst, src in zip(self.h.fields(W2), W):
+            dst[:] = np.ascontiguousarray(src, dtype=np.float64).reshape(-1)
+        for dst, src in zip(self.h.fields(U2), U):
+            dst[:] = np.ascontiguousarray(src, dtype=np.float64).reshape(-1)
+
+    def launch(self) -> tuple[int, str, SimulationStatus, dict]:
+        """One hydro_gpu_launch_simulation call on the System as it stands:
+        (code, message, status, stats).  The System's arrays hold the final
+        state afterwards."""
+        st = SimulationStatus(0, 0.0, 0.0)
         stats = HydroGpuStats()
-        code, msg = _consume(lib, lib.hydro_gpu_launch_simulation(
-            C.byref(bcp), C.byref(h.s), C.byref(ip), C.byref(sp), C.byref(settings),
-            C.byref(simp), C.byref(st), C.byref(opt), C.byref(stats)))
-        Wout = np.stack([f.copy() for f in h.fields(W2)]).reshape((4,) + h.shape)
-        Uout = np.stack([f.copy() for f in h.fields(U2)]).reshape((4,) + h.shape)
-        return RunResult(code, msg, Wout, Uout, st.num_steps, st.t, st.dt, _stats_dict(stats))
-    finally:
-        h.close()
+        code, msg = _consume(self.lib, self.lib.hydro_gpu_launch_simulation(
+            C.byref(self.bcp), C.byref(self.h.s), C.byref(self.ip), C.byref(self.sp),
+            C.byref(self.settings), C.byref(self.simp), C.byref(st), C.byref(self.opt), C.byref(stats)))
+        return code, msg, st, _stats_dict(stats)
+
+    def result(self, code, msg, st, stats) -> RunResult:
+        Wout = np.stack([f.copy() for f in self.h.fields(W2)]).reshape((4,) + self.h.shape)
+        Uout = np.stack([f.copy() for f in self.h.fields(U2)]).reshape((4,) + self.h.shape)
+        return RunResult(code, msg, Wout, Uout, st.num_steps, st.t, st.dt, stats)
+
+    def close(self) -> None:
+        self.h.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+def run_2d(nx: int, ny: int, g: int, bounds, gamma: float, W: np.ndarray, U: np.ndarray,
+           bc=("periodic",) * 4, integrator="muscl_hancock_2d",
+           riemann_solver="riemann_solver_hllc", slope_limiter="monotonized_central",
+           cfl=0.8, tf=1.0, max_steps=-1, options: HydroGpuOptions | None = None,
+           storing: dict | None = None, gravity: float = 0.0, custom_bc=None) -> RunResult:
+    """Run a 2D problem through hydro_gpu_launch_simulation (see
+    Simulation2D) and return the final state."""
+    with Simulation2D(nx, ny, g, bounds, gamma, W, U, bc=bc, integrator=integrator,
+                      riemann_solver=riemann_solver, slope_limiter=slope_limiter, cfl=cfl, tf=tf,
+                      max_steps=max_steps, options=options, storing=storing, gravity=gravity,
+                      custom_bc=custom_bc) as sim:
+        return sim.result(*sim.launch())
 
 
 def run_1d(nx: int, g: int, bounds, gamma: float, W: np.ndarray, U: np.ndarray,
