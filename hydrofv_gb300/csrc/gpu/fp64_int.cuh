@@ -62,10 +62,16 @@ namespace fx {
 typedef unsigned long long u64;
 typedef long long i64;
 
+/* The bits of a double.  On the device through an opaque move: a plain
+ * bitcast lets the compiler recognise the bit tests below (zero, exponent
+ * range, sign) as floating-point class tests and emit them as FP64 compares
+ * on the FP64 pipe, which is what these forms exist to avoid. */
 FXHD u64 bits(double x)
 {
 #if defined(__CUDA_ARCH__)
-    return (u64) __double_as_longlong(x);
+    u64 u;
+    asm("mov.b64 %0, %1;" : "=l"(u) : "d"(x));
+    return u;
 #else
     u64 b;
     memcpy(&b, &x, sizeof b);
