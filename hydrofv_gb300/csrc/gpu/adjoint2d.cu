@@ -190,6 +190,17 @@ __device__ __forceinline__ void record(int *err, int code)
     for (long long k = blockIdx.x * (long long) blockDim.x + threadIdx.x; k < (total); \
          k += (long long) gridDim.x * blockDim.x)
 
+/* Row and column of padded index k.  Sessions are created only for grids of
+ * fewer than 2^32 padded cells, so 32-bit unsigned arithmetic is exact (a
+ * 64-bit integer divide is a long software sequence on the device). */
+__device__ __forceinline__ void row_col(const AdGeom &q, long long k, int &r, int &c)
+{
+    const unsigned kk = (unsigned) k, t = (unsigned) q.tx;
+    const unsigned rr = kk / t;
+    r = (int) rr;
+    c = (int) (kk - rr * t);
+}
+
 /* ------------------------------------------------------- forward pieces */
 
 /* Interior: sound speed and U = W->U(W). */
@@ -197,7 +208,8 @@ template <class R>
 __global__ void ad_init_kernel(const AdGeom q, const GasConst<R> gas, StateP<R> s, R vol)
 {
     GRID_STRIDE(k, (long long) q.tx * q.ty) {
-        const int r = (int) (k / q.tx), c = (int) (k % q.tx);
+        int r, c;
+        row_col(q, k, r, c);
         if (!interior(q, r, c)) continue;
         R w[4], U[4];
 #pragma unroll
@@ -213,7 +225,8 @@ __global__ void ad_init_kernel(const AdGeom q, const GasConst<R> gas, StateP<R> 
 __global__ void ad_fill_ghosts_kernel(const AdGeom q, StateP<double> s)
 {
     GRID_STRIDE(k, (long long) q.tx * q.ty) {
-        const int r = (int) (k / q.tx), c = (int) (k % q.tx);
+        int r, c;
+        row_col(q, k, r, c);
         const bool in_r = r >= q.g && r < q.g + q.ny, in_c = c >= q.g && c < q.g + q.nx;
         if (in_r == in_c) continue;   /* interior or corner */
         double w[4];
@@ -231,7 +244,8 @@ __global__ void __launch_bounds__(kThreads) ad_recon_kernel(const AdGeom q, Stat
 {
     unsigned long long h = 0;
     GRID_STRIDE(k, (long long) q.tx * q.ty) {
-        const int r = (int) (k / q.tx), c = (int) (k % q.tx);
+        int r, c;
+        row_col(q, k, r, c);
         const bool nx_ = need_x(q, r, c), ny_ = need_y(q, r, c);
         if (!nx_ && !ny_) continue;
         R w0[4], a0, t;
@@ -287,7 +301,8 @@ __global__ void __launch_bounds__(kThreads) ad_flux_kernel(const AdGeom q, const
     unsigned long long h = 0;
     const int g = q.g;
     GRID_STRIDE(k, (long long) q.tx * q.ty) {
-        const int r = (int) (k / q.tx), c = (int) (k % q.tx);
+        int r, c;
+        row_col(q, k, r, c);
         if (r >= g && r < g + q.ny && c >= g - 1 && c <= g + q.nx - 1) {
             R F[4];
             const R L0 = f.xhi[0][k], L1 = f.xhi[1][k], L2 = f.xhi[2][k], L3 = f.xhi[3][k];
@@ -347,7 +362,8 @@ __global__ void __launch_bounds__(kThreads) ad_update_kernel(const AdGeom q, con
 {
     const int ymap[4] = { 0, 2, 1, 3 };
     GRID_STRIDE(k, (long long) q.tx * q.ty) {
-        const int r = (int) (k / q.tx), c = (int) (k % q.tx);
+        int r, c;
+        row_col(q, k, r, c);
         if (!interior(q, r, c)) continue;
         R Un[4];
 #pragma unroll
@@ -372,7 +388,8 @@ __global__ void __launch_bounds__(kThreads) ad_update_kernel(const AdGeom q, con
 __global__ void ad_pack_dual_kernel(const AdGeom q, F4<double> w, F4<double> dw, StateP<Dual> s)
 {
     GRID_STRIDE(k, (long long) q.tx * q.ty) {
-        const int r = (int) (k / q.tx), c = (int) (k % q.tx);
+        int r, c;
+        row_col(q, k, r, c);
         if (!interior(q, r, c)) continue;
 #pragma unroll
         for (int f = 0; f < 4; f++) s.W[f][k] = Dual(w.p[f][k], dw.p[f][k]);
@@ -383,7 +400,8 @@ __global__ void ad_pack_dual_kernel(const AdGeom q, F4<double> w, F4<double> dw,
 __global__ void ad_unpack_dual_kernel(const AdGeom q, StateP<Dual> s, F4<double> w, F4<double> dw)
 {
     GRID_STRIDE(k, (long long) q.tx * q.ty) {
-        const int r = (int) (k / q.tx), c = (int) (k % q.tx);
+        int r, c;
+        row_col(q, k, r, c);
         const bool in = interior(q, r, c);
 #pragma unroll
         for (int f = 0; f < 4; f++) {
@@ -398,7 +416,8 @@ __global__ void ad_unpack_dual_kernel(const AdGeom q, StateP<Dual> s, F4<double>
 __global__ void ad_copy_interior_kernel(const AdGeom q, F4<double> src, F4<double> dst)
 {
     GRID_STRIDE(k, (long long) q.tx * q.ty) {
-        const int r = (int) (k / q.tx), c = (int) (k % q.tx);
+        int r, c;
+        row_col(q, k, r, c);
         const bool in = interior(q, r, c);
 #pragma unroll
         for (int f = 0; f < 4; f++) dst.p[f][k] = in ? src.p[f][k] : 0.0;
@@ -423,7 +442,8 @@ __global__ void ad_compare_kernel(const AdGeom q, StateP<double> a, StateP<doubl
 {
     unsigned long long n = 0;
     GRID_STRIDE(k, (long long) q.tx * q.ty) {
-        const int r = (int) (k / q.tx), c = (int) (k % q.tx);
+        int r, c;
+        row_col(q, k, r, c);
         if (!interior(q, r, c)) continue;
         bool diff = false;
 #pragma unroll
@@ -445,7 +465,8 @@ __global__ void ad_seed_kernel(const AdGeom q, const GasConst<double> gas, doubl
                                F4<double> seed, F4<double> Ub)
 {
     GRID_STRIDE(k, (long long) q.tx * q.ty) {
-        const int r = (int) (k / q.tx), c = (int) (k % q.tx);
+        int r, c;
+        row_col(q, k, r, c);
         if (!interior(q, r, c)) continue;
         const double wb[4] = { seed.p[0][k], seed.p[1][k], seed.p[2][k], seed.p[3][k] };
         double ub[4] = { 0, 0, 0, 0 };
@@ -458,13 +479,14 @@ __global__ void ad_seed_kernel(const AdGeom q, const GasConst<double> gas, doubl
 /* Per face: Fbar = dt * area * (Ubar of the cell above - Ubar of the cell
  * below) (ghost Ubar is zero: ghost U is not state), then the reverse of the
  * HLLC flux into the adjoints of the two face states. */
-__global__ void __launch_bounds__(kThreads) ad_flux_vjp_kernel(const AdGeom q, const GasConst<double> gas,
+__global__ void __launch_bounds__(kThreads, 2) ad_flux_vjp_kernel(const AdGeom q, const GasConst<double> gas,
                                                                FacesP<double> f, FacesP<double> fb,
                                                                F4<double> Ub, double cx, double cy, int *err)
 {
     const int g = q.g;
     GRID_STRIDE(k, (long long) q.tx * q.ty) {
-        const int r = (int) (k / q.tx), c = (int) (k % q.tx);
+        int r, c;
+        row_col(q, k, r, c);
         if (r >= g && r < g + q.ny && c >= g - 1 && c <= g + q.nx - 1) {
             double L[4], Rs[4], Fb[4], Lb[4], Rb[4];
 #pragma unroll
@@ -502,14 +524,15 @@ __global__ void __launch_bounds__(kThreads) ad_flux_vjp_kernel(const AdGeom q, c
 /* The same from the tape the recomputation wrote (face states and the HLLC
  * guess with its factors), so neither the reconstruction nor the guesses
  * are evaluated again. */
-__global__ void __launch_bounds__(kThreads) ad_flux_vjp_tape_kernel(const AdGeom q, const GasConst<double> gas,
+__global__ void __launch_bounds__(kThreads, 2) ad_flux_vjp_tape_kernel(const AdGeom q, const GasConst<double> gas,
                                                                     const double *tape, long long plane,
                                                                     FacesP<double> fb, F4<double> Ub,
                                                                     double cx, double cy, int *err)
 {
     const int g = q.g;
     GRID_STRIDE(k, (long long) q.tx * q.ty) {
-        const int r = (int) (k / q.tx), c = (int) (k % q.tx);
+        int r, c;
+        row_col(q, k, r, c);
 #pragma unroll
         for (int dir = 0; dir < 2; dir++) {
             const bool on = dir == 0 ? (r >= g && r < g + q.ny && c >= g - 1 && c <= g + q.nx - 1)
@@ -567,7 +590,8 @@ __global__ void __launch_bounds__(kThreads) ad_recon_vjp_kernel(const AdGeom q, 
                                                                 SharesP sh, double dtA_x, double dtA_y)
 {
     GRID_STRIDE(k, (long long) q.tx * q.ty) {
-        const int r = (int) (k / q.tx), c = (int) (k % q.tx);
+        int r, c;
+        row_col(q, k, r, c);
         const bool nx_ = need_x(q, r, c), ny_ = need_y(q, r, c);
         if (!nx_ && !ny_) continue;
         double w0[4], a0, o[4] = { 0, 0, 0, 0 };
@@ -626,7 +650,8 @@ __global__ void __launch_bounds__(kThreads) ad_gather_kernel(const AdGeom q, con
 {
     const int g = q.g;
     GRID_STRIDE(k, (long long) q.tx * q.ty) {
-        const int r = (int) (k / q.tx), c = (int) (k % q.tx);
+        int r, c;
+        row_col(q, k, r, c);
         if (!interior(q, r, c)) continue;
         double wb[4];
         gather_cell(q, sh, r, c, wb);
@@ -952,6 +977,11 @@ extern "C" int hydro_adj2d_create(const HydroGrid2D *grid, const HydroGpuOptions
                  "The adjoint needs G >= 2, at least 2 x 2 cells, num_steps >= 1, checkpoint_every >= 1 and FP64.");
         return -1;
     }
+    if ((long long) (grid->nx + 2 * grid->g) * (grid->ny + 2 * grid->g) >= (1ll << 32)) {
+        oc->kind = HYDRO_RUN_UNSUPPORTED;
+        snprintf(oc->message, sizeof oc->message, "The adjoint needs fewer than 2^32 padded cells.");
+        return -1;
+    }
     HydroAdj2D *a = new (std::nothrow) HydroAdj2D();
     if (!a) {
         oc->kind = HYDRO_RUN_CUDA_ERROR;
@@ -969,6 +999,7 @@ extern "C" int hydro_adj2d_create(const HydroGrid2D *grid, const HydroGpuOptions
     a->n_ckpt = (int) ((num_steps + a->K - 1) / a->K);
     const int tx = grid->nx + 2 * grid->g, ty = grid->ny + 2 * grid->g;
     a->ncell = (size_t) tx * ty;
+
     a->fbytes = a->ncell * sizeof(double);
     a->geom.nx = grid->nx;
     a->geom.ny = grid->ny;
