@@ -186,6 +186,7 @@ _SIGNATURES = {
                                      _dp, _dp, _P(C.c_int)]),
     "hydro_fx_eval_host": (None, [C.c_int, C.c_longlong, _dp, _dp, _dp, C.c_void_p]),
     "hydro_gpu_fx_eval": (C.c_int, [C.c_int, C.c_int, C.c_longlong, _dp, _dp, _dp, _dp, C.c_void_p]),
+    "hydro_fx_div_seeded_host": (None, [C.c_longlong, _dp, _dp, C.c_void_p, _dp, C.c_void_p]),
     "hydro_gpu_device_count": (C.c_int, []),
     "hydro_gpu_calibrate": (C.c_int, [C.c_int, _dp, _dp]),
     "hydro_gpu_version": (C.c_char_p, []),
@@ -839,3 +840,17 @@ def gpu_fx_eval(op, a, b=None, device=0):
     if rc != 0:
         raise HydroError(rc, "hydro_gpu_fx_eval failed (CUDA error)")
     return fast, hw, ok.astype(bool)
+
+
+def fx_div_seeded_host(a, b, seed_scale):
+    """Host build of the integer division with its FP32 reciprocal seed
+    scaled by seed_scale: (results, fast-path flags)."""
+    a, b = _fx_args(0, a, b)
+    sc = np.ascontiguousarray(seed_scale, dtype=np.float32).ravel()
+    if sc.shape != a.shape:
+        raise ValueError("seed_scale must have the size of a")
+    out = np.empty_like(a)
+    ok = np.zeros(a.shape, dtype=np.uint8)
+    library().hydro_fx_div_seeded_host(a.size, a.ctypes.data_as(_dp), b.ctypes.data_as(_dp), sc.ctypes.data,
+                                       out.ctypes.data_as(_dp), ok.ctypes.data)
+    return out, ok.astype(bool)

@@ -17,9 +17,10 @@
  *      error is ~e0^2 ~ 2^-44;
  *   3. the quotient Q = floor(ma 2^(52+s) / mb) (s = [ma < mb], so Q has 53
  *      bits) by a multiply-high with Y1, one correction by the remainder
- *      times Y1, and at most two single-step fixes;
- *   4. an exact 128-bit check that A - Q mb lies in [0, mb) (A = ma 2^(52+s)),
- *      then round-to-nearest-even on the remainder (2R against mb).
+ *      times Y1, and one single-step fix, which make Q exact whenever the
+ *      seed's residual is small (|e0| < 3 2^61, checked; the bounds are in
+ *      div_fast);
+ *   4. round-to-nearest-even on the remainder (2R against mb).
  * This is the reciprocal-multiply-and-correct form of long division
  * (Knuth, TAOCP vol. 2, 4.3.1; Moller & Granlund, "Improved division by
  * invariant integers", IEEE TC 2011) applied to the 53-bit mantissas.
@@ -35,8 +36,9 @@
  *   4. an exact 128-bit check that 0 <= M 2^52 - S^2 <= 2S, then rounding
  *      up where the residual exceeds S (a square root is never a midpoint).
  *
- * Correctness does not rest on the seed's accuracy: step 4 verifies the
- * result exactly, and every operand or result outside the fast path
+ * Correctness does not rest on the seed's accuracy: the divide checks the
+ * seed's exact residual, the square root verifies its result exactly, and
+ * every operand or result outside the fast path
  * (zero, subnormal, infinite, NaN, negative for sqrt, quotients that
  * overflow the normal range before rounding or underflow) or a failed check
  * takes the hardware operation.  The results are therefore bit-identical to
@@ -157,8 +159,10 @@ static const u64 FRAC = 0x000fffffffffffffull;
 static const u64 HIDDEN = 0x0010000000000000ull;
 static const u64 SIGN = 0x8000000000000000ull;
 
-/* RN(a / b) when `ok` comes back true (see the header comment). */
-FXHD double div_fast(double a, double b, bool &ok)
+/* RN(a / b) when `ok` comes back true (see the header comment).
+ * seed_scale multiplies the FP32 reciprocal seed: 1 in the kernels; the
+ * tests perturb it to exercise the seed check. */
+FXHD double div_fast(double a, double b, bool &ok, float seed_scale = 1.0f)
 {
     const u64 ua = bits(a), ub = bits(b);
     const unsigned ea = (unsigned) (ua >> 52) & 0x7ffu, eb = (unsigned) (ub >> 52) & 0x7ffu;
@@ -167,22 +171,32 @@ FXHD double div_fast(double a, double b, bool &ok)
     const int s = ma < mb ? 1 : 0;
     const int e = (int) ea - (int) eb + 1023 - s;          /* biased exponent of the quotient */
 
-    const unsigned Y0 = seed_fixed(rcp_seed(from_fbits(0x3f800000u | (unsigned) ((mb >> 29) & 0x7fffffu))));
-    const i64 e0 = (i64) (0ull - mb * (u64) Y0);             /* 2^84 - mb Y0 */
+    const unsigned Y0 = seed_fixed(rcp_seed(from_fbits(0x3f800000u | (unsigned) ((mb >> 29) & 0x7fffffu))) * seed_scale);
+    /* mb Y0 (85 bits) from two 32 x 32 products.  Its low 64 bits, negated,
+     * are the residual e0 = 2^84 - mb Y0 exactly when the high bits are
+     * 2^20 - 1 with e0 > 0, or 2^20 with e0 <= 0 (so |2^84 - mb Y0| < 2^63) */
+    const u64 t = (u64) (unsigned) mb * Y0;
+    const u64 hm = (u64) (unsigned) (mb >> 32) * Y0 + (t >> 32);
+    const i64 e0 = (i64) (0ull - ((hm << 32) | (t & 0xffffffffull)));
+    const unsigned top = (unsigned) (hm >> 32);
+    /* the seed is good enough when |e0| < 3 2^61 (relative error < 2^-21.4):
+     * then Y1 <= 2^116 / mb with relative error < 2^-42.8, the first
+     * remainder R lies in [0, 2^64), the correction leaves it in [0, 2 mb)
+     * and one step finishes the exact quotient (a seed outside the bound
+     * takes the hardware divide) */
+    const bool seed_ok = (top == (1u << 20) - 1u ? e0 > 0 : (top == (1u << 20) && e0 <= 0))
+                      && e0 < 3 * (1ll << 61) && e0 > -3 * (1ll << 61);
     const i64 d = ((i64) (int) (e0 >> 32) * (i64) Y0) >> 20; /* Y0 e0 2^-52 */
     const u64 Y1 = ((u64) Y0 << 32) + (u64) d;               /* ~2^116 / mb, from below */
 
-    const u64 A_lo = ma << (52 + s), A_hi = ma >> (12 - s);
-    u64 Q = mulhi(ma << s, Y1);
+    const u64 A_lo = ma << (52 + s);
+    u64 Q = mulhi(ma << s, Y1);                              /* <= floor(A / mb), A = ma 2^(52+s) */
     u64 R = A_lo - Q * mb;
     const u64 dq = ((R >> 32) * (Y1 >> 32)) >> 52;
     Q += dq;
     R -= dq * mb;
     if (R >= mb) { Q += 1; R -= mb; }
-    if (R >= mb) { Q += 1; R -= mb; }
-
-    const u64 P_lo = Q * mb, P_hi = mulhi(Q, mb);
-    const bool exact = (A_hi - P_hi - (A_lo < P_lo ? 1ull : 0ull)) == 0ull && (A_lo - P_lo) < mb;
+    const bool exact = seed_ok;
     const u64 r2 = R << 1;
     Q += (r2 > mb || (r2 == mb && (Q & 1ull))) ? 1ull : 0ull;
     const u64 res = sign | (((u64) (unsigned) (e - 1) << 52) + Q);

@@ -74,6 +74,16 @@ void hydro_fx_eval_host(int op, long long n, const double *a, const double *b, d
     }
 }
 
+void hydro_fx_div_seeded_host(long long n, const double *a, const double *b, const float *seed_scale,
+                              double *out, unsigned char *ok)
+{
+    for (long long i = 0; i < n; i++) {
+        bool k;
+        out[i] = fx::div_fast(a[i], b[i], k, seed_scale[i]);
+        ok[i] = k ? 1 : 0;
+    }
+}
+
 int hydro_gpu_fx_eval(int device, int op, long long n, const double *a, const double *b,
                       double *fast, double *hw, unsigned char *ok)
 {

@@ -350,6 +350,10 @@ void hydro_fx_eval_host(int op, long long n, const double *a, const double *b, d
                         unsigned char *ok);
 int hydro_gpu_fx_eval(int device, int op, long long n, const double *a, const double *b,
                       double *fast, double *hw, unsigned char *ok);
+/* Host build of the division with its FP32 reciprocal seed multiplied by
+ * seed_scale[i] (tests of the seed check: where ok[i], out[i] = RN(a/b)). */
+void hydro_fx_div_seeded_host(long long n, const double *a, const double *b, const float *seed_scale,
+                              double *out, unsigned char *ok);
 
 /* Number of visible CUDA devices (0 when none; never fails). */
 int hydro_gpu_device_count(void);

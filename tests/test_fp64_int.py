@@ -116,6 +116,29 @@ def test_host_division_exact_quotients_and_zero_numerators():
     assert ok.all() and np.array_equal(out.view(np.uint64), (z / den).view(np.uint64))
 
 
+def test_host_division_seed_check_catches_bad_seeds():
+    """The divide trusts its FP32 reciprocal seed only when the seed's exact
+    residual is small; a perturbed seed either still gives RN(a/b) or takes
+    the fallback, never a wrong quotient.  Mantissas near 2 are included
+    (their reciprocal seed sits at 0.5, where a low seed changes scale)."""
+    rng = np.random.default_rng(31)
+    n = 1 << 19
+    a = _doubles(rng, n, 1000, 1050)
+    b = _doubles(rng, n, 1000, 1050)
+    b[: n // 8] = np.nextafter(2.0 ** rng.integers(-20, 20, n // 8), 0.0) * rng.choice([1.0, -1.0], n // 8)
+    with np.errstate(all="ignore"):
+        ref = a / b
+    for spread in (2.0 ** -23, 2.0 ** -21.5, 2.0 ** -20, 2.0 ** -16, 0.5):
+        scale = (1.0 + rng.uniform(-spread, spread, n)).astype(np.float32)
+        out, ok = h.fx_div_seeded_host(a, b, scale)
+        assert _same_bits(out[ok], ref[ok]).all(), spread
+        if spread <= 2.0 ** -23:
+            assert ok.all()
+    for far in (0.75, 1.3):                                  # seeds off by 25-30%
+        out, ok = h.fx_div_seeded_host(a, b, np.full(n, far, dtype=np.float32))
+        assert not ok.any()
+
+
 def test_host_division_special_operands_take_the_fallback():
     sp = np.array([0.0, -0.0, np.inf, -np.inf, np.nan, 5e-324, -2.2e-308, 1.0])
     a = np.repeat(sp, sp.size)
