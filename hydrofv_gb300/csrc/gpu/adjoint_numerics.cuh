@@ -35,6 +35,34 @@ namespace hydro {
 template <int LIM>
 HD double limit_slope_partials(double a, double b, double &da, double &db, int &code)
 {
+#if defined(__CUDA_ARCH__)
+    /* the branch decided on the bits, as the forward limiter decides it
+     * (fx::product_nonpositive; minima of positive doubles on their bit
+     * patterns); operands it does not decide take the code below */
+    {
+        const fx::u64 ua = fx::bits(a), ub = fx::bits(b);
+        const int t = fx::product_nonpositive(ua, ub);
+        if (t > 0) { da = 0.0; db = 0.0; code = 0; return 0.0; }
+        if (t == 0 && LIM != LIM_VAN_LEER) {
+            const fx::u64 aa = ua & ~fx::SIGN, ab = ub & ~fx::SIGN;
+            if (LIM == LIM_MINMOD) {
+                if (aa < ab) { da = 1.0; db = 0.0; code = 1; return a; }
+                da = 0.0; db = 1.0; code = 2; return b;
+            }
+            const bool take_b = ab < aa;
+            const double two = 2.0 * fx::from_bits(take_b ? ab : aa);
+            const double avg = ((ua >> 63) ? -0.5 : 0.5) * (a + b);
+            const fx::u64 ut = fx::bits(two), uv = fx::bits(avg);
+            if (ut < uv) {
+                if (take_b) { da = 0.0; db = 2.0; code = 3; }
+                else { da = 2.0; db = 0.0; code = 2; }
+                return fx::from_bits(ut | (ua & fx::SIGN));
+            }
+            da = 0.5; db = 0.5; code = 1;
+            return fx::from_bits(uv | (ua & fx::SIGN));
+        }
+    }
+#endif
     const double d = limit_slope<LIM>(a, b);
     if (a * b <= 0.0) { da = 0.0; db = 0.0; code = 0; return d; }
     if (LIM == LIM_MINMOD) {
