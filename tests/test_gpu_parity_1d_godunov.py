@@ -132,11 +132,11 @@ def test_geometry_and_random_choice_against_oracle(gpu_available, oracle_mod, co
     r = run1(p)
     assert r.code == 0 and ref.rc == 0, (r.message, ref.message)
     assert r.num_steps == ref.num_steps == 60
-    # The exact solver's pow (rarefaction fans, two-rarefaction guess) may
-    # differ from the CPU's by an ulp; random choice samples the exact
-    # solution directly, and at the reflective origin of a spherical grid
-    # (a symmetric, nearly degenerate Riemann problem) one step amplified
-    # such a difference to ~1.8e4 ulps.  Paths without pow stay bit-exact.
-    tol = 1e-11 if integ == "random_choice_1d" else REL_L1_TOL
-    assert np.all(rel_l1_1d(r.U, ref.U, p.g) <= tol)
-    assert np.all(rel_l1_1d(r.W, ref.W, p.g) <= tol)
+    # The exact solver's pow (rarefaction fans, two-rarefaction guess) is
+    # correctly rounded on the device; glibc's differs from that in rare
+    # cases, and random choice, which samples the exact solution directly,
+    # amplifies such a difference at the reflective origin of a spherical
+    # grid (a symmetric, nearly degenerate Riemann problem): ~3e-13 here.
+    # Paths without pow are bit-exact.
+    assert np.all(rel_l1_1d(r.U, ref.U, p.g) <= REL_L1_TOL)
+    assert np.all(rel_l1_1d(r.W, ref.W, p.g) <= REL_L1_TOL)
