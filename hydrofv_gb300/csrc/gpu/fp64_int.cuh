@@ -45,6 +45,16 @@
  * '/' and sqrt.  Host builds keep the plain operators; the integer forms are
  * also compiled for the host (with host seeds) so that they can be checked
  * against the host's IEEE operations on the CPU.
+ *
+ * The same file holds the other FP64-pipe savings of the step kernel, each
+ * exact: the slope limiter's sign test on the bits (product_nonpositive),
+ * ordered comparisons (lt, le), and the reference's "+ 0.0" terms
+ * (add_zero, zero_minus).  All of them read a double's bits through an
+ * opaque move (bits): with a plain bitcast the compiler recognises zero,
+ * sign and exponent tests as floating-point class tests and emits FP64
+ * compares again.  The divide and square root run out of line on the device
+ * (div_dev, sqrt_dev), one copy per kernel: inlined at the step kernel's ~40
+ * call sites they overflow the instruction cache.
  */
 #ifndef HYDRO_GPU_FP64_INT_CUH
 #define HYDRO_GPU_FP64_INT_CUH
