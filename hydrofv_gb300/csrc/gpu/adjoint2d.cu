@@ -521,60 +521,110 @@ __global__ void __launch_bounds__(kThreads, 2) ad_flux_vjp_kernel(const AdGeom q
     }
 }
 
-/* The same from the tape the recomputation wrote (face states and the HLLC
- * guess with its factors), so neither the reconstruction nor the guesses
- * are evaluated again. */
-__global__ void __launch_bounds__(kThreads, 2) ad_flux_vjp_tape_kernel(const AdGeom q, const GasConst<double> gas,
-                                                                    const double *tape, long long plane,
-                                                                    FacesP<double> fb, F4<double> Ub,
-                                                                    double cx, double cy, int *err)
+/* Reverse HLLC of one face from the tape the recomputation wrote (face
+ * states, the HLLC guess with its factors, and the wave-speed factors and
+ * S*), so neither the reconstruction, the guesses nor the wave speeds are
+ * evaluated again.  dir 0: the x face above cell k, dir 1: the y face. */
+__device__ __forceinline__ void flux_vjp_tape_face(const AdGeom &q, const GasConst<double> &gas,
+                                                   const double *tape, long long plane, FacesP<double> &fb,
+                                                   const F4<double> &Ub, double cx, double cy, int *err,
+                                                   long long k, int dir)
+{
+    const double *T = tape + (long long) (dir * MH2D_TAPE_FIELDS) * plane + k;
+    const long long kn = dir == 0 ? k + 1 : k + q.tx;
+    double L[4], Rs[4], Fb[4], Lb[4], Rb[4];
+#pragma unroll
+    for (int e = 0; e < 4; e++) {
+        L[e] = T[(TAPE_L + e) * plane];
+        Rs[e] = T[(TAPE_R + e) * plane];
+    }
+    if (dir == 0) {
+#pragma unroll
+        for (int e = 0; e < 4; e++) Fb[e] = cx * (Ub.p[e][kn] - Ub.p[e][k]);
+    } else {
+        /* y flux components are (mass, mom_y, mom_x, energy) */
+        Fb[0] = cy * (Ub.p[0][kn] - Ub.p[0][k]);
+        Fb[1] = cy * (Ub.p[2][kn] - Ub.p[2][k]);
+        Fb[2] = cy * (Ub.p[1][kn] - Ub.p[1][k]);
+        Fb[3] = cy * (Ub.p[3][kn] - Ub.p[3][k]);
+    }
+    HllcFwd st;
+    const int rc = hllc_fwd_from_tape(gas, L[0], L[1], L[3], Rs[0], Rs[1], Rs[3], T[TAPE_AL * plane],
+                                      T[TAPE_AR * plane], T[TAPE_PG * plane], (int) T[TAPE_REG * plane],
+                                      T[TAPE_QL * plane], T[TAPE_QR * plane], T[TAPE_SS * plane], st);
+    if (rc) {
+        record(err, rc);
+#pragma unroll
+        for (int e = 0; e < 4; e++) { Lb[e] = 0.0; Rb[e] = 0.0; }
+    } else {
+        hllc_vjp_core(gas, L, Rs, st, true, T[TAPE_Z0 * plane], T[TAPE_Z1 * plane], Fb, Lb, Rb);
+    }
+    if (dir == 0) {
+#pragma unroll
+        for (int e = 0; e < 4; e++) { fb.xhi[e][k] = Lb[e]; fb.xlo[e][kn] = Rb[e]; }
+    } else {
+#pragma unroll
+        for (int e = 0; e < 4; e++) { fb.yhi[e][k] = Lb[e]; fb.ylo[e][kn] = Rb[e]; }
+    }
+}
+
+/* Whether cell k owns an x face (dir 0) or a y face (dir 1) of the sweep. */
+__device__ __forceinline__ bool owns_face(const AdGeom &q, int r, int c, int dir)
 {
     const int g = q.g;
+    return dir == 0 ? (r >= g && r < g + q.ny && c >= g - 1 && c <= g + q.nx - 1)
+                    : (c >= g && c < g + q.nx && r >= g - 1 && r <= g + q.ny - 1);
+}
+
+/* Faces of one step binned by their taped guess regime (PREG_*: vacuum,
+ * PVRS, two-rarefaction, two-shock), so that the reverse HLLC runs warps of
+ * one regime (the regimes' reverse code differs; mixed warps serialise
+ * over it).  A face is 2k + dir; bins[b * cap + i], counts[b].  Appends are
+ * aggregated per warp and regime. */
+__global__ void ad_face_bins_kernel(const AdGeom q, const double *tape, long long plane, unsigned *bins,
+                                    unsigned *counts, long long cap)
+{
     GRID_STRIDE(k, (long long) q.tx * q.ty) {
         int r, c;
         row_col(q, k, r, c);
 #pragma unroll
         for (int dir = 0; dir < 2; dir++) {
-            const bool on = dir == 0 ? (r >= g && r < g + q.ny && c >= g - 1 && c <= g + q.nx - 1)
-                                     : (c >= g && c < g + q.nx && r >= g - 1 && r <= g + q.ny - 1);
-            if (!on) continue;
-            const double *T = tape + (long long) (dir * MH2D_TAPE_FIELDS) * plane + k;
-            const long long kn = dir == 0 ? k + 1 : k + q.tx;
-            double L[4], Rs[4], Fb[4], Lb[4], Rb[4];
-#pragma unroll
-            for (int e = 0; e < 4; e++) {
-                L[e] = T[(TAPE_L + e) * plane];
-                Rs[e] = T[(TAPE_R + e) * plane];
-            }
-            if (dir == 0) {
-#pragma unroll
-                for (int e = 0; e < 4; e++) Fb[e] = cx * (Ub.p[e][kn] - Ub.p[e][k]);
-            } else {
-                /* y flux components are (mass, mom_y, mom_x, energy) */
-                Fb[0] = cy * (Ub.p[0][kn] - Ub.p[0][k]);
-                Fb[1] = cy * (Ub.p[2][kn] - Ub.p[2][k]);
-                Fb[2] = cy * (Ub.p[1][kn] - Ub.p[1][k]);
-                Fb[3] = cy * (Ub.p[3][kn] - Ub.p[3][k]);
-            }
-            HllcFwd st;
-            const int rc = hllc_fwd_from_guess(gas, L[0], L[1], L[3], Rs[0], Rs[1], Rs[3], T[TAPE_AL * plane],
-                                               T[TAPE_AR * plane], T[TAPE_PG * plane], (int) T[TAPE_REG * plane],
-                                               st);
-            if (rc) {
-                record(err, rc);
-#pragma unroll
-                for (int e = 0; e < 4; e++) { Lb[e] = 0.0; Rb[e] = 0.0; }
-            } else {
-                hllc_vjp_core(gas, L, Rs, st, true, T[TAPE_Z0 * plane], T[TAPE_Z1 * plane], Fb, Lb, Rb);
-            }
-            if (dir == 0) {
-#pragma unroll
-                for (int e = 0; e < 4; e++) { fb.xhi[e][k] = Lb[e]; fb.xlo[e][kn] = Rb[e]; }
-            } else {
-#pragma unroll
-                for (int e = 0; e < 4; e++) { fb.yhi[e][k] = Lb[e]; fb.ylo[e][kn] = Rb[e]; }
-            }
+            if (!owns_face(q, r, c, dir)) continue;
+            const int b = (int) tape[(long long) (dir * MH2D_TAPE_FIELDS + TAPE_REG) * plane + k] & 3;
+            const unsigned mask = __activemask();
+            const unsigned peers = __match_any_sync(mask, b);
+            const int lane = threadIdx.x & 31;
+            const int leader = __ffs(peers) - 1;
+            unsigned base = 0;
+            if (lane == leader) base = atomicAdd(&counts[b], (unsigned) __popc(peers));
+            base = __shfl_sync(peers, base, leader);
+            const unsigned pos = base + (unsigned) __popc(peers & ((1u << lane) - 1u));
+            bins[(long long) b * cap + pos] = (unsigned) (2 * k + dir);
         }
+    }
+}
+
+/* The reverse HLLC over the binned faces: PVRS, two-rarefaction, two-shock,
+ * then vacuum faces. */
+__global__ void __launch_bounds__(kThreads, 2) ad_flux_vjp_bins_kernel(const AdGeom q, const GasConst<double> gas,
+                                                                     const double *tape, long long plane,
+                                                                     FacesP<double> fb, F4<double> Ub, double cx,
+                                                                     double cy, int *err, const unsigned *bins,
+                                                                     const unsigned *counts, long long cap)
+{
+    const unsigned n1 = counts[PREG_PVRS], n2 = counts[PREG_TRRS], n3 = counts[PREG_TSRS];
+    const unsigned n0 = counts[PREG_VACUUM];
+    const long long total = (long long) n0 + n1 + n2 + n3;
+    for (long long i = blockIdx.x * (long long) blockDim.x + threadIdx.x; i < total;
+         i += (long long) gridDim.x * blockDim.x) {
+        int b;
+        long long j = i;
+        if (j < n1) b = PREG_PVRS;
+        else if ((j -= n1) < n2) b = PREG_TRRS;
+        else if ((j -= n2) < n3) b = PREG_TSRS;
+        else { j -= n3; b = PREG_VACUUM; }
+        const unsigned id = bins[(long long) b * cap + j];
+        flux_vjp_tape_face(q, gas, tape, plane, fb, Ub, cx, cy, err, (long long) (id >> 1), (int) (id & 1u));
     }
 }
 
@@ -596,7 +646,7 @@ __global__ void __launch_bounds__(kThreads) ad_recon_vjp_kernel(const AdGeom q, 
         if (!nx_ && !ny_) continue;
         double w0[4], a0, o[4] = { 0, 0, 0, 0 };
         load_w(q, s.W, r, c, w0, a0);
-        const double inv_rho = dv(1.0, w0[0]), inv_p = dv(1.0, w0[3]);
+        const double inv_rho = rv(w0[0]), inv_p = rv(w0[3]);
         if (nx_) {
             double wm[4], wp[4], lob[4], hib[4], ox[4], A[4], B[4];
             load_w4(q, s.W, r, c - 1, wm);
@@ -750,6 +800,9 @@ struct HydroAdj2D {
      * recomputation and read by the reverse sweep */
     bool use_tape = true;
     double *tape_d = nullptr;
+    /* faces of a step binned by regime for the reverse HLLC (4 x 2 ncell) */
+    unsigned *bins_d = nullptr;
+    unsigned *bin_counts_d = nullptr;
     /* statistics */
     double forward_ms = 0, recompute_ms = 0, vjp_ms = 0, tangent_ms = 0, replay_ms = 0;
     long long launches = 0;
@@ -1061,7 +1114,6 @@ extern "C" int hydro_adj2d_create(const HydroGrid2D *grid, const HydroGpuOptions
     pa.g = grid->g;
     pa.pitch = tx;
     pa.strip_w = MH2D_THREADS - 2;
-    pa.chunk_h = opt->chunk_rows > 0 ? opt->chunk_rows : 32;
     for (int s = 0; s < 4; s++) pa.bc[s] = grid->bc[s];
     pa.dx = grid->dx;
     pa.dy = grid->dy;
@@ -1070,6 +1122,8 @@ extern "C" int hydro_adj2d_create(const HydroGrid2D *grid, const HydroGpuOptions
     pa.vol = grid->vol;
     pa.first_order = 0;
     pa.grid_ctas = mh2d_resident_ctas<double>(grid->limiter, 0, a->device);
+    pa.chunk_h = opt->chunk_rows > 0 ? opt->chunk_rows
+                                     : mh2d_default_chunk(pa.nx, pa.ny, pa.strip_w, pa.grid_ctas);
 
     /* initial state: interior W0, ghosts from the boundary rules, U0 = W->U(W0) */
     StateP<double> s0 = a->ckpt[0];
@@ -1195,6 +1249,10 @@ extern "C" int hydro_adj2d_backward(HydroAdj2D *a, double *const seed[4], double
             void *p;
             if (dalloc(a, (size_t) a->K * 2 * MH2D_TAPE_FIELDS * a->ncell * sizeof(double), &p, oc)) return -1;
             a->tape_d = static_cast<double *>(p);
+            if (dalloc(a, (size_t) 4 * 2 * a->ncell * sizeof(unsigned), &p, oc)) return -1;
+            a->bins_d = static_cast<unsigned *>(p);
+            if (dalloc(a, 4 * sizeof(unsigned), &p, oc)) return -1;
+            a->bin_counts_d = static_cast<unsigned *>(p);
         }
         tape_base = a->tape_d;
     }
@@ -1227,10 +1285,16 @@ extern "C" int hydro_adj2d_backward(HydroAdj2D *a, double *const seed[4], double
             const StateP<double> &st = slab(k);
             const double dt = a->dt_h[(size_t) k];
             if (tape_base) {
-                ad_flux_vjp_tape_kernel<<<nb, kThreads, 0, a->stream>>>(q, gas, tape_of(k), (long long) a->ncell,
-                                                                        a->faces_b, f4(a->Ub), dt * a->grid.area_x,
-                                                                        dt * a->grid.area_y, a->err_d);
+                const long long cap = 2 * (long long) a->ncell;
+                CK(cudaMemsetAsync(a->bin_counts_d, 0, 4 * sizeof(unsigned), a->stream), "cudaMemset(bins)");
+                ad_face_bins_kernel<<<nb, kThreads, 0, a->stream>>>(q, tape_of(k), (long long) a->ncell, a->bins_d,
+                                                                    a->bin_counts_d, cap);
+                CK(cudaGetLastError(), "face bins kernel");
+                ad_flux_vjp_bins_kernel<<<grid_for(cap), kThreads, 0, a->stream>>>(
+                    q, gas, tape_of(k), (long long) a->ncell, a->faces_b, f4(a->Ub), dt * a->grid.area_x,
+                    dt * a->grid.area_y, a->err_d, a->bins_d, a->bin_counts_d, cap);
                 CK(cudaGetLastError(), "flux vjp kernel");
+                a->launches++;
             } else {
                 if (launch_recon<double>(a, st, a->faces, dt, nullptr, BranchP{}, oc)) return -1;
                 ad_flux_vjp_kernel<<<nb, kThreads, 0, a->stream>>>(q, gas, a->faces, a->faces_b, f4(a->Ub),

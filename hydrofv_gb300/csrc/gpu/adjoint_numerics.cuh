@@ -163,17 +163,46 @@ HD int hllc_fwd(const GasConst<double> &c, double rl, double ul, double pl, doub
     s.pg = s.ppv;
     if (s.reg == PREG_TRRS) s.pg = guess_p_trrs(c, ul, pl, s.aL, ur, pr, s.aR);
     else if (s.reg == PREG_TSRS) s.pg = guess_p_tsrs(c, rl, ul, pl, rr, ur, pr, s.ppv);
-    s.ps = (s.pg < c.tol) ? c.tol : s.pg;
+    s.ps = lt(s.pg, c.tol) ? c.tol : s.pg;
     s.qL = hllc_q(c, pl, s.ps);
     s.qR = hllc_q(c, pr, s.ps);
     s.SL = ul - s.aL * s.qL;
     s.SR = ur + s.aR * s.qR;
     s.Ss = dv(pr - pl + rl * ul * (s.SL - ul) - rr * ur * (s.SR - ur),
               rl * (s.SL - ul) - rr * (s.SR - ur));
-    if (0.0 <= s.SL) s.region = 0;
-    else if (s.SL <= 0.0 && 0.0 <= s.Ss) s.region = 1;
-    else if (s.Ss <= 0.0 && 0.0 <= s.SR) s.region = 2;
-    else if (s.SR <= 0.0) s.region = 3;
+    if (le(0.0, s.SL)) s.region = 0;
+    else if (le(s.SL, 0.0) && le(0.0, s.Ss)) s.region = 1;
+    else if (le(s.Ss, 0.0) && le(0.0, s.SR)) s.region = 2;
+    else if (le(s.SR, 0.0)) s.region = 3;
+    else return DEV_ERR_HLLC_WAVE_SPEED;
+    return DEV_OK;
+}
+
+/* The intermediates of a non-vacuum face from the tape: sound speeds,
+ * unfloored guess, regime and the finish's q_L, q_R and S* as the forward
+ * pass computed them (the same values hllc_fwd_from_guess recomputes). */
+HD int hllc_fwd_from_tape(const GasConst<double> &c, double rl, double ul, double pl, double rr, double ur,
+                          double pr, double aL, double aR, double pg, int reg, double qL, double qR, double Ss,
+                          HllcFwd &s)
+{
+    s.aL = aL;
+    s.aR = aR;
+    s.reg = reg;
+    s.region = -1;
+    s.ppv = 0.5 * (pl + pr) - 0.125 * (ur - ul) * (rl + rr) * (aL + aR);
+    s.pg = pg;
+    s.ps = s.qL = s.qR = s.SL = s.SR = s.Ss = 0.0;
+    if (reg == PREG_VACUUM) return DEV_OK;
+    s.ps = lt(s.pg, c.tol) ? c.tol : s.pg;
+    s.qL = qL;
+    s.qR = qR;
+    s.SL = ul - s.aL * s.qL;
+    s.SR = ur + s.aR * s.qR;
+    s.Ss = Ss;
+    if (le(0.0, s.SL)) s.region = 0;
+    else if (le(s.SL, 0.0) && le(0.0, s.Ss)) s.region = 1;
+    else if (le(s.Ss, 0.0) && le(0.0, s.SR)) s.region = 2;
+    else if (le(s.SR, 0.0)) s.region = 3;
     else return DEV_ERR_HLLC_WAVE_SPEED;
     return DEV_OK;
 }
@@ -251,17 +280,17 @@ HD int hllc_fwd_from_guess(const GasConst<double> &c, double rl, double ul, doub
     s.pg = pg;
     s.ps = s.qL = s.qR = s.SL = s.SR = s.Ss = 0.0;
     if (reg == PREG_VACUUM) return DEV_OK;
-    s.ps = (s.pg < c.tol) ? c.tol : s.pg;
+    s.ps = lt(s.pg, c.tol) ? c.tol : s.pg;
     s.qL = hllc_q(c, pl, s.ps);
     s.qR = hllc_q(c, pr, s.ps);
     s.SL = ul - s.aL * s.qL;
     s.SR = ur + s.aR * s.qR;
     s.Ss = dv(pr - pl + rl * ul * (s.SL - ul) - rr * ur * (s.SR - ur),
               rl * (s.SL - ul) - rr * (s.SR - ur));
-    if (0.0 <= s.SL) s.region = 0;
-    else if (s.SL <= 0.0 && 0.0 <= s.Ss) s.region = 1;
-    else if (s.Ss <= 0.0 && 0.0 <= s.SR) s.region = 2;
-    else if (s.SR <= 0.0) s.region = 3;
+    if (le(0.0, s.SL)) s.region = 0;
+    else if (le(s.SL, 0.0) && le(0.0, s.Ss)) s.region = 1;
+    else if (le(s.Ss, 0.0) && le(0.0, s.SR)) s.region = 2;
+    else if (le(s.SR, 0.0)) s.region = 3;
     else return DEV_ERR_HLLC_WAVE_SPEED;
     return DEV_OK;
 }
@@ -324,8 +353,8 @@ HD void hllc_vjp_core(const GasConst<double> &c, const double L[4], const double
      * formed once as a reciprocal (a derivative, not a bit-parity value). */
     const double rl = L[0], ul = L[1], vl = L[2], pl = L[3];
     const double rr = Rs[0], ur = Rs[1], vr = Rs[2], pr = Rs[3];
-    const double inv_rl = dv(1.0, rl), inv_rr = dv(1.0, rr), inv_pl = dv(1.0, pl), inv_pr = dv(1.0, pr);
-    const double inv_gm1 = dv(1.0, c.gm1);
+    const double inv_rl = rv(rl), inv_rr = rv(rr), inv_pl = rv(pl), inv_pr = rv(pr);
+    const double inv_gm1 = c.inv_gm1;
     double rLb = 0, uLb = 0, vLb = 0, pLb = 0, rRb = 0, uRb = 0, vRb = 0, pRb = 0;
     double aLb = 0, aRb = 0;
     /* ---- region flux of the selected side K ---- */
@@ -345,9 +374,9 @@ HD void hllc_vjp_core(const GasConst<double> &c, const double L[4], const double
         const double S = left ? s.SL : s.SR;
         const double Ss = s.Ss;
         const double Smu = S - u, SmS = S - Ss;
-        const double inv_SmS = dv(1.0, SmS);
+        const double inv_SmS = rv(SmS);
         const double D = rho * Smu;
-        const double inv_D = dv(1.0, D);
+        const double inv_D = rv(D);
         const double rs = D * inv_SmS;
         const double pD = p * inv_D;
         const double Z = Ss + pD;
@@ -394,7 +423,7 @@ HD void hllc_vjp_core(const GasConst<double> &c, const double L[4], const double
     else { rRb += rhob; uRb += ub; vRb += vb; pRb += pb; }
 
     /* ---- S* ---- */
-    if (Ssb != 0.0) {
+    if (!eq_zero(Ssb)) {
         const double dL = s.SL - ul, dR = s.SR - ur;
         const double Dd = rl * dL - rr * dR;
         const double Nnb = dv(Ssb, Dd);
@@ -417,17 +446,17 @@ HD void hllc_vjp_core(const GasConst<double> &c, const double L[4], const double
     aRb += SRb * s.qR;
     const double qRb = SRb * s.aR;
     double psb = 0.0;
-    if (s.ps > pl) {
+    if (lt(pl, s.ps)) {
         const double t = dv(qLb * (0.5 * c.q_coef), s.qL) * inv_pl;
         psb += t;
         pLb -= t * s.ps * inv_pl;
     }
-    if (s.ps > pr) {
+    if (lt(pr, s.ps)) {
         const double t = dv(qRb * (0.5 * c.q_coef), s.qR) * inv_pr;
         psb += t;
         pRb -= t * s.ps * inv_pr;
     }
-    const double pgb = (s.pg < c.tol) ? 0.0 : psb;
+    const double pgb = lt(s.pg, c.tol) ? 0.0 : psb;
 
     /* ---- star-pressure guess ---- */
     double ppvb = 0.0;
@@ -436,7 +465,7 @@ HD void hllc_vjp_core(const GasConst<double> &c, const double L[4], const double
     } else if (s.reg == PREG_TRRS) {
         const double zL = have_z ? z0 : pw(pl, c.half_gm1_g);
         const double zR = have_z ? z1 : pw(pr, c.half_gm1_g);
-        const double izL = dv(1.0, zL), izR = dv(1.0, zR);
+        const double izL = rv(zL), izR = rv(zR);
         const double num = s.aL + s.aR - c.half_gm1 * (ur - ul);
         const double den = s.aL * izL + s.aR * izR;
         /* pg = (num / den)^(1/hg): d pg = (pg / hg) (d num / num - d den / den) */
@@ -469,7 +498,7 @@ HD void hllc_vjp_core(const GasConst<double> &c, const double L[4], const double
         pLb += BLb * c.gm1_gp1;
         pRb += BRb * c.gm1_gp1;
     }
-    if (ppvb != 0.0) {
+    if (!eq_zero(ppvb)) {
         pLb += 0.5 * ppvb;
         pRb += 0.5 * ppvb;
         const double du = ur - ul, sr = rl + rr, sa = s.aL + s.aR;

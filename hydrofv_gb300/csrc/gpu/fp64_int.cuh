@@ -293,6 +293,15 @@ static __device__ __noinline__ double div_dev(double a, double b)
     return ok ? q : div_hw(a, b);
 }
 
+/* 1 / x: the divide with a known numerator, which the compiler folds into
+ * the integer sequence (the quotient step becomes a shift of Y1). */
+static __device__ __noinline__ double rcp_dev(double x)
+{
+    bool ok;
+    const double q = div_fast(1.0, x, ok);
+    return ok ? q : div_hw(1.0, x);
+}
+
 static __device__ __noinline__ double sqrt_dev(double x)
 {
     bool ok;
@@ -311,6 +320,19 @@ FXHD R dv(R a, R b) { return a / b; }
 
 template <class R>
 FXHD R sq(R x) { return sqrt(x); }
+
+/* 1 / x as the kernels evaluate it (the value of dv(1, x)). */
+template <class R>
+FXHD R rv(R x) { return R(1) / x; }
+
+FXHD double rv(double x)
+{
+#if defined(__CUDA_ARCH__)
+    return fx::rcp_dev(x);
+#else
+    return 1.0 / x;
+#endif
+}
 
 FXHD double dv(double a, double b)
 {
@@ -358,6 +380,19 @@ FXHD double zero_minus(double x)
     return fx::from_bits((u << 1) == 0ull ? 0ull : (u ^ fx::SIGN));
 #else
     return 0.0 - x;
+#endif
+}
+
+/* x == 0.0 (either zero; false for NaN), on the bits for double on the device. */
+template <class R>
+FXHD bool eq_zero(R x) { return x == R(0); }
+
+FXHD bool eq_zero(double x)
+{
+#if defined(__CUDA_ARCH__)
+    return (fx::bits(x) << 1) == 0ull;
+#else
+    return x == 0.0;
 #endif
 }
 

@@ -76,12 +76,13 @@ struct Mh2dArgs {
  * (x fields first, then y): the face states (4 + 4, normal velocity in
  * slot 1), both sound speeds, the star-pressure guess before the floor, the
  * guess's factors (p^((g-1)/2g) of each side for the two-rarefaction guess,
- * g_K of each side for the two-shock guess) and the regime.
+ * g_K of each side for the two-shock guess), the regime, and the wave-speed
+ * factors q_L, q_R and S* of the finish (zero for vacuum faces).
  */
-#define MH2D_TAPE_FIELDS 14
+#define MH2D_TAPE_FIELDS 17
 enum : int {
     TAPE_L = 0, TAPE_R = 4, TAPE_AL = 8, TAPE_AR = 9, TAPE_PG = 10, TAPE_Z0 = 11, TAPE_Z1 = 12,
-    TAPE_REG = 13,
+    TAPE_REG = 13, TAPE_QL = 14, TAPE_QR = 15, TAPE_SS = 16,
 };
 
 /* Where solve_faces writes the tape of a batch: faces [0, nxf) are x faces
@@ -252,6 +253,19 @@ __device__ __forceinline__ int solve_faces(Mh2dShared<R, NT> &sm, const GasConst
         }
         if (sm.reg[f] == PREG_VACUUM) {
             vacuum_flux_dev(gas, rl, ul, vl, pl, sm.aL[f], rr, ur, vr, pr, sm.aR[f], F);
+            if constexpr (TAPE) {
+                *tc.field(f, TAPE_QL) = R(0);
+                *tc.field(f, TAPE_QR) = R(0);
+                *tc.field(f, TAPE_SS) = R(0);
+            }
+        } else if constexpr (TAPE) {
+            R wave[3];
+            const int rc = hllc_finish(gas, rl, ul, vl, pl, sm.aL[f], rr, ur, vr, pr, sm.aR[f],
+                                       sm.pg[f], F, wave);
+            if (rc) err = rc;
+            *tc.field(f, TAPE_QL) = wave[0];
+            *tc.field(f, TAPE_QR) = wave[1];
+            *tc.field(f, TAPE_SS) = wave[2];
         } else {
             const int rc = hllc_finish(gas, rl, ul, vl, pl, sm.aL[f], rr, ur, vr, pr, sm.aR[f],
                                        sm.pg[f], F);

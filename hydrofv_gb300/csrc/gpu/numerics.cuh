@@ -87,6 +87,7 @@ struct GasConst {
     R gp1_2g;       /* (gamma + 1.0) / (2.0 * gamma) */
     R neg_gp1_2g;   /* -0.5 * (gamma + 1.0) / gamma */
     R inv_g;        /* 1.0 / gamma */
+    R inv_gm1;      /* 1.0 / (gamma - 1.0) (the adjoint's reverse code) */
     R tol;          /* integrator tolerance (guess_p floor, exact solver) */
 };
 
@@ -110,6 +111,7 @@ HD GasConst<R> make_gas_const(double gamma, double tol)
     c.gp1_2g = (R) ((gamma + 1.0) / (2.0 * gamma));
     c.neg_gp1_2g = (R) (-0.5 * (gamma + 1.0) / gamma);
     c.inv_g = (R) (1.0 / gamma);
+    c.inv_gm1 = (R) (1.0 / (gamma - 1.0));
     c.tol = (R) tol;
     return c;
 }
@@ -365,16 +367,20 @@ HD void hllc_vacuum_flux(const GasConst<R> &c, R rho_L, R u_L, R v_L, R p_L, R a
 }
 
 /* From the (unfloored) star-pressure guess to the flux.  Returns DEV_OK or
- * DEV_ERR_HLLC_WAVE_SPEED. */
+ * DEV_ERR_HLLC_WAVE_SPEED.  wave (may be null) receives q_L, q_R and S*, the
+ * intermediates the adjoint's tape keeps. */
 template <class R>
 HD int hllc_finish(const GasConst<R> &c, R rho_L, R u_L, R v_L, R p_L, R a_L,
-                   R rho_R, R u_R, R v_R, R p_R, R a_R, R pg, R F[4])
+                   R rho_R, R u_R, R v_R, R p_R, R a_R, R pg, R F[4], R *wave = nullptr)
 {
     const R ps = lt(pg, c.tol) ? c.tol : pg;
-    const R S_L = u_L - a_L * hllc_q(c, p_L, ps);
-    const R S_R = u_R + a_R * hllc_q(c, p_R, ps);
+    const R q_L = hllc_q(c, p_L, ps);
+    const R q_R = hllc_q(c, p_R, ps);
+    const R S_L = u_L - a_L * q_L;
+    const R S_R = u_R + a_R * q_R;
     const R S_s = dv(p_R - p_L + rho_L * u_L * (S_L - u_L) - rho_R * u_R * (S_R - u_R),
                      rho_L * (S_L - u_L) - rho_R * (S_R - u_R));
+    if (wave) { wave[0] = q_L; wave[1] = q_R; wave[2] = S_s; }
     int region;
     if (le(R(0), S_L)) region = 0;
     else if (le(S_L, R(0)) && le(R(0), S_s)) region = 1;

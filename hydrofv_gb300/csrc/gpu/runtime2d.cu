@@ -135,7 +135,6 @@ static void setup_args(HydroRun2D *run, Mh2dArgs<R> &a, const HydroGrid2D *grid,
     a.g = grid->g;
     a.pitch = run->tx;
     a.strip_w = MH2D_THREADS - 2;
-    a.chunk_h = opt->chunk_rows > 0 ? opt->chunk_rows : 32;
     for (int s = 0; s < 4; s++) a.bc[s] = grid->bc[s];
     a.dx = grid->dx;
     a.dy = grid->dy;
@@ -144,6 +143,8 @@ static void setup_args(HydroRun2D *run, Mh2dArgs<R> &a, const HydroGrid2D *grid,
     a.vol = grid->vol;
     a.first_order = (grid->integrator == INTEGRATOR_GODUNOV_FIRST_ORDER_2D) ? 1 : 0;
     a.grid_ctas = mh2d_resident_ctas<R>(grid->limiter, a.first_order, run->device);
+    a.chunk_h = opt->chunk_rows > 0 ? opt->chunk_rows
+                                    : mh2d_default_chunk(a.nx, a.ny, a.strip_w, a.grid_ctas);
     a.gravity = grid->gravity;
 }
 

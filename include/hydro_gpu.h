@@ -37,7 +37,7 @@ typedef struct HydroGpuOptions
     int chunk_steps;        /* steps enqueued between host polls (0: auto) */
     int use_graph;          /* replay step chunks as CUDA graphs (default 1) */
     int block_threads;      /* threads per step CTA (0: tuned default) */
-    int chunk_rows;         /* grid rows per step work item (0: default 32) */
+    int chunk_rows;         /* grid rows per step work item (0: chosen from the grid shape and the resident CTAs) */
     int autotune;           /* 1: before the first step, time candidate work-item
                                shapes and persistent grid sizes on the actual
                                state (then rewind) and keep the fastest; cached
