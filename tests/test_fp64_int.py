@@ -333,3 +333,22 @@ def test_gpu_limiters_match_the_fp64_expressions(op):
     host, _ = h.fx_eval_host(op, a, b)
     assert _same_bits(fast, host).all()
     assert ok[: 1 << 21].mean() > 0.99
+
+
+def test_pow_tables_match_their_generator():
+    """pow_tables.h is generated by gen_pow_tables.py (300-bit mpmath); the
+    committed header must be exactly its output."""
+    pytest.importorskip("mpmath")
+    import contextlib
+    import importlib.util
+    import io
+    import os
+    here = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "hydrofv_gb300", "csrc", "gpu")
+    spec = importlib.util.spec_from_file_location("gen_pow_tables", os.path.join(here, "gen_pow_tables.py"))
+    gen = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(gen)
+    buf = io.StringIO()
+    with contextlib.redirect_stdout(buf):
+        gen.main()
+    with open(os.path.join(here, "pow_tables.h")) as f:
+        assert buf.getvalue() == f.read()
