@@ -187,12 +187,16 @@ _SIGNATURES = {
     "hydro_fx_eval_host": (None, [C.c_int, C.c_longlong, _dp, _dp, _dp, C.c_void_p]),
     "hydro_gpu_fx_eval": (C.c_int, [C.c_int, C.c_int, C.c_longlong, _dp, _dp, _dp, _dp, C.c_void_p]),
     "hydro_fx_div_seeded_host": (None, [C.c_longlong, _dp, _dp, C.c_void_p, _dp, C.c_void_p]),
+    "hydro_gpu_pointwise_eval": (C.c_int, [C.c_int, C.c_int, C.c_longlong, _dp, C.c_double, _dp, _dp, _dp,
+                                           _dp, _P(C.c_int)]),
     "hydro_gpu_device_count": (C.c_int, []),
     "hydro_gpu_calibrate": (C.c_int, [C.c_int, _dp, _dp]),
     "hydro_gpu_version": (C.c_char_p, []),
     "free_traceback": (None, [_P(ErrorStatus)]),
     "solve_flux_hllc_2d": (ErrorStatus, [_dp] * 4 + [C.c_double] * 10),
     "solve_flux_exact_1d": (ErrorStatus, [_dp] * 3 + [C.c_double] * 9 + [C.c_int]),
+    "solve_flux_hllc_1d": (ErrorStatus, [_dp] * 3 + [C.c_double] * 8),
+    "solve_exact_1d": (ErrorStatus, [_dp] * 3 + [C.c_double] * 9 + [C.c_int]),
     "guess_p": (C.c_double, [C.c_double] * 10),
     "limit_slope": (ErrorStatus, [_dp, _P(IntegratorParam), C.c_double, C.c_double]),
     "get_time_step_2d": (C.c_double, [_P(System), C.c_double]),
@@ -840,6 +844,36 @@ def gpu_fx_eval(op, a, b=None, device=0):
     if rc != 0:
         raise HydroError(rc, "hydro_gpu_fx_eval failed (CUDA error)")
     return fast, hw, ok.astype(bool)
+
+
+POINTWISE_OPS = {"hllc_2d": (0, 4), "guess_p": (1, 1), "exact_flux_1d": (2, 3), "hllc_1d": (3, 3),
+                 "exact_1d": (4, 3)}
+
+
+def gpu_pointwise_eval(name, gamma, L, R, aux=None, tol=1e-6, device=0):
+    """Device build of an exported pointwise function over n state pairs
+    (L, R: (n, 4) arrays of rho, u, v, p; gamma: (n,)): (outputs, return
+    codes).  name: "hllc_2d", "hllc_1d", "guess_p" (aux = (n, 2) sound
+    speeds a_L, a_R), "exact_flux_1d" or "exact_1d" (aux = (n,) sample
+    speeds).  Return codes: 0, 1 (HLLC wave speed), 3 or 4 (exact solver)."""
+    op, width = POINTWISE_OPS[name]
+    g = np.ascontiguousarray(gamma, dtype=np.float64).ravel()
+    n = g.size
+    L = np.ascontiguousarray(L, dtype=np.float64).reshape(n, 4)
+    R = np.ascontiguousarray(R, dtype=np.float64).reshape(n, 4)
+    need = {1: 2, 2: 1, 4: 1}.get(op, 0)
+    a = np.ascontiguousarray(np.zeros(n * max(need, 1)) if aux is None else aux, dtype=np.float64).ravel()
+    if a.size < n * need:
+        raise ValueError(f"{name} needs {need} auxiliary values per state pair")
+    out = np.empty(n * width)
+    rc = np.empty(n, dtype=np.int32)
+    code = library().hydro_gpu_pointwise_eval(int(device), op, n, g.ctypes.data_as(_dp), float(tol),
+                                              L.ctypes.data_as(_dp), R.ctypes.data_as(_dp),
+                                              a.ctypes.data_as(_dp), out.ctypes.data_as(_dp),
+                                              rc.ctypes.data_as(_P(C.c_int)))
+    if code != 0:
+        raise HydroError(code, "hydro_gpu_pointwise_eval failed (CUDA error)")
+    return (out if width == 1 else out.reshape(n, width)), rc
 
 
 def fx_div_seeded_host(a, b, seed_scale):

@@ -1,8 +1,14 @@
 /*
- * fx_check.cu -- evaluation entry points for the integer-pipe FP64 division
- * and square root (fp64_int.cuh), used by the tests: the host build over
- * arrays (checked on the CPU against the host's IEEE operations), and the
- * device build next to the hardware operations on the GPU.
+ * fx_check.cu -- evaluation entry points used by the tests:
+ *  - the integer-pipe FP64 division, square root and power (fp64_int.cuh,
+ *    pow_int.cuh) over arrays: the host build (checked on the CPU against
+ *    the host's IEEE operations and libm) and the device build next to the
+ *    hardware operations on the GPU;
+ *  - the device build of the exported pointwise numerics (HLLC fluxes,
+ *    guess_p, the exact solver) over arrays of states, so that the kernels'
+ *    arithmetic is checked against the reference's known answers branch by
+ *    branch (vacuum generation, TRRS, TSRS, rarefaction and shock sampling),
+ *    including branches that whole simulations rarely reach.
  */
 #include <cuda_runtime.h>
 
@@ -47,6 +53,40 @@ __global__ void fx_eval_kernel(int op, long long n, const double *a, const doubl
             hw[i] = f;
         }
         ok[i] = k ? 1 : 0;
+    }
+}
+
+/* The exported pointwise numerics, device build (one state pair per thread;
+ * the gas constants are formed per element because gamma varies). */
+__global__ void pointwise_kernel(int op, long long n, const double *gamma, double tol,
+                                 const double *L, const double *R, const double *aux, double *out,
+                                 int *rc)
+{
+    const long long stride = (long long) gridDim.x * blockDim.x;
+    for (long long k = (long long) blockIdx.x * blockDim.x + threadIdx.x; k < n; k += stride) {
+        const GasConst<double> c = make_gas_const<double>(gamma[k], tol);
+        const double *l = L + 4 * k, *r = R + 4 * k;
+        int code = DEV_OK;
+        if (op == 0) {
+            double F[4];
+            code = hllc_flux_2d(c, l[0], l[1], l[2], l[3], r[0], r[1], r[2], r[3], F);
+            for (int q = 0; q < 4; q++) out[4 * k + q] = F[q];
+        } else if (op == 1) {
+            out[k] = guess_p(c, l[0], l[1], l[3], aux[2 * k], r[0], r[1], r[3], aux[2 * k + 1]);
+        } else if (op == 2) {
+            double F[3];
+            code = exact_flux_1d(c, l[0], l[1], l[3], r[0], r[1], r[3], aux[k], F);
+            for (int q = 0; q < 3; q++) out[3 * k + q] = F[q];
+        } else if (op == 3) {
+            double F[3];
+            code = hllc_flux_1d(c, l[0], l[1], l[3], r[0], r[1], r[3], F);
+            for (int q = 0; q < 3; q++) out[3 * k + q] = F[q];
+        } else {
+            double o[3];
+            code = exact_solve_1d(c, l[0], l[1], l[3], r[0], r[1], r[3], aux[k], o);
+            for (int q = 0; q < 3; q++) out[3 * k + q] = o[q];
+        }
+        rc[k] = code;
     }
 }
 
@@ -106,6 +146,37 @@ int hydro_gpu_fx_eval(int device, int op, long long n, const double *a, const do
     if (e == cudaSuccess) e = cudaMemcpy(fast, df, nb, cudaMemcpyDeviceToHost);
     if (e == cudaSuccess) e = cudaMemcpy(hw, dh, nb, cudaMemcpyDeviceToHost);
     if (e == cudaSuccess) e = cudaMemcpy(ok, dk, (size_t) n, cudaMemcpyDeviceToHost);
+    cudaFree(slab);
+    return (int) e;
+}
+
+int hydro_gpu_pointwise_eval(int device, int op, long long n, const double *gamma, double tol,
+                             const double *L, const double *R, const double *aux, double *out,
+                             int *rc)
+{
+    if (n <= 0) return 0;
+    if (op < 0 || op > 4) return (int) cudaErrorInvalidValue;
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) return (int) e;
+    const int width = (op == 0) ? 4 : (op == 1) ? 1 : 3;
+    const int naux = (op == 1) ? 2 : (op == 2 || op == 4) ? 1 : 0;
+    const size_t nb = (size_t) n * sizeof(double);
+    char *slab = nullptr;
+    e = cudaMalloc(&slab, (9 + naux + width) * nb + (size_t) n * sizeof(int));
+    if (e != cudaSuccess) return (int) e;
+    double *dg = (double *) slab, *dl = dg + n, *dr = dl + 4 * n, *da = dr + 4 * n;
+    double *dout = da + naux * n;
+    int *drc = (int *) (dout + width * n);
+    e = cudaMemcpy(dg, gamma, nb, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(dl, L, 4 * nb, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(dr, R, 4 * nb, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && naux) e = cudaMemcpy(da, aux, naux * nb, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        pointwise_kernel<<<152, 128>>>(op, n, dg, tol, dl, dr, da, dout, drc);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(out, dout, width * nb, cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(rc, drc, (size_t) n * sizeof(int), cudaMemcpyDeviceToHost);
     cudaFree(slab);
     return (int) e;
 }

@@ -355,6 +355,26 @@ int hydro_gpu_fx_eval(int device, int op, long long n, const double *a, const do
 void hydro_fx_div_seeded_host(long long n, const double *a, const double *b, const float *seed_scale,
                               double *out, unsigned char *ok);
 
+/* Device build of the exported pointwise numerics over n state pairs:
+ * L[4k..4k+3], R[4k..4k+3] = (rho, u, v, p) (the 1D forms read rho, u, p),
+ * gas constants from gamma[k] and tol.
+ *   op 0: solve_flux_hllc_2d (src/riemann_solver_hllc.h:46-61): out[4k..4k+3]
+ *   op 1: guess_p (src/riemann_solver.h:123-134), a_L = aux[2k],
+ *         a_R = aux[2k+1]: out[k]
+ *   op 2: solve_flux_exact_1d at speed aux[k] (src/riemann_solver_exact.h:73-87):
+ *         out[3k..3k+2]
+ *   op 3: solve_flux_hllc_1d (src/riemann_solver_hllc.h:32-44): out[3k..3k+2]
+ *   op 4: solve_exact_1d at speed aux[k] (src/riemann_solver_exact.h:37-51):
+ *         the sampled (rho, u, p) in out[3k..3k+2]
+ * rc[k] = 0, or 1 (HLLC wave-speed error), 3 (exact solver: no bracket),
+ * 4 (exact solver: bisection did not converge).  These are the functions the
+ * step kernels call, compiled for the GPU, so the tests can check them
+ * against the reference's known answers branch by branch.  Returns a
+ * cudaError_t. */
+int hydro_gpu_pointwise_eval(int device, int op, long long n, const double *gamma, double tol,
+                             const double *L, const double *R, const double *aux, double *out,
+                             int *rc);
+
 /* Number of visible CUDA devices (0 when none; never fails). */
 int hydro_gpu_device_count(void);
 

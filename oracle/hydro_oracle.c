@@ -1337,6 +1337,20 @@ int oracle_exact_flux_1d(double gamma, double rho_L, double u_L, double p_L,
     return exact_flux_1d(gamma, rho_L, u_L, p_L, rho_R, u_R, p_R, tol, speed, out3);
 }
 
+int oracle_hllc_1d(double gamma, double rho_L, double u_L, double p_L,
+                   double rho_R, double u_R, double p_R, double tol, double *out3)
+{
+    return hllc_1d(gamma, rho_L, u_L, p_L, rho_R, u_R, p_R, tol, out3);
+}
+
+/* solve_exact_1d (src/riemann_solver_exact.c:332-469): the state sampled at
+ * x/t = speed, as (rho, u, p). */
+int oracle_exact_1d(double gamma, double rho_L, double u_L, double p_L,
+                    double rho_R, double u_R, double p_R, double tol, double speed, double *out3)
+{
+    return exact_state_1d(gamma, rho_L, u_L, p_L, rho_R, u_R, p_R, tol, speed, out3);
+}
+
 double oracle_guess_p(double gamma, double rho_L, double u_L, double p_L, double a_L,
                       double rho_R, double u_R, double p_R, double a_R, double tol)
 {

@@ -68,6 +68,10 @@ int oracle_hllc_2d(double gamma, double rho_L, double u_L, double v_L, double p_
 int oracle_exact_flux_1d(double gamma, double rho_L, double u_L, double p_L,
                          double rho_R, double u_R, double p_R, double tol, double speed,
                          double *out3);
+int oracle_hllc_1d(double gamma, double rho_L, double u_L, double p_L,
+                   double rho_R, double u_R, double p_R, double tol, double *out3);
+int oracle_exact_1d(double gamma, double rho_L, double u_L, double p_L,
+                    double rho_R, double u_R, double p_R, double tol, double speed, double *out3);
 double oracle_guess_p(double gamma, double rho_L, double u_L, double p_L, double a_L,
                       double rho_R, double u_R, double p_R, double a_R, double tol);
 int oracle_limit_slope(int limiter_flag, double a, double b, double *out);

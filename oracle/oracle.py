@@ -72,6 +72,12 @@ def _bind(lib: C.CDLL, prefix: str) -> C.CDLL:
     f = getattr(lib, prefix + "exact_flux_1d")
     f.restype = C.c_int
     f.argtypes = [C.c_double] * 9 + [_dp]
+    f = getattr(lib, prefix + "hllc_1d")
+    f.restype = C.c_int
+    f.argtypes = [C.c_double] * 8 + [_dp]
+    f = getattr(lib, prefix + "exact_1d")
+    f.restype = C.c_int
+    f.argtypes = [C.c_double] * 9 + [_dp]
     f = getattr(lib, prefix + "guess_p")
     f.restype = C.c_double
     f.argtypes = [C.c_double] * 10
@@ -172,6 +178,17 @@ class Backend:
     def exact_flux_1d(self, gamma, L, R, tol=1e-6, speed=0.0):
         out = np.zeros(3)
         rc = getattr(self.lib, self.prefix + "exact_flux_1d")(gamma, *L, *R, tol, speed, _ptr(out))
+        return rc, out
+
+    def hllc_1d(self, gamma, L, R, tol=1e-6):
+        out = np.zeros(3)
+        rc = getattr(self.lib, self.prefix + "hllc_1d")(gamma, *L, *R, tol, _ptr(out))
+        return rc, out
+
+    def exact_1d(self, gamma, L, R, tol=1e-6, speed=0.0):
+        """solve_exact_1d: the exact solution sampled at x/t = speed, (rho, u, p)."""
+        out = np.zeros(3)
+        rc = getattr(self.lib, self.prefix + "exact_1d")(gamma, *L, *R, tol, speed, _ptr(out))
         return rc, out
 
     def guess_p(self, gamma, rho_L, u_L, p_L, a_L, rho_R, u_R, p_R, a_R, tol=1e-6):

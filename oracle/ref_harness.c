@@ -286,7 +286,7 @@ int ref_run_1d_ex(
 }
 
 /* Pointwise known-answer helpers: thin pass-throughs to exported reference
- * functions (src/riemann_solver_hllc.h:43-61, src/riemann_solver_exact.h:37-87,
+ * functions (src/riemann_solver_hllc.h:32-61, src/riemann_solver_exact.h:37-87,
  * src/riemann_solver.h:144-186, src/slope_limiter.h:24-47). */
 int ref_hllc_2d(double gamma, double rho_L, double u_L, double v_L, double p_L,
                 double rho_R, double u_R, double v_R, double p_R, double tol, double *out4)
@@ -303,6 +303,26 @@ int ref_exact_flux_1d(double gamma, double rho_L, double u_L, double p_L,
 {
     ErrorStatus e = solve_flux_exact_1d(&out3[0], &out3[1], &out3[2], gamma,
                                         rho_L, u_L, p_L, rho_R, u_R, p_R, tol, speed, 0);
+    int rc = e.return_code;
+    free_traceback(&e);
+    return rc;
+}
+
+int ref_hllc_1d(double gamma, double rho_L, double u_L, double p_L,
+                double rho_R, double u_R, double p_R, double tol, double *out3)
+{
+    ErrorStatus e = solve_flux_hllc_1d(&out3[0], &out3[1], &out3[2], gamma,
+                                       rho_L, u_L, p_L, rho_R, u_R, p_R, tol);
+    int rc = e.return_code;
+    free_traceback(&e);
+    return rc;
+}
+
+int ref_exact_1d(double gamma, double rho_L, double u_L, double p_L,
+                 double rho_R, double u_R, double p_R, double tol, double speed, double *out3)
+{
+    ErrorStatus e = solve_exact_1d(&out3[0], &out3[1], &out3[2], gamma,
+                                   rho_L, u_L, p_L, rho_R, u_R, p_R, tol, speed, 0);
     int rc = e.return_code;
     free_traceback(&e);
     return rc;

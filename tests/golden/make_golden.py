@@ -1,7 +1,7 @@
 """Generate the golden fixtures in tests/golden/ from the unmodified reference.
 
     make -C oracle ref          # compiles the reference's src/*.c into oracle/_ref
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [name ...]   # all fixtures, or the named ones
 
 Each fixture stores the reference's outputs (final W and U, status) for a
 seeded problem from hydrofv_gb300.problems, plus a checksum of the inputs so a
@@ -110,6 +110,14 @@ def pointwise(ref):
     speeds[: m // 2] = 0.0
     for k in range(m):
         ex_rc[k], ex[k] = ref.exact_flux_1d(gam[k], L[k, [0, 1, 3]], R[k, [0, 1, 3]], speed=speeds[k])
+    # the 1D HLLC flux and the sampled exact solution on the same states
+    hllc1 = np.zeros((m, 3))
+    hllc1_rc = np.zeros(m, dtype=np.int32)
+    ex_state = np.zeros((m, 3))
+    ex_state_rc = np.zeros(m, dtype=np.int32)
+    for k in range(m):
+        hllc1_rc[k], hllc1[k] = ref.hllc_1d(gam[k], L[k, [0, 1, 3]], R[k, [0, 1, 3]])
+        ex_state_rc[k], ex_state[k] = ref.exact_1d(gam[k], L[k, [0, 1, 3]], R[k, [0, 1, 3]], speed=speeds[k])
     gp = np.array([ref.guess_p(gam[k], L[k, 0], L[k, 1], L[k, 3], np.sqrt(gam[k] * L[k, 3] / max(L[k, 0], 1e-30)),
                                R[k, 0], R[k, 1], R[k, 3], np.sqrt(gam[k] * R[k, 3] / max(R[k, 0], 1e-30)))
                    for k in range(n)])
@@ -122,7 +130,8 @@ def pointwise(ref):
         for k in range(1000):
             lim[f - 1, k] = ref.limit_slope(f, a[k], b[k])[1]
     return dict(gamma=gam, L=L, R=R, hllc=hllc, hllc_rc=hllc_rc, speeds=speeds, exact=ex,
-                exact_rc=ex_rc, guess_p=gp, lim_a=a, lim_b=b, limited=lim)
+                exact_rc=ex_rc, guess_p=gp, lim_a=a, lim_b=b, limited=lim, hllc_1d=hllc1,
+                hllc_1d_rc=hllc1_rc, exact_state=ex_state, exact_state_rc=ex_state_rc)
 
 
 def main():
@@ -130,18 +139,28 @@ def main():
         sys.exit("oracle/_ref not built: run `make -C oracle ref` where the reference tree exists")
     ref = O.load("ref")
     ref_serial = O.load("ref_serial")
+    only = set(sys.argv[1:])
+
+    def wanted(name):
+        return not only or name in only
+
     for name, p in cases_2d().items():
+        if not wanted(name):
+            continue
         r = ref.run_2d(p)
         np.savez_compressed(os.path.join(HERE, f"{name}.npz"), W=r.W, U=r.U, rc=r.rc,
                             num_steps=r.num_steps, t=r.t, dt=r.dt, input_sha=digest(p.W, p.U))
         print(name, r.rc, r.num_steps, r.t)
     for name, p in cases_1d().items():
+        if not wanted(name):
+            continue
         r = ref_serial.run_1d(p)  # the reference's OpenMP 1D loops race; serial build
         np.savez_compressed(os.path.join(HERE, f"{name}.npz"), W=r.W, U=r.U, rc=r.rc,
                             num_steps=r.num_steps, t=r.t, dt=r.dt, input_sha=digest(p.W, p.U))
         print(name, r.rc, r.num_steps, r.t)
-    np.savez_compressed(os.path.join(HERE, "pointwise.npz"), **pointwise(ref))
-    print("pointwise done")
+    if wanted("pointwise"):
+        np.savez_compressed(os.path.join(HERE, "pointwise.npz"), **pointwise(ref))
+        print("pointwise done")
 
 
 if __name__ == "__main__":

@@ -90,6 +90,14 @@ def test_restatement_pointwise_matches_golden(oracle_mod):
         assert rc == g["exact_rc"][k]
         if rc == 0:
             assert bits_equal(f, g["exact"][k]), k
+    for k in range(len(g["speeds"])):
+        L3, R3 = g["L"][k, [0, 1, 3]], g["R"][k, [0, 1, 3]]
+        rc, f = orc.hllc_1d(g["gamma"][k], L3, R3)
+        assert rc == g["hllc_1d_rc"][k]
+        assert bits_equal(f, g["hllc_1d"][k]), k
+        rc, s = orc.exact_1d(g["gamma"][k], L3, R3, speed=g["speeds"][k])
+        assert rc == g["exact_state_rc"][k]
+        assert bits_equal(s, g["exact_state"][k]), k
     for f in (1, 2, 3):
         got = np.array([orc.limit_slope(f, a, b)[1] for a, b in zip(g["lim_a"], g["lim_b"])])
         assert bits_equal(got, g["limited"][f - 1])
@@ -136,6 +144,18 @@ def test_library_pointwise_exports_match_golden(hydro_lib):
                 worst = max(worst, float(err.max()))
     # identical algorithm; only libm pow may differ from glibc's by an ulp
     assert worst <= 1e-14
+    for k in range(len(g["speeds"])):
+        L, R = g["L"][k], g["R"][k]
+        e = lib.solve_flux_hllc_1d(*[C.byref(o) for o in out[:3]], g["gamma"][k], L[0], L[1], L[3],
+                                   R[0], R[1], R[3], 1e-6)
+        code, _ = H._consume(lib, e)
+        assert code == g["hllc_1d_rc"][k]
+        assert bits_equal(np.array([o.value for o in out[:3]]), g["hllc_1d"][k]), k
+        e = lib.solve_exact_1d(*[C.byref(o) for o in out[:3]], g["gamma"][k], L[0], L[1], L[3],
+                               R[0], R[1], R[3], 1e-6, g["speeds"][k], 0)
+        code, _ = H._consume(lib, e)
+        assert code == g["exact_state_rc"][k]
+        assert bits_equal(np.array([o.value for o in out[:3]]), g["exact_state"][k]), k
     ip = H.IntegratorParam()
     res = C.c_double()
     for f in (1, 2, 3):
