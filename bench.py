@@ -445,6 +445,83 @@ def run_snapshots(args, H, device, ws, rank) -> None:
     print(json.dumps(line))
 
 
+def run_sod(args, H, device, ws, rank) -> None:
+    """The Sod tube (1000 cells, Godunov first order + exact solver, CFL 0.9,
+    t = 0.2: 496 time steps) through the drop-in call.  One "step" here is one
+    whole run: a latency workload, reported as time per run and as
+    cell-updates/s (cells x time steps per second).  value: the device time of
+    the stepping (CUDA events inside the call); e2e: the wall clock of the
+    call with the host arrays (upload, stepping, download).  cpu_baseline:
+    the serial CPU implementation (the reference's 1D OpenMP loops race, so
+    the serial build is the one to compare with)."""
+    from hydrofv_gb300.problems import sod_1d
+    p = sod_1d(1000)
+    opts = H.default_options(device=device)
+
+    def run():
+        return H.run_1d(p.nx, p.g, (p.x_min, p.x_max), p.gamma, p.W, p.U, bc=p.bc,
+                        integrator=p.integrator, riemann_solver=p.riemann_solver,
+                        slope_limiter=p.slope_limiter, cfl=p.cfl, tf=p.tf, max_steps=-1,
+                        options=opts)
+
+    for _ in range(args.warmup):
+        r = run()
+        assert r.code == 0, r.message
+    barrier(ws)
+    walls, device_ms, launches = [], [], 0
+    clk = ClockSampler(device)
+    with clk:
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            r = run()
+            walls.append(time.perf_counter() - t0)
+            assert r.code == 0, r.message
+            device_ms.append(r.stats["step_ms"])
+            launches += int(r.stats["kernel_launches"])
+    steps = r.num_steps
+    dev_s = max_over_ranks(statistics.median(device_ms) * 1e-3, ws)
+    wall_s = max_over_ranks(statistics.median(walls), ws)
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle as O
+    if not os.path.exists(os.path.join(O.BUILD, "liboracle.so")):
+        O.build(with_reference=False)
+    orc = O.load("oracle")
+    kind = "reference" if O.reference_available() else "port"
+    cpu = O.load("ref_serial") if kind == "reference" else orc
+    ref = orc.run_1d(p)
+    max_rel = float(np.max(np.abs(r.U - ref.U)) / np.max(np.abs(ref.U)))
+    cpu_s = []
+    budget = time.perf_counter() + 10.0
+    while len(cpu_s) < 3 or (time.perf_counter() < budget and len(cpu_s) < 50):
+        cpu_s.append(cpu.run_1d(p).seconds)
+    cpu_run = statistics.median(cpu_s)
+    cells_steps = p.nx * steps
+    line = {
+        "metric": "1D Godunov + exact Riemann solver: time per Sod run (cell-updates/s)",
+        "value": ws * cells_steps / dev_s, "unit": "cell-updates/s", "n_gpus": ws,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": dev_s * 1e3,
+        "ms_per_run_device": dev_s * 1e3, "ms_per_run_e2e": wall_s * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (Sod tube, the reference example's initial states)",
+        "config": {"workload": "sod_1000_godunov_first_order_exact_fp64", "cells": p.nx,
+                   "ghost_cells": p.g, "cfl": p.cfl, "tf": p.tf, "time_steps_per_run": steps,
+                   "step": "one whole run to t = 0.2"},
+        "e2e": {"value": ws * cells_steps / wall_s, "unit": "cell-updates/s",
+                "h2d_bytes_per_step": int(r.stats["h2d_bytes"]),
+                "d2h_bytes_per_step": int(r.stats["d2h_bytes"]),
+                "note": "one hydro_gpu_launch_simulation call per run, host arrays in and out"},
+        "cpu_baseline": {"value": cells_steps / cpu_run, "unit": "cell-updates/s", "cores": 1,
+                         "kind": kind, "ms_per_run": cpu_run * 1e3,
+                         "sample": f"{len(cpu_s)} whole runs, serial"},
+        "max_rel_diff_U_vs_oracle": max_rel,
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(line))
+
+
 def main() -> None:
     global N_SIDE, WORKLOAD
     ap = argparse.ArgumentParser()
@@ -458,10 +535,11 @@ def main() -> None:
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"],
                     help="state precision of the timed path (fp64 is the drop-in)")
     ap.add_argument("--workload", default="shear_layer",
-                    choices=["shear_layer", "point_blast", "ensemble", "adjoint", "snapshots"],
+                    choices=["shear_layer", "point_blast", "ensemble", "adjoint", "snapshots", "sod"],
                     help="shear_layer: MC, periodic, CFL 0.8; point_blast: Van Leer, reflective, "
                          "CFL 0.4; ensemble: 256 four-quadrant problems, side log-uniform in "
-                         "[128, 1024], minmod, transmissive, one launch per step for all")
+                         "[128, 1024], minmod, transmissive, one launch per step for all; "
+                         "sod: the 1000-cell Sod tube, Godunov + exact solver, one step = one run")
     ap.add_argument("--instances", type=int, default=256, help="ensemble size")
     ap.add_argument("--checkpoint-every", type=int, default=50, help="adjoint checkpoint interval")
     ap.add_argument("--fd-directions", type=int, default=2,
@@ -498,6 +576,9 @@ def main() -> None:
         return
     if args.workload == "snapshots":
         run_snapshots(args, H, local, ws, rank)
+        return
+    if args.workload == "sod":
+        run_sod(args, H, local, ws, rank)
         return
 
     device = local

@@ -214,12 +214,12 @@ template <class R>
 HD void sample_right_vacuum(const GasConst<R> &c, R rho, R u, R v, R p, R a, R S, R o[4])
 {
     if (S <= (u - a)) { o[0] = rho; o[1] = u; o[2] = v; o[3] = p; return; }
-    const R front = u + R(2) * a / c.gm1;
+    const R front = u + dv(R(2) * a, c.gm1);
     if (S < front) {
-        R tmp = c.two_gp1 + (u - S) * c.gm1 / (c.gp1 * a);
+        R tmp = c.two_gp1 + dv((u - S) * c.gm1, c.gp1 * a);
         tmp = pw(tmp, c.two_gm1);
         o[0] = rho * tmp;
-        o[1] = (a + c.half_gm1 * u + S) * R(2) / c.gp1;
+        o[1] = dv((a + c.half_gm1 * u + S) * R(2), c.gp1);
         o[2] = v;
         o[3] = p * pw(tmp, c.gamma);
     } else {
@@ -231,12 +231,12 @@ template <class R>
 HD void sample_left_vacuum(const GasConst<R> &c, R rho, R u, R v, R p, R a, R S, R o[4])
 {
     if (S >= (u + a)) { o[0] = rho; o[1] = u; o[2] = v; o[3] = p; return; }
-    const R front = u - R(2) * a / c.gm1;
+    const R front = u - dv(R(2) * a, c.gm1);
     if (S > front) {
-        R tmp = c.two_gp1 - (u - S) * c.gm1 / (c.gp1 * a);
+        R tmp = c.two_gp1 - dv((u - S) * c.gm1, c.gp1 * a);
         tmp = pw(tmp, c.two_gm1);
         o[0] = rho * tmp;
-        o[1] = (-a + c.half_gm1 * u + S) * R(2) / c.gp1;
+        o[1] = dv((-a + c.half_gm1 * u + S) * R(2), c.gp1);
         o[2] = v;
         o[3] = p * pw(tmp, c.gamma);
     } else {
@@ -255,8 +255,8 @@ HD void solve_vacuum(const GasConst<R> &c,
     if (rho_L <= R(0) && rho_R <= R(0)) { o[0] = o[1] = o[2] = o[3] = R(0); return; }
     if (rho_L <= R(0)) { sample_right_vacuum(c, rho_L, u_L, v_L, p_L, a_L, S, o); return; }
     if (rho_R <= R(0)) { sample_left_vacuum(c, rho_R, u_R, v_R, p_R, a_R, S, o); return; }
-    const R SL = R(2) * a_L / c.gm1;
-    const R SR = R(2) * a_R / c.gm1;
+    const R SL = dv(R(2) * a_L, c.gm1);
+    const R SR = dv(R(2) * a_R, c.gm1);
     if (S <= SL) { sample_right_vacuum(c, rho_L, u_L, v_L, p_L, a_L, S, o); return; }
     if (SR <= S) { sample_left_vacuum(c, rho_R, u_R, v_R, p_R, a_R, S, o); return; }
     o[0] = o[1] = o[2] = o[3] = R(0);
@@ -359,7 +359,7 @@ HD void hllc_vacuum_flux(const GasConst<R> &c, R rho_L, R u_L, R v_L, R p_L, R a
 {
     R s[4];
     solve_vacuum(c, rho_L, u_L, v_L, p_L, a_L, rho_R, u_R, v_R, p_R, a_R, R(0), s);
-    const R E = s[0] * (R(0.5) * (s[1] * s[1] + s[2] * s[2]) + s[3] / (s[0] * c.gm1));
+    const R E = s[0] * (R(0.5) * (s[1] * s[1] + s[2] * s[2]) + dv(s[3], s[0] * c.gm1));
     F[0] = s[0] * s[1];
     F[1] = s[0] * s[1] * s[1] + s[3];
     F[2] = s[0] * s[1] * s[2];
@@ -440,7 +440,7 @@ HD int hllc_flux_1d(const GasConst<R> &c, R rho_L, R u_L, R p_L, R rho_R, R u_R,
     if (rho_L <= R(0) || rho_R <= R(0) || dv((a_L + a_R) * R(2), c.gp1) <= (u_R - u_L)) {
         R s[4];
         solve_vacuum(c, rho_L, u_L, R(0), p_L, a_L, rho_R, u_R, R(0), p_R, a_R, R(0), s);
-        const R E = s[0] * (R(0.5) * s[1] * s[1] + s[3] / (s[0] * c.gm1));
+        const R E = s[0] * (R(0.5) * s[1] * s[1] + dv(s[3], s[0] * c.gm1));
         F[0] = s[0] * s[1];
         F[1] = s[0] * s[1] * s[1] + s[3];
         F[2] = s[1] * (E + s[3]);
@@ -494,11 +494,11 @@ template <class R>
 HD R exact_fK(const GasConst<R> &c, R rho, R p, R a, R ps)
 {
     if (ps > p) {
-        const R A = R(2) / (c.gp1 * rho);
+        const R A = dv(R(2), c.gp1 * rho);
         const R B = p * c.gm1_gp1;
-        return (ps - p) * sqrt(A / (ps + B));
+        return (ps - p) * sq(dv(A, ps + B));
     }
-    return R(2) * a * (pw((ps / p), c.gm1_2g) - R(1)) / c.gm1;
+    return dv(R(2) * a * (pw(dv(ps, p), c.gm1_2g) - R(1)), c.gm1);
 }
 
 /* Derivative; the shock branch's (B - p*) follows the reference
@@ -507,11 +507,11 @@ template <class R>
 HD R exact_dfK(const GasConst<R> &c, R rho, R p, R a, R ps)
 {
     if (ps > p) {
-        const R A = R(2) / (c.gp1 * rho);
+        const R A = dv(R(2), c.gp1 * rho);
         const R B = p * c.gm1_gp1;
-        return (R(1) - R(0.5) * (ps - p) / (B - ps)) * sqrt(A / (B + ps));
+        return (R(1) - dv(R(0.5) * (ps - p), B - ps)) * sq(dv(A, B + ps));
     }
-    return pw(ps / p, c.neg_gp1_2g) / (p * a);
+    return dv(pw(dv(ps, p), c.neg_gp1_2g), p * a);
 }
 
 template <class R>
@@ -540,9 +540,9 @@ HD int exact_p_star(const GasConst<R> &c, R rho_L, R u_L, R p_L, R a_L,
             f_lo = f;
             p_lo = p0;
         }
-        const R p1 = p0 - f / fp;
+        const R p1 = p0 - dv(f, fp);
         if (p1 < R(0)) break;
-        if (R(2) * fabs(p1 - p0) / (p1 + p0) < c.tol) {
+        if (dv(R(2) * fabs(p1 - p0), p1 + p0) < c.tol) {
             *out = p1;
             return DEV_OK;
         }
@@ -553,7 +553,7 @@ HD int exact_p_star(const GasConst<R> &c, R rho_L, R u_L, R p_L, R a_L,
         f_lo = exact_f(c, rho_L, u_L, p_L, a_L, rho_R, u_R, p_R, a_R, p_lo);
         if (f_lo * f_hi >= R(0)) {
             p_hi *= R(10);
-            const R dp = (p_hi - p_lo) / R(100);
+            const R dp = dv(p_hi - p_lo, R(100));
             for (int i = 0; i < 100; i++) {
                 const R a = p_lo + R(i) * dp;
                 const R b = p_lo + R(i + 1) * dp;
@@ -586,51 +586,51 @@ HD void exact_sample(const GasConst<R> &c, R rho_L, R u_L, R p_L, R a_L,
 {
     if (S < us) {
         if (ps > p_L) {
-            const R r = ps / p_L;
-            const R SL = u_L - a_L * sqrt(c.gp1_2g * r + c.gm1_2g);
+            const R r = dv(ps, p_L);
+            const R SL = u_L - a_L * sq(c.gp1_2g * r + c.gm1_2g);
             if (S < SL) { o[0] = rho_L; o[1] = u_L; o[2] = p_L; return; }
             const R k = c.gm1_gp1;
-            o[0] = rho_L * (r + k) / (k * r + R(1));
+            o[0] = dv(rho_L * (r + k), k * r + R(1));
             o[1] = us;
             o[2] = ps;
             return;
         }
         const R SH = u_L - a_L;
         if (S < SH) { o[0] = rho_L; o[1] = u_L; o[2] = p_L; return; }
-        const R as = a_L * pw(ps / p_L, c.gm1_2g);
+        const R as = a_L * pw(dv(ps, p_L), c.gm1_2g);
         if (S < us - as) {
-            const R cm = pw((c.two_gp1 + (u_L - S) * (c.gm1 / (a_L * c.gp1))), c.two_gm1);
+            const R cm = pw((c.two_gp1 + (u_L - S) * dv(c.gm1, a_L * c.gp1)), c.two_gm1);
             o[0] = rho_L * cm;
             o[1] = c.two_gp1 * (a_L + R(0.5) * u_L * c.gm1 + S);
             o[2] = p_L * pw(cm, c.gamma);
             return;
         }
-        o[0] = rho_L * pw(ps / p_L, c.inv_g);
+        o[0] = rho_L * pw(dv(ps, p_L), c.inv_g);
         o[1] = us;
         o[2] = ps;
         return;
     }
     if (ps > p_R) {
-        const R r = ps / p_R;
-        const R SR = u_R + a_R * sqrt(r * c.gp1 / (R(2) * c.gamma) + c.gm1_2g);
+        const R r = dv(ps, p_R);
+        const R SR = u_R + a_R * sq(dv(r * c.gp1, R(2) * c.gamma) + c.gm1_2g);
         if (S > SR) { o[0] = rho_R; o[1] = u_R; o[2] = p_R; return; }
         const R k = c.gm1_gp1;
-        o[0] = rho_R * (r + k) / (k * r + R(1));
+        o[0] = dv(rho_R * (r + k), k * r + R(1));
         o[1] = us;
         o[2] = ps;
         return;
     }
     const R SH = u_R + a_R;
     if (S > SH) { o[0] = rho_R; o[1] = u_R; o[2] = p_R; return; }
-    const R as = a_R * pw(ps / p_R, c.gm1_2g);
+    const R as = a_R * pw(dv(ps, p_R), c.gm1_2g);
     if (S > us + as) {
-        const R cm = pw((c.two_gp1 - (u_R - S) * c.gm1 / (a_R * c.gp1)), c.two_gm1);
+        const R cm = pw((c.two_gp1 - dv((u_R - S) * c.gm1, a_R * c.gp1)), c.two_gm1);
         o[0] = rho_R * cm;
         o[1] = c.two_gp1 * (-a_R + R(0.5) * u_R * c.gm1 + S);
         o[2] = p_R * pw(cm, c.gamma);
         return;
     }
-    o[0] = rho_R * pw(ps / p_R, c.inv_g);
+    o[0] = rho_R * pw(dv(ps, p_R), c.inv_g);
     o[1] = us;
     o[2] = ps;
 }

@@ -1,6 +1,6 @@
 /*
  * run1d.cu -- 1D integrators (Cartesian, cylindrical, spherical) in one
- * persistent CTA.
+ * persistent thread-block cluster.
  *
  * Replaces the time loops of godunov_first_order_1d
  * (src/integrator_godunov_first_order.c:26-261), muscl_hancock_1d
@@ -17,12 +17,18 @@
  * (src/integrator_godunov_first_order.c:182-192).
  *
  * 1D problems are small (the Sod tube of the benchmark configurations has
- * 1000 cells), so the whole run is one launch of one CTA of 1024 threads:
- * per step a block-wide max gives dt, every face flux is computed into a
- * global scratch array, and after a barrier each cell gathers its two faces
- * in the reference's order (+F_left, then -F_right, each (F*dt)*A), then
- * the all-cell U->W conversion and the ghost fill run.  The arrays are
- * L2-resident at these sizes.  The exact solver's Newton (<= 100) and
+ * 1000 cells), so the whole run is one launch of one thread-block cluster:
+ * 16 CTAs of 256 threads (8 where the device cannot place 16), one per SM,
+ * with hardware cluster barriers between the phases of a step.  A single
+ * CTA would put every face's exact Riemann solve (Newton iterations, pow)
+ * on one SM's FP64 pipe, about as fast as one host core; the cluster spreads
+ * the faces over 16 SMs, and four lanes share each exact Riemann solve
+ * (quad_exact_solve below).  Per step a cluster-wide max (partials exchanged
+ * through distributed shared memory) gives dt, every face flux is computed
+ * into a global scratch array, and after a barrier each cell gathers its two
+ * faces in the reference's order (+F_left, then -F_right, each (F*dt)*A)
+ * and converts U->W, then the ghost fill runs.  The arrays are L2-resident
+ * at these sizes.  The exact solver's Newton (<= 100) and
  * bisection (<= 5000) loops are bounded.  The kernel leaves the loop when
  * the run stops or a snapshot is due (the host stores it and relaunches).
  *
@@ -35,6 +41,7 @@
  *
  * Compiled with --fmad=false (same IEEE operation sequence as the reference).
  */
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 #include <math_constants.h>
 
@@ -49,10 +56,16 @@
 #include "step_control.h"
 
 using namespace hydro;
+namespace cg = cooperative_groups;
 
 namespace {
 
-constexpr int kThreads = 1024;
+/* threads per CTA (a multiple of 4: the exact solver's quads); a run is
+ * one cluster of up to 16 CTAs, one per SM */
+constexpr int kThreads = 256;
+/* four lanes per exact Riemann solve (quad_exact_solve) instead of one */
+constexpr bool kQuadExact = true;
+constexpr int kClusterMax = 16;
 
 struct Run1dArgs {
     double *W[3];          /* rho, u, p (padded, nx + 2G) */
@@ -96,20 +109,253 @@ __device__ double van_der_corput(long long n)
 __device__ __forceinline__ void geometry_rates(double pf, double gm1, double rho, double sm, double se,
                                                double &dm, double &dmom, double &de)
 {
-    const double p = gm1 * (se - 0.5 * sm * sm / rho);
+    const double p = gm1 * (se - dv(0.5 * sm * sm, rho));
     dm = pf * sm;
-    dmom = pf * sm * sm / rho;
-    de = pf * sm * (se + p) / rho;
+    dmom = dv(pf * sm * sm, rho);
+    de = dv(pf * sm * (se + p), rho);
 }
 
-__device__ int face_flux(const Run1dArgs &a, double rl, double ul, double pl, double rr,
-                         double ur, double pr, double F[3])
+/*
+ * The exact solver with four lanes per Riemann problem.
+ *
+ * A Newton step of the star pressure needs fK and dfK of both sides
+ * (src/riemann_solver_exact.c:515-560), each a pow (rarefaction side) or a
+ * divide and square root (shock side).  One thread per problem evaluates the
+ * four in sequence, and a warp of 32 different problems runs every branch
+ * any of them takes.  Here lane q of a quad evaluates one of them (q = 0, 1:
+ * fK of the left / right side; q = 2, 3: dfK) and the quad exchanges them by
+ * shuffles, so a Newton step costs about one pow.  Every lane then forms
+ *   f = (fK_L + fK_R) + (u_R - u_L),   f' = dfK_L + dfK_R
+ * in the reference's order and runs the same control flow, so the quad's
+ * lanes stay together and the result is that of exact_p_star / exact_solve_1d
+ * (numerics.cuh) bit for bit.
+ */
+struct Quad {
+    unsigned mask;   /* the quad's four lanes */
+    int base;        /* its first lane */
+    int q;           /* this lane's role, 0..3 */
+};
+
+__device__ __forceinline__ Quad make_quad()
 {
-    if (a.solver == 1) return exact_flux_1d(a.gas, rl, ul, pl, rr, ur, pr, 0.0, F);
-    return hllc_flux_1d(a.gas, rl, ul, pl, rr, ur, pr, F);
+    const int lane = threadIdx.x & 31;
+    Quad Q;
+    Q.base = lane & ~3;
+    Q.mask = 0xfu << Q.base;
+    Q.q = lane & 3;
+    return Q;
 }
 
-__device__ double block_max(double v, double *red)
+struct Sides {
+    double rho_L, p_L, a_L, rho_R, p_R, a_R, du;
+};
+
+/* fK (q < 2) or dfK (q >= 2) of side q & 1 at p*, the same expressions as
+ * exact_fK / exact_dfK; all four values come back in v[].  With `sample`
+ * set, lanes 2, 3 compute pow(p* / p_K, 1 / gamma) of side K instead (the
+ * star density factor of exact_sample's rarefaction branch, used only when
+ * p* <= p_K), and pre[] receives, per side, pow(p* / p_K, (gamma - 1) / 2
+ * gamma) from the fK lanes (the same value exact_sample's `as` needs) and
+ * that density factor. */
+__device__ void quad_fdf(const Quad &Q, const GasConst<double> &c, const Sides &S, double ps, double v[4],
+                         bool sample = false, double pre[4] = nullptr)
+{
+    const int side = Q.q & 1;
+    const bool d = Q.q >= 2;
+    const double rho = side ? S.rho_R : S.rho_L;
+    const double p = side ? S.p_R : S.p_L;
+    const double a = side ? S.a_R : S.a_L;
+    double x, r = 0.0;
+    if (ps > p) {
+        const double A = dv(2.0, c.gp1 * rho);
+        const double B = p * c.gm1_gp1;
+        if (d) x = sample ? 0.0 : (1.0 - dv(0.5 * (ps - p), B - ps)) * sq(dv(A, B + ps));
+        else x = (ps - p) * sq(dv(A, ps + B));
+    } else {
+        r = pw(dv(ps, p), d ? (sample ? c.inv_g : c.neg_gp1_2g) : c.gm1_2g);
+        x = d ? (sample ? r : dv(r, p * a)) : dv(2.0 * a * (r - 1.0), c.gm1);
+    }
+#pragma unroll
+    for (int k = 0; k < 4; k++) v[k] = __shfl_sync(Q.mask, x, Q.base + k);
+    if (sample) {
+        pre[0] = __shfl_sync(Q.mask, r, Q.base + 0);
+        pre[1] = __shfl_sync(Q.mask, r, Q.base + 1);
+        pre[2] = v[2];
+        pre[3] = v[3];
+    }
+}
+
+__device__ __forceinline__ double quad_f(const Quad &Q, const GasConst<double> &c, const Sides &S, double ps)
+{
+    double v[4];
+    quad_fdf(Q, c, S, ps, v);
+    return v[0] + v[1] + S.du;
+}
+
+/* exact_p_star (numerics.cuh) with the function evaluations shared by the quad. */
+__device__ int quad_p_star(const Quad &Q, const GasConst<double> &c, double rho_L, double u_L, double p_L,
+                           double a_L, double rho_R, double u_R, double p_R, double a_R, double *out)
+{
+    const Sides S{ rho_L, p_L, a_L, rho_R, p_R, a_R, u_R - u_L };
+    const double pg = guess_p(c, rho_L, u_L, p_L, a_L, rho_R, u_R, p_R, a_R);
+    bool bracket = false;
+    double p_hi = pg;
+    /* f(p_hi) and, for the first Newton step at p0 = p_hi, f'(p_hi) */
+    double v[4];
+    quad_fdf(Q, c, S, p_hi, v);
+    double f_hi = v[0] + v[1] + S.du;
+    double p_lo = 0.0, f_lo = 0.0;
+    double p0 = pg;
+    for (int it = 0; it < 100; it++) {
+        if (it > 0) quad_fdf(Q, c, S, p0, v);
+        const double f = v[0] + v[1] + S.du;
+        const double fp = v[2] + v[3];
+        if (!bracket && f * f_hi < 0.0) {
+            bracket = true;
+            f_lo = f;
+            p_lo = p0;
+        }
+        const double p1 = p0 - dv(f, fp);
+        if (p1 < 0.0) break;
+        if (dv(2.0 * fabs(p1 - p0), p1 + p0) < c.tol) {
+            *out = p1;
+            return DEV_OK;
+        }
+        p0 = p1;
+    }
+    if (!bracket) {
+        p_lo = 0.0;
+        f_lo = quad_f(Q, c, S, p_lo);
+        if (f_lo * f_hi >= 0.0) {
+            p_hi *= 10.0;
+            const double dp = dv(p_hi - p_lo, 100.0);
+            for (int i = 0; i < 100; i++) {
+                const double a = p_lo + (double) i * dp;
+                const double b = p_lo + (double) (i + 1) * dp;
+                const double fa = quad_f(Q, c, S, a);
+                const double fb = quad_f(Q, c, S, b);
+                if (fa * fb < 0.0) {
+                    p_lo = a; f_lo = fa; p_hi = b; f_hi = fb;
+                    break;
+                }
+            }
+            if (f_lo * f_hi >= 0.0) return DEV_ERR_EXACT_BRACKET;
+        }
+    }
+    for (int count = 1; count <= 5001; count++) {
+        const double pm = 0.5 * (p_lo + p_hi);
+        if (p_hi - p_lo < c.tol) {
+            *out = pm;
+            return DEV_OK;
+        }
+        const double fm = quad_f(Q, c, S, pm);
+        if (fm * f_lo < 0.0) { p_hi = pm; f_hi = fm; }
+        else { p_lo = pm; f_lo = fm; }
+    }
+    return DEV_ERR_EXACT_BISECTION;
+}
+
+/* exact_sample (numerics.cuh) with pow(p* / p_K, (gamma - 1) / 2 gamma) and
+ * pow(p* / p_K, 1 / gamma) of each side taken from pre[] (computed in
+ * parallel by the quad, the same expressions): the same branches and
+ * operations. */
+__device__ void quad_sample(const GasConst<double> &c, double rho_L, double u_L, double p_L, double a_L,
+                            double rho_R, double u_R, double p_R, double a_R, double us, double ps,
+                            double S, const double pre[4], double o[3])
+{
+    if (S < us) {
+        if (ps > p_L) {
+            const double r = dv(ps, p_L);
+            const double SL = u_L - a_L * sq(c.gp1_2g * r + c.gm1_2g);
+            if (S < SL) { o[0] = rho_L; o[1] = u_L; o[2] = p_L; return; }
+            const double k = c.gm1_gp1;
+            o[0] = dv(rho_L * (r + k), k * r + 1.0);
+            o[1] = us;
+            o[2] = ps;
+            return;
+        }
+        const double SH = u_L - a_L;
+        if (S < SH) { o[0] = rho_L; o[1] = u_L; o[2] = p_L; return; }
+        const double as = a_L * pre[0];
+        if (S < us - as) {
+            const double cm = pw((c.two_gp1 + (u_L - S) * dv(c.gm1, a_L * c.gp1)), c.two_gm1);
+            o[0] = rho_L * cm;
+            o[1] = c.two_gp1 * (a_L + 0.5 * u_L * c.gm1 + S);
+            o[2] = p_L * pw(cm, c.gamma);
+            return;
+        }
+        o[0] = rho_L * pre[2];
+        o[1] = us;
+        o[2] = ps;
+        return;
+    }
+    if (ps > p_R) {
+        const double r = dv(ps, p_R);
+        const double SR = u_R + a_R * sq(dv(r * c.gp1, 2.0 * c.gamma) + c.gm1_2g);
+        if (S > SR) { o[0] = rho_R; o[1] = u_R; o[2] = p_R; return; }
+        const double k = c.gm1_gp1;
+        o[0] = dv(rho_R * (r + k), k * r + 1.0);
+        o[1] = us;
+        o[2] = ps;
+        return;
+    }
+    const double SH = u_R + a_R;
+    if (S > SH) { o[0] = rho_R; o[1] = u_R; o[2] = p_R; return; }
+    const double as = a_R * pre[1];
+    if (S > us + as) {
+        const double cm = pw((c.two_gp1 - dv((u_R - S) * c.gm1, a_R * c.gp1)), c.two_gm1);
+        o[0] = rho_R * cm;
+        o[1] = c.two_gp1 * (-a_R + 0.5 * u_R * c.gm1 + S);
+        o[2] = p_R * pw(cm, c.gamma);
+        return;
+    }
+    o[0] = rho_R * pre[3];
+    o[1] = us;
+    o[2] = ps;
+}
+
+/* exact_solve_1d (numerics.cuh) on a quad: the state sampled at x/t = S. */
+__device__ int quad_exact_solve(const Quad &Q, const GasConst<double> &c, double rho_L, double u_L, double p_L,
+                                double rho_R, double u_R, double p_R, double S, double o[3])
+{
+    const double a_L = (rho_L > 0.0) ? sound_speed(c, rho_L, p_L) : 0.0;
+    const double a_R = (rho_R > 0.0) ? sound_speed(c, rho_R, p_R) : 0.0;
+    if (rho_L <= 0.0 || rho_R <= 0.0 || dv((a_L + a_R) * 2.0, c.gp1) <= (u_R - u_L)) {
+        double s[4];
+        solve_vacuum(c, rho_L, u_L, 0.0, p_L, a_L, rho_R, u_R, 0.0, p_R, a_R, S, s);
+        o[0] = s[0]; o[1] = s[1]; o[2] = s[3];
+        return DEV_OK;
+    }
+    double ps = 0.0;
+    const int rc = quad_p_star(Q, c, rho_L, u_L, p_L, a_L, rho_R, u_R, p_R, a_R, &ps);
+    if (rc != DEV_OK) { o[0] = o[1] = o[2] = 0.0; return rc; }
+    const Sides Sd{ rho_L, p_L, a_L, rho_R, p_R, a_R, u_R - u_L };
+    double v[4], pre[4];
+    quad_fdf(Q, c, Sd, ps, v, true, pre);
+    const double us = 0.5 * (u_L + u_R) + 0.5 * (v[1] - v[0]);
+    quad_sample(c, rho_L, u_L, p_L, a_L, rho_R, u_R, p_R, a_R, us, ps, S, pre, o);
+    return DEV_OK;
+}
+
+/* exact_flux_1d (numerics.cuh) on a quad, at x/t = 0. */
+__device__ int quad_exact_flux(const Quad &Q, const GasConst<double> &c, double rl, double ul, double pl,
+                               double rr, double ur, double pr, double F[3])
+{
+    double s[3];
+    const int rc = quad_exact_solve(Q, c, rl, ul, pl, rr, ur, pr, 0.0, s);
+    F[0] = s[0] * s[1];
+    F[1] = s[0] * s[1] * s[1] + s[2];
+    F[2] = (s[2] * c.g_gm1 + 0.5 * s[0] * s[1] * s[1]) * s[1];
+    return rc;
+}
+
+/* The cluster's threads: a global index and count for the cell and face loops. */
+struct Lanes {
+    int gt, GT;
+};
+
+/* The CTA's maximum of v, written to *part (this CTA's shared memory). */
+__device__ void block_partial_max(double v, double *red, double *part)
 {
     for (int o = 16; o > 0; o >>= 1) {
         const double w = __shfl_xor_sync(0xffffffffu, v, o);
@@ -123,6 +369,23 @@ __device__ double block_max(double v, double *red)
             const double w = __shfl_xor_sync(0xffffffffu, v, o);
             if (w > v) v = w;
         }
+        if (threadIdx.x == 0) *part = v;
+    }
+}
+
+/* The maximum of every CTA's *part: after a cluster barrier, warp 0 reads
+ * the partials through distributed shared memory.  Callers alternate two
+ * `part` slots between steps, so no CTA overwrites a slot another may still
+ * be reading; a cluster barrier separates the reads from any exit. */
+__device__ double cluster_gather_max(double *part, double *red, cg::cluster_group &cl)
+{
+    cl.sync();
+    if (threadIdx.x < 32) {
+        double v = (threadIdx.x < (int) cl.num_blocks()) ? *cl.map_shared_rank(part, threadIdx.x) : -CUDART_INF;
+        for (int o = 16; o > 0; o >>= 1) {
+            const double w = __shfl_xor_sync(0xffffffffu, v, o);
+            if (w > v) v = w;
+        }
         if (threadIdx.x == 0) red[0] = v;
     }
     __syncthreads();
@@ -131,24 +394,41 @@ __device__ double block_max(double v, double *red)
     return r;
 }
 
-/* All-cell U -> W (src/system.c:735-761). */
-__device__ void convert_all(const Run1dArgs &a, double *const *U, double *const *W, int ntot)
+/* The first nonzero error code of the cluster's CTAs (lowest rank first),
+ * from each CTA's `err` slot, after a cluster barrier. */
+__device__ int cluster_error(int *err, int *bcast, cg::cluster_group &cl)
 {
-    for (int i = threadIdx.x; i < ntot; i += kThreads) {
+    cl.sync();
+    if (threadIdx.x < 32) {
+        const int e = (threadIdx.x < (int) cl.num_blocks()) ? *cl.map_shared_rank(err, threadIdx.x) : 0;
+        const unsigned m = __ballot_sync(0xffffffffu, e != 0);
+        const int first = __shfl_sync(0xffffffffu, e, m ? __ffs(m) - 1 : 0);
+        if (threadIdx.x == 0) *bcast = first;
+    }
+    __syncthreads();
+    const int r = *bcast;
+    __syncthreads();
+    return r;
+}
+
+/* All-cell U -> W (src/system.c:735-761). */
+__device__ void convert_all(const Run1dArgs &a, double *const *U, double *const *W, int ntot, Lanes L)
+{
+    for (int i = L.gt; i < ntot; i += L.GT) {
         const double m = U[0][i];
         const double vol = a.vol[i];
-        const double rho = m / vol;
-        const double u = U[1][i] / m;
+        const double rho = dv(m, vol);
+        const double u = dv(U[1][i], m);
         W[0][i] = rho;
         W[1][i] = u;
-        W[2][i] = a.gas.gm1 * (U[2][i] - 0.5 * m * u * u) / vol;
+        W[2][i] = dv(a.gas.gm1 * (U[2][i] - 0.5 * m * u * u), vol);
     }
 }
 
 /* Ghost fill (src/boundary.c:411-511). */
-__device__ void ghost_fill(const Run1dArgs &a, double *const *W, int g, int n)
+__device__ void ghost_fill(const Run1dArgs &a, double *const *W, int g, int n, Lanes L)
 {
-    for (int k = threadIdx.x; k < g; k += kThreads) {
+    for (int k = L.gt; k < g; k += L.GT) {
         for (int side = 0; side < 2; side++) {
             const int f = a.bc[side];
             if (f == BC_NONE || (f == BC_PERIODIC && side == 0)) continue;
@@ -166,49 +446,79 @@ __device__ void ghost_fill(const Run1dArgs &a, double *const *W, int g, int n)
     }
 }
 
+/* Every phase boundary is a cluster barrier: it orders the phase's global
+ * writes (release) before the next phase's reads on any SM of the cluster
+ * (acquire).  Every exit is taken by all CTAs at the same point, after a
+ * cluster barrier that follows the last distributed-shared-memory read. */
 __global__ void __launch_bounds__(kThreads) run1d_kernel(const Run1dArgs a)
 {
     __shared__ double red[kThreads / 32];
+    __shared__ double part[2];
+    __shared__ int errs[2];
     __shared__ int s_err;
-    HydroStepControl *ctrl = a.ctrl;
+    cg::cluster_group cl = cg::this_cluster();
+    const Lanes L{ (int) cl.block_rank() * kThreads + (int) threadIdx.x, (int) cl.num_blocks() * kThreads };
+    const bool leader = cl.block_rank() == 0 && threadIdx.x == 0;
+    const Quad Q = make_quad();
+    volatile HydroStepControl *ctrl = a.ctrl;
     const int g = a.g, n = a.nx, ntot = n + 2 * g;
     const int tid = threadIdx.x;
     double *const *W = a.W;
     double *const *U = a.U;
 
+    /* The control state is constant during a launch or advanced identically
+     * by every CTA (dt is cluster-uniform), so it lives in registers; the
+     * leader writes t, dt, the step count and the stop flags back each step
+     * for the host. */
+    if (!ctrl->active) return;
+    const double tf = ctrl->tf;
+    const long long max_steps = ctrl->max_steps;
+    const int store_count = ctrl->store_count;
+    long long ns = ctrl->num_steps;
+    double t = ctrl->t;
+    /* Godunov or MUSCL-Hancock on a Cartesian grid: the final per-cell loop
+     * also writes the ghost cells (each from its source cell, by the thread
+     * that converts that cell) and the next step's partial maximum of
+     * a + |u|, so a step needs two cluster barriers */
+    const bool fused = a.scheme != 2 && a.alpha == 0.0;
+    const bool periodic = a.bc[1] == BC_PERIODIC;
+    const bool ghost_l = periodic || (a.bc[0] != BC_NONE && a.bc[0] != BC_PERIODIC);
+    const bool ghost_r = a.bc[1] != BC_NONE;
+    bool have_part = false;
+
     /* at most 65536 steps per launch; the host relaunches while active */
     for (int guard = 0; guard < 65536; guard++) {
-        if (!*(volatile int *) &ctrl->active) return;
-        const long long ns = ctrl->num_steps;
-        const double t = ctrl->t;
-        const double tf = ctrl->tf;
+        const int buf = guard & 1;
+        if (tid == 0) errs[buf] = 0;
 
         /* ---- dt (src/utils.c:28-53) ---- */
-        double smax = -CUDART_INF;
-        for (int i = g + tid; i < g + n; i += kThreads) {
-            const double s = sound_speed(a.gas, W[0][i], W[2][i]) + fabs(W[1][i]);
-            if (s > smax) smax = s;
+        if (!have_part) {
+            double smax = -CUDART_INF;
+            for (int i = g + L.gt; i < g + n; i += L.GT) {
+                const double s = sound_speed(a.gas, W[0][i], W[2][i]) + fabs(W[1][i]);
+                if (s > smax) smax = s;
+            }
+            block_partial_max(smax, red, &part[buf]);
         }
-        smax = block_max(smax, red);
+        const double smax = cluster_gather_max(&part[buf], red, cl);
         const double cfl = (ns < a.sp.shrink_steps) ? a.sp.cfl_shrunk : a.sp.cfl;
-        double dt = cfl * a.dx / smax;
+        double dt = dv(cfl * a.dx, smax);
         if (t + dt > tf) dt = tf - t;
         if (dt == 0.0) {
-            if (tid == 0) {
+            if (leader) {
                 ctrl->dt = dt;
                 ctrl->error_code = DEV_ERR_DT_ZERO;
                 ctrl->active = 0;
             }
+            cl.sync();
             return;
         }
-        if (tid == 0) s_err = 0;
-        __syncthreads();
 
         /* ---- interface states (MUSCL-Hancock, :159-246) ---- */
         if (a.scheme == 1) {
-            for (int i = tid; i < n + 2; i += kThreads) {
+            for (int i = L.gt; i < n + 2; i += L.GT) {
                 const int k = g + i - 1;
-                const double dtA = dt * a.area[k] / a.vol[k];
+                const double dtA = dv(dt * a.area[k], a.vol[k]);
                 const double rho = W[0][k], u = W[1][k], p = W[2][k];
                 const double as = sound_speed(a.gas, rho, p);
                 double d[3];
@@ -222,7 +532,7 @@ __global__ void __launch_bounds__(kThreads) run1d_kernel(const Run1dArgs a)
                 if (i < n + 1)
                     for (int q = 0; q < 3; q++) a.Lf[q][g + i] = hi[q];
             }
-            __syncthreads();
+            cl.sync();
         }
 
         if (a.scheme == 2) {
@@ -230,133 +540,193 @@ __global__ void __launch_bounds__(kThreads) run1d_kernel(const Run1dArgs a)
              * exact solution of the left or right Riemann problem of each cell,
              * sampled at theta dx / dt or (theta - 1) dx / dt, from a copy of W ---- */
             const double theta = van_der_corput(ns + 1);
-            for (int i = tid; i < ntot; i += kThreads)
+            for (int i = L.gt; i < ntot; i += L.GT)
                 for (int q = 0; q < 3; q++) a.Lf[q][i] = W[q][i];
-            __syncthreads();
+            cl.sync();
             double *const *T = a.Lf;
-            for (int i = g + tid; i <= g + n; i += kThreads) {
+            const int c0 = kQuadExact ? (L.gt >> 2) : L.gt, cs = kQuadExact ? (L.GT >> 2) : L.GT;
+            for (int i = g + c0; i <= g + n; i += cs) {
                 const bool left = theta <= 0.5;
                 const int l = left ? i - 1 : i, r = left ? i : i + 1;
-                const double speed = left ? theta * a.dx / dt : (theta - 1.0) * a.dx / dt;
+                const double speed = left ? dv(theta * a.dx, dt) : dv((theta - 1.0) * a.dx, dt);
                 double o[3];
-                const int rc = exact_solve_1d(a.gas, T[0][l], T[1][l], T[2][l], T[0][r], T[1][r], T[2][r],
-                                              speed, o);
-                if (rc != DEV_OK) atomicCAS(&s_err, 0, rc);
-                W[0][i] = o[0];
-                W[1][i] = o[1];
-                W[2][i] = o[2];
+                const int rc = kQuadExact
+                    ? quad_exact_solve(Q, a.gas, T[0][l], T[1][l], T[2][l], T[0][r], T[1][r], T[2][r], speed, o)
+                    : exact_solve_1d(a.gas, T[0][l], T[1][l], T[2][l], T[0][r], T[1][r], T[2][r], speed, o);
+                if (!kQuadExact || Q.q == 0) {
+                    if (rc != DEV_OK) atomicCAS(&errs[buf], 0, rc);
+                    W[0][i] = o[0];
+                    W[1][i] = o[1];
+                    W[2][i] = o[2];
+                }
             }
-            __syncthreads();
-            if (s_err) {
+            const int err = cluster_error(&errs[buf], &s_err, cl);
+            if (err) {
                 /* the state from before the failing step */
-                for (int i = tid; i < ntot; i += kThreads)
+                for (int i = L.gt; i < ntot; i += L.GT)
                     for (int q = 0; q < 3; q++) W[q][i] = T[q][i];
-                __syncthreads();
-                if (tid == 0) {
+                if (leader) {
                     ctrl->dt = dt;
-                    ctrl->error_code = s_err;
+                    ctrl->error_code = err;
                     ctrl->active = 0;
                 }
+                cl.sync();
                 return;
             }
-            ghost_fill(a, W, g, n);
-            __syncthreads();
+            ghost_fill(a, W, g, n, L);
+            cl.sync();
             /* all-cell W -> U (src/system.c:866-883) */
-            for (int i = tid; i < ntot; i += kThreads) {
+            for (int i = L.gt; i < ntot; i += L.GT) {
                 const double rho = W[0][i], u = W[1][i], p = W[2][i], vol = a.vol[i];
                 const double m = rho * vol;
                 U[0][i] = m;
                 U[1][i] = m * u;
-                U[2][i] = vol * (0.5 * rho * u * u + p / a.gas.gm1);
+                U[2][i] = vol * (0.5 * rho * u * u + dv(p, a.gas.gm1));
             }
-            __syncthreads();
+            cl.sync();
         } else {
-            /* ---- face fluxes: face i between cells i-1 and i, i in [g, g+n] ---- */
-            for (int i = g + tid; i <= g + n; i += kThreads) {
+            /* ---- face fluxes: face i between cells i-1 and i, i in [g, g+n];
+             * the exact solver takes a quad of lanes per face, HLLC one ---- */
+            const bool quad = kQuadExact && a.solver == 1;
+            const int f0 = quad ? (L.gt >> 2) : L.gt, fs = quad ? (L.GT >> 2) : L.GT;
+            for (int i = g + f0; i <= g + n; i += fs) {
                 double F[3] = { 0.0, 0.0, 0.0 };
-                int rc;
-                if (a.scheme == 1)
-                    rc = face_flux(a, a.Lf[0][i], a.Lf[1][i], a.Lf[2][i], a.Rf[0][i], a.Rf[1][i],
-                                   a.Rf[2][i], F);
-                else
-                    rc = face_flux(a, W[0][i - 1], W[1][i - 1], W[2][i - 1], W[0][i], W[1][i], W[2][i], F);
-                if (rc != DEV_OK && a.scheme == 0) atomicCAS(&s_err, 0, rc);
-                for (int q = 0; q < 3; q++) a.F[q][i] = F[q];
+                double *const *sl = a.scheme == 1 ? a.Lf : W;
+                double *const *sr = a.scheme == 1 ? a.Rf : W;
+                const int il = a.scheme == 1 ? i : i - 1;
+                const double rl = sl[0][il], ul = sl[1][il], pl = sl[2][il];
+                const double rr = sr[0][i], ur = sr[1][i], pr = sr[2][i];
+                const int rc = quad ? quad_exact_flux(Q, a.gas, rl, ul, pl, rr, ur, pr, F)
+                             : a.solver == 1 ? exact_flux_1d(a.gas, rl, ul, pl, rr, ur, pr, 0.0, F)
+                                             : hllc_flux_1d(a.gas, rl, ul, pl, rr, ur, pr, F);
+                if (!quad || Q.q == 0) {
+                    if (rc != DEV_OK && a.scheme == 0) atomicCAS(&errs[buf], 0, rc);
+                    for (int q = 0; q < 3; q++) a.F[q][i] = F[q];
+                }
             }
-            __syncthreads();
-            if (s_err) {
-                if (tid == 0) {
+            const int err = cluster_error(&errs[buf], &s_err, cl);
+            if (err) {
+                if (leader) {
                     ctrl->dt = dt;
-                    ctrl->error_code = s_err;
+                    ctrl->error_code = err;
                     ctrl->active = 0;
                 }
+                cl.sync();
                 return;
             }
 
-            /* ---- gather update in the serial order ---- */
-            for (int c = g - 1 + tid; c <= g + n; c += kThreads) {
-                const double A = a.area[c];
-                for (int q = 0; q < 3; q++) {
-                    double v = U[q][c];
-                    if (c >= g) v = v + (a.F[q][c] * dt) * A;          /* face c: c is its right cell */
-                    if (c + 1 <= g + n) v = v - (a.F[q][c + 1] * dt) * A; /* face c+1: c is its left cell */
-                    U[q][c] = v;
+            /* ---- gather update in the serial order, then U -> W of the same
+             * cell (the conversion reads only the cell's own U, which this
+             * thread just wrote; cells outside the update range keep U) ---- */
+            double snext = -CUDART_INF;
+            for (int c = L.gt; c < ntot; c += L.GT) {
+                if (c >= g - 1 && c <= g + n) {
+                    const double A = a.area[c];
+                    for (int q = 0; q < 3; q++) {
+                        double v = U[q][c];
+                        if (c >= g) v = v + (a.F[q][c] * dt) * A;          /* face c: c is its right cell */
+                        if (c + 1 <= g + n) v = v - (a.F[q][c + 1] * dt) * A; /* face c+1: c is its left cell */
+                        U[q][c] = v;
+                    }
+                }
+                /* a ghost cell that the boundary routine fills keeps only its U */
+                if (fused && ((c < g && ghost_l) || (c >= g + n && ghost_r))) continue;
+                const double m = U[0][c];
+                const double vol = a.vol[c];
+                const double rho = dv(m, vol);
+                const double u = dv(U[1][c], m);
+                const double p = dv(a.gas.gm1 * (U[2][c] - 0.5 * m * u * u), vol);
+                W[0][c] = rho;
+                W[1][c] = u;
+                W[2][c] = p;
+                if (fused && c >= g && c < g + n) {
+                    /* the ghost cells filled from this cell (src/boundary.c:411-511:
+                     * the left side mirrors cell g + k into g - 1 - k, the right
+                     * side cell g + n - 1 - k into g + n + k; a periodic right
+                     * side copies both ways instead) */
+                    const int kl = c - g, kr = g + n - 1 - c;
+                    if (kl < g) {
+                        if (periodic) {
+                            W[0][g + n + kl] = rho; W[1][g + n + kl] = u; W[2][g + n + kl] = p;
+                        } else if (ghost_l) {
+                            W[0][g - 1 - kl] = rho;
+                            W[1][g - 1 - kl] = (a.bc[0] == BC_REFLECTIVE) ? -u : u;
+                            W[2][g - 1 - kl] = p;
+                        }
+                    }
+                    if (kr < g) {
+                        if (periodic) {
+                            W[0][g - 1 - kr] = rho; W[1][g - 1 - kr] = u; W[2][g - 1 - kr] = p;
+                        } else if (ghost_r) {
+                            W[0][g + n + kr] = rho;
+                            W[1][g + n + kr] = (a.bc[1] == BC_REFLECTIVE) ? -u : u;
+                            W[2][g + n + kr] = p;
+                        }
+                    }
+                    const double s = sound_speed(a.gas, rho, p) + fabs(u);
+                    if (s > snext) snext = s;
                 }
             }
-            __syncthreads();
-            convert_all(a, U, W, ntot);
-            __syncthreads();
-            ghost_fill(a, W, g, n);
-            __syncthreads();
+            if (fused) {
+                block_partial_max(snext, red, &part[buf ^ 1]);
+            } else {
+                cl.sync();
+                ghost_fill(a, W, g, n, L);
+                cl.sync();
+            }
         }
 
         /* ---- cylindrical / spherical source, RK4 (src/source_term.c:45-183) ---- */
         if (a.alpha != 0.0) {
             const double gm1 = a.gas.gm1;
-            for (int i = g + tid; i < g + n; i += kThreads) {
+            for (int i = g + L.gt; i < g + n; i += L.GT) {
                 const double vol = a.vol[i];
                 const double m = U[0][i], mom = U[1][i], E = U[2][i], rho = W[0][i];
-                const double pf = -a.alpha * vol / a.mid[i];
+                const double pf = dv(-a.alpha * vol, a.mid[i]);
                 double k1m, k1p, k1e, k2m, k2p, k2e, k3m, k3p, k3e, k4m, k4p, k4e;
-                geometry_rates(pf, gm1, rho, mom / vol, E / vol, k1m, k1p, k1e);
+                geometry_rates(pf, gm1, rho, dv(mom, vol), dv(E, vol), k1m, k1p, k1e);
                 double tm = m + 0.5 * dt * k1m, tp = mom + 0.5 * dt * k1p, te = E + 0.5 * dt * k1e;
-                geometry_rates(pf, gm1, tm / vol, tp / vol, te / vol, k2m, k2p, k2e);
+                geometry_rates(pf, gm1, dv(tm, vol), dv(tp, vol), dv(te, vol), k2m, k2p, k2e);
                 tm = m + 0.5 * dt * k2m;
                 tp = mom + 0.5 * dt * k2p;
                 te = E + 0.5 * dt * k2e;
-                geometry_rates(pf, gm1, tm / vol, tp / vol, te / vol, k3m, k3p, k3e);
+                geometry_rates(pf, gm1, dv(tm, vol), dv(tp, vol), dv(te, vol), k3m, k3p, k3e);
                 tm = m + dt * k3m;
                 tp = mom + dt * k3p;
                 te = E + dt * k3e;
-                geometry_rates(pf, gm1, tm / vol, tp / vol, te / vol, k4m, k4p, k4e);
-                U[0][i] = m + dt * (k1m + 2.0 * k2m + 2.0 * k3m + k4m) / 6.0;
-                U[1][i] = mom + dt * (k1p + 2.0 * k2p + 2.0 * k3p + k4p) / 6.0;
-                U[2][i] = E + dt * (k1e + 2.0 * k2e + 2.0 * k3e + k4e) / 6.0;
+                geometry_rates(pf, gm1, dv(tm, vol), dv(tp, vol), dv(te, vol), k4m, k4p, k4e);
+                U[0][i] = m + dv(dt * (k1m + 2.0 * k2m + 2.0 * k3m + k4m), 6.0);
+                U[1][i] = mom + dv(dt * (k1p + 2.0 * k2p + 2.0 * k3p + k4p), 6.0);
+                U[2][i] = E + dv(dt * (k1e + 2.0 * k2e + 2.0 * k3e + k4e), 6.0);
             }
-            __syncthreads();
-            convert_all(a, U, W, ntot);
-            __syncthreads();
-            ghost_fill(a, W, g, n);
-            __syncthreads();
+            cl.sync();
+            convert_all(a, U, W, ntot, L);
+            cl.sync();
+            ghost_fill(a, W, g, n, L);
+            cl.sync();
         }
 
-        /* ---- clock (thread 0 only; everyone re-reads after the barrier) ---- */
-        if (tid == 0) {
-            const double tn = t + dt;
-            const long long nn = ns + 1;
-            ctrl->t = tn;
-            ctrl->dt = dt;
-            ctrl->num_steps = nn;
-            int act = (tn < tf) && (ctrl->max_steps < 0 || nn < ctrl->max_steps);
-            if (a.sp.is_storing &&
-                tn >= a.sp.storing_interval * (double) (ctrl->store_count - a.sp.store_initial_offset + 1)) {
-                ctrl->snapshot_due = 1;
-                act = 0;
-            }
-            ctrl->active = act;
-            __threadfence_block();
+        /* ---- clock: every thread advances its copy; the leader publishes it ---- */
+        t = t + dt;
+        ns = ns + 1;
+        int act = (t < tf) && (max_steps < 0 || ns < max_steps);
+        bool snap = false;
+        if (a.sp.is_storing &&
+            t >= a.sp.storing_interval * (double) (store_count - a.sp.store_initial_offset + 1)) {
+            snap = true;
+            act = 0;
         }
-        __syncthreads();
+        if (leader) {
+            ctrl->t = t;
+            ctrl->dt = dt;
+            ctrl->num_steps = ns;
+            if (snap) ctrl->snapshot_due = 1;
+            ctrl->active = act;
+        }
+        have_part = fused;
+        /* the fused path's next barrier is the dt gather at the top */
+        if (!act || !fused) cl.sync();
+        if (!act) return;
     }
 }
 
@@ -373,6 +743,29 @@ __global__ void __launch_bounds__(kThreads) run1d_kernel(const Run1dArgs a)
             goto done;                                                                       \
         }                                                                                    \
     } while (0)
+
+/* The largest cluster (16, 8, ... CTAs of kThreads) that this device can
+ * place: 16 needs the non-portable cluster size. */
+int run1d_cluster_size()
+{
+    cudaFuncSetAttribute(run1d_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    for (int c = kClusterMax; c > 1; c /= 2) {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(c);
+        cfg.blockDim = dim3(kThreads);
+        cudaLaunchAttribute at;
+        at.id = cudaLaunchAttributeClusterDimension;
+        at.val.clusterDim.x = c;
+        at.val.clusterDim.y = 1;
+        at.val.clusterDim.z = 1;
+        cfg.attrs = &at;
+        cfg.numAttrs = 1;
+        int num = 0;
+        if (cudaOccupancyMaxActiveClusters(&num, run1d_kernel, &cfg) == cudaSuccess && num > 0) return c;
+        cudaGetLastError();
+    }
+    return 1;
+}
 
 extern "C" int hydro_run1d(const HydroGrid1D *grid, double *const Wh[3], double *const Uh[3],
                            const HydroStepParams *sp, double tf, int64 max_steps, int store_count,
@@ -394,6 +787,9 @@ extern "C" int hydro_run1d(const HydroGrid1D *grid, double *const Wh[3], double 
     int rc = -1;
     Run1dArgs a;
     memset(&a, 0, sizeof a);
+    cudaLaunchConfig_t lcfg = {};
+    cudaLaunchAttribute lattr;
+    memset(&lattr, 0, sizeof lattr);
 
     CK1(cudaSetDevice(opt->device), "cudaSetDevice");
     CK1(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking), "cudaStreamCreate");
@@ -445,10 +841,22 @@ extern "C" int hydro_run1d(const HydroGrid1D *grid, double *const Wh[3], double 
     CK1(cudaStreamSynchronize(s), "upload");
     CK1(cudaEventElapsedTime(&ms_h2d, ev[0], ev[1]), "cudaEventElapsedTime");
 
+    {
+        const int cs = run1d_cluster_size();
+        lcfg.gridDim = dim3(cs);
+        lcfg.blockDim = dim3(kThreads);
+        lcfg.stream = s;
+        lattr.id = cudaLaunchAttributeClusterDimension;
+        lattr.val.clusterDim.x = cs;
+        lattr.val.clusterDim.y = 1;
+        lattr.val.clusterDim.z = 1;
+        lcfg.attrs = &lattr;
+        lcfg.numAttrs = 1;
+    }
     for (;;) {
         if (!c.active) break;
         CK1(cudaEventRecord(ev[2], s), "cudaEventRecord");
-        run1d_kernel<<<1, kThreads, 0, s>>>(a);
+        CK1(cudaLaunchKernelEx(&lcfg, run1d_kernel, a), "run1d launch");
         launches++;
         CK1(cudaGetLastError(), "run1d kernel");
         CK1(cudaEventRecord(ev[3], s), "cudaEventRecord");

@@ -18,6 +18,7 @@ import ctypes as C
 import os
 import sys
 import subprocess
+import time
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -129,7 +130,6 @@ class Backend:
         self.prefix = prefix
 
     def run_2d(self, prob: Problem2D) -> Result:
-        import time
         W = np.ascontiguousarray(prob.W.copy())
         U = np.ascontiguousarray(prob.U.copy())
         n = C.c_longlong(0)
@@ -162,13 +162,15 @@ class Backend:
         err = C.create_string_buffer(4096)
         f = getattr(self.lib, self.prefix + "run_1d_ex")
         enc = lambda s: s.encode() if s is not None else None
+        t0 = time.perf_counter()
         rc = f(prob.nx, prob.g, prob.x_min, prob.x_max, prob.gamma,
                enc(prob.integrator), enc(prob.riemann_solver), enc(prob.slope_limiter),
                enc(prob.bc[0]), enc(prob.bc[1]), prob.cfl, prob.tf, prob.max_steps,
                _ptr(W[0]), _ptr(W[1]), _ptr(W[2]), _ptr(U[0]), _ptr(U[1]), _ptr(U[2]),
                C.byref(n), C.byref(t), C.byref(dt), err, len(err),
                enc(getattr(prob, "coord_sys", "cartesian_1d")))
-        return Result(rc, W, U, n.value, t.value, dt.value, err.value.decode(errors="replace"))
+        secs = time.perf_counter() - t0
+        return Result(rc, W, U, n.value, t.value, dt.value, err.value.decode(errors="replace"), secs)
 
     def hllc_2d(self, gamma, L, R, tol=1e-6):
         out = np.zeros(4)
