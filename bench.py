@@ -21,6 +21,12 @@ roofline: the step kernel against measured HBM bandwidth (64 algorithmic
 cpu_baseline: the CPU implementation of the same step on this host's cores,
   on a bounded sample (the first few steps of the same grid).
 
+Other workloads (--workload): point_blast (8192^2 with --size 8192), ensemble
+(256 four-quadrant grids), adjoint (1024^2 shear layer), snapshots, and sod:
+the 1000-cell Sod tube, Godunov + exact solver, one "step" = one whole run to
+t = 0.2, timed on the device and through the drop-in call, with the serial
+CPU implementation timed beside it.
+
 --impl reference times the reference's CPU implementation of the path: the
 unmodified reference build (oracle/_ref) where it exists, else this
 project's C restatement (oracle/), OpenMP over all host cores.
