@@ -80,6 +80,29 @@ def test_random_1d_against_oracle(gpu_available, oracle_mod, bc, integ, solver, 
     assert np.all(rel_l1_1d(r.U, ref.U, p.g) <= REL_L1_TOL)
 
 
+@pytest.mark.parametrize("bc", [("reflective", "transmissive"), ("transmissive", "reflective"),
+                                ("transmissive", "none"), ("none", "none"), ("periodic", "periodic")])
+@pytest.mark.parametrize("n,g", [(2, 2), (3, 2), (5, 3), (7, 1), (64, 3)])
+@pytest.mark.parametrize("integ,solver", [("godunov_first_order_1d", "riemann_solver_exact"),
+                                          ("muscl_hancock_1d", "riemann_solver_hllc")])
+def test_1d_ghost_cells_small_grids(gpu_available, oracle_mod, bc, n, g, integ, solver):
+    """The boundary routine's ghost cells, written by the threads that convert
+    their source cells, on grids down to n = g (sources of the two sides
+    overlapping), every ghost width the reference allows and mixed sides:
+    the whole padded state, ghost cells included, against the oracle."""
+    if integ == "muscl_hancock_1d" and g < 2:
+        pytest.skip("MUSCL-Hancock needs two ghost cells")
+    from hydrofv_gb300.problems import random_problem_1d
+    p = random_problem_1d(n, 3, bc, integ, solver, "minmod", steps=12, g=g)
+    ref = oracle_mod.load("oracle").run_1d(p)
+    r = run1(p)
+    assert r.code == 0 and ref.rc == 0, r.message
+    assert r.num_steps == ref.num_steps == 12
+    for got, want in ((r.W, ref.W), (r.U, ref.U)):
+        scale = np.max(np.abs(want), axis=1, keepdims=True)
+        assert np.all(np.abs(got - want) <= 1e-12 * scale)
+
+
 def test_1d_large_grid_runs_in_one_cta(gpu_available, oracle_mod):
     from hydrofv_gb300.problems import random_problem_1d
     p = random_problem_1d(5000, 8, ("periodic", "periodic"), "muscl_hancock_1d",
