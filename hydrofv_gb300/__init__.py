@@ -187,6 +187,7 @@ _SIGNATURES = {
     "hydro_fx_eval_host": (None, [C.c_int, C.c_longlong, _dp, _dp, _dp, C.c_void_p]),
     "hydro_gpu_fx_eval": (C.c_int, [C.c_int, C.c_int, C.c_longlong, _dp, _dp, _dp, _dp, C.c_void_p]),
     "hydro_fx_div_seeded_host": (None, [C.c_longlong, _dp, _dp, C.c_void_p, _dp, C.c_void_p]),
+    "hydro_fx_ratio_below_host": (None, [C.c_longlong, _dp, _dp, _dp, C.c_void_p, C.c_void_p]),
     "hydro_gpu_pointwise_eval": (C.c_int, [C.c_int, C.c_int, C.c_longlong, _dp, C.c_double, _dp, _dp, _dp,
                                            _dp, _P(C.c_int)]),
     "hydro_gpu_device_count": (C.c_int, []),
@@ -844,6 +845,19 @@ def gpu_fx_eval(op, a, b=None, device=0):
     if rc != 0:
         raise HydroError(rc, "hydro_gpu_fx_eval failed (CUDA error)")
     return fast, hw, ok.astype(bool)
+
+
+def fx_ratio_below_host(x, y, tol):
+    """The exact solver's convergence test RN(x / y) < tol decided without the
+    divide (host build): (answers, decided flags)."""
+    x = np.ascontiguousarray(x, dtype=np.float64).ravel()
+    y = np.ascontiguousarray(np.broadcast_to(y, x.shape), dtype=np.float64).ravel()
+    t = np.ascontiguousarray(np.broadcast_to(tol, x.shape), dtype=np.float64).ravel()
+    out = np.zeros(x.size, dtype=np.uint8)
+    dec = np.zeros(x.size, dtype=np.uint8)
+    library().hydro_fx_ratio_below_host(x.size, x.ctypes.data_as(_dp), y.ctypes.data_as(_dp),
+                                        t.ctypes.data_as(_dp), out.ctypes.data, dec.ctypes.data)
+    return out.astype(bool), dec.astype(bool)
 
 
 POINTWISE_OPS = {"hllc_2d": (0, 4), "guess_p": (1, 1), "exact_flux_1d": (2, 3), "hllc_1d": (3, 3),

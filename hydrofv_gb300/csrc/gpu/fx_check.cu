@@ -124,6 +124,16 @@ void hydro_fx_div_seeded_host(long long n, const double *a, const double *b, con
     }
 }
 
+void hydro_fx_ratio_below_host(long long n, const double *x, const double *y, const double *tol,
+                               unsigned char *out, unsigned char *decided)
+{
+    for (long long i = 0; i < n; i++) {
+        bool d;
+        out[i] = ratio_below_fast(x[i], y[i], tol[i], d) ? 1 : 0;
+        decided[i] = d ? 1 : 0;
+    }
+}
+
 int hydro_gpu_fx_eval(int device, int op, long long n, const double *a, const double *b,
                       double *fast, double *hw, unsigned char *ok)
 {

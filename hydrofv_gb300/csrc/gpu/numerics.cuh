@@ -184,6 +184,40 @@ HD bool ratio_at_most_two(R p_max, R p_min)
     return p_max / p_min <= R(2);
 }
 
+/*
+ * RN(x / y) < tol for x >= 0 and y > 0 (the exact solver's convergence test),
+ * decided without the divide where a margin allows.  With T = RN(RN(tol y) c):
+ *   c = 1 - 2^-50:  x < T implies x / y < tol (1 - 2^-51), so RN(x / y) is at
+ *                   least one ulp below tol: true;
+ *   c = 1 + 2^-50:  x > T implies x / y > tol (1 + 2^-51), so RN(x / y) >= tol:
+ *                   false
+ * (each rounding is within a factor 1 +- 2^-53, and one ulp of tol is at most
+ * tol 2^-52).  The bounds need tol y to be a normal double: otherwise, and
+ * between the two margins, `decided` comes back false and the caller divides.
+ */
+FXHD bool ratio_below_fast(double x, double y, double tol, bool &decided)
+{
+    const double ty = tol * y;
+    decided = false;
+    if (!(ty > 1e-290 && ty < 1e290 && x <= 1e300)) return false;
+    if (x < ty * (1.0 - 0x1p-50)) { decided = true; return true; }
+    if (x > ty * (1.0 + 0x1p-50)) { decided = true; return false; }
+    return false;
+}
+
+template <class R>
+HD bool ratio_below(R x, R y, R tol) { return dv(x, y) < tol; }
+
+HD bool ratio_below(double x, double y, double tol)
+{
+#if defined(__CUDA_ARCH__)
+    bool decided;
+    const bool r = ratio_below_fast(x, y, tol, decided);
+    if (decided) return r;
+#endif
+    return dv(x, y) < tol;
+}
+
 /* Star-pressure guess (PVRS / two-rarefaction / two-shock). */
 template <class R>
 HD R guess_p(const GasConst<R> &c, R rho_L, R u_L, R p_L, R a_L,
@@ -542,7 +576,7 @@ HD int exact_p_star(const GasConst<R> &c, R rho_L, R u_L, R p_L, R a_L,
         }
         const R p1 = p0 - dv(f, fp);
         if (p1 < R(0)) break;
-        if (dv(R(2) * fabs(p1 - p0), p1 + p0) < c.tol) {
+        if (ratio_below(R(2) * fabs(p1 - p0), p1 + p0, c.tol)) {
             *out = p1;
             return DEV_OK;
         }

@@ -148,6 +148,7 @@ __device__ __forceinline__ Quad make_quad()
 
 struct Sides {
     double rho_L, p_L, a_L, rho_R, p_R, a_R, du;
+    double A_L, A_R;   /* 2 / ((gamma + 1) rho) of each side, the shock branch's A */
 };
 
 /* fK (q < 2) or dfK (q >= 2) of side q & 1 at p*, the same expressions as
@@ -167,7 +168,7 @@ __device__ void quad_fdf(const Quad &Q, const GasConst<double> &c, const Sides &
     const double a = side ? S.a_R : S.a_L;
     double x, r = 0.0;
     if (ps > p) {
-        const double A = dv(2.0, c.gp1 * rho);
+        const double A = side ? S.A_R : S.A_L;
         const double B = p * c.gm1_gp1;
         if (d) x = sample ? 0.0 : (1.0 - dv(0.5 * (ps - p), B - ps)) * sq(dv(A, B + ps));
         else x = (ps - p) * sq(dv(A, ps + B));
@@ -193,10 +194,9 @@ __device__ __forceinline__ double quad_f(const Quad &Q, const GasConst<double> &
 }
 
 /* exact_p_star (numerics.cuh) with the function evaluations shared by the quad. */
-__device__ int quad_p_star(const Quad &Q, const GasConst<double> &c, double rho_L, double u_L, double p_L,
-                           double a_L, double rho_R, double u_R, double p_R, double a_R, double *out)
+__device__ int quad_p_star(const Quad &Q, const GasConst<double> &c, const Sides &S, double rho_L, double u_L,
+                           double p_L, double a_L, double rho_R, double u_R, double p_R, double a_R, double *out)
 {
-    const Sides S{ rho_L, p_L, a_L, rho_R, p_R, a_R, u_R - u_L };
     const double pg = guess_p(c, rho_L, u_L, p_L, a_L, rho_R, u_R, p_R, a_R);
     bool bracket = false;
     double p_hi = pg;
@@ -217,7 +217,7 @@ __device__ int quad_p_star(const Quad &Q, const GasConst<double> &c, double rho_
         }
         const double p1 = p0 - dv(f, fp);
         if (p1 < 0.0) break;
-        if (dv(2.0 * fabs(p1 - p0), p1 + p0) < c.tol) {
+        if (ratio_below(2.0 * fabs(p1 - p0), p1 + p0, c.tol)) {
             *out = p1;
             return DEV_OK;
         }
@@ -318,18 +318,24 @@ __device__ void quad_sample(const GasConst<double> &c, double rho_L, double u_L,
 __device__ int quad_exact_solve(const Quad &Q, const GasConst<double> &c, double rho_L, double u_L, double p_L,
                                 double rho_R, double u_R, double p_R, double S, double o[3])
 {
-    const double a_L = (rho_L > 0.0) ? sound_speed(c, rho_L, p_L) : 0.0;
-    const double a_R = (rho_R > 0.0) ? sound_speed(c, rho_R, p_R) : 0.0;
+    /* lanes 0, 2 the left side, 1, 3 the right: the sound speed (exact_solve_1d's
+     * a_L, a_R) and the shock coefficient A of exact_fK / exact_dfK */
+    const int side = Q.q & 1;
+    const double rho_s = side ? rho_R : rho_L, p_s = side ? p_R : p_L;
+    const double a_s = (rho_s > 0.0) ? sound_speed(c, rho_s, p_s) : 0.0;
+    const double A_s = dv(2.0, c.gp1 * rho_s);
+    const double a_L = __shfl_sync(Q.mask, a_s, Q.base), a_R = __shfl_sync(Q.mask, a_s, Q.base + 1);
+    const double A_L = __shfl_sync(Q.mask, A_s, Q.base), A_R = __shfl_sync(Q.mask, A_s, Q.base + 1);
     if (rho_L <= 0.0 || rho_R <= 0.0 || dv((a_L + a_R) * 2.0, c.gp1) <= (u_R - u_L)) {
         double s[4];
         solve_vacuum(c, rho_L, u_L, 0.0, p_L, a_L, rho_R, u_R, 0.0, p_R, a_R, S, s);
         o[0] = s[0]; o[1] = s[1]; o[2] = s[3];
         return DEV_OK;
     }
+    const Sides Sd{ rho_L, p_L, a_L, rho_R, p_R, a_R, u_R - u_L, A_L, A_R };
     double ps = 0.0;
-    const int rc = quad_p_star(Q, c, rho_L, u_L, p_L, a_L, rho_R, u_R, p_R, a_R, &ps);
+    const int rc = quad_p_star(Q, c, Sd, rho_L, u_L, p_L, a_L, rho_R, u_R, p_R, a_R, &ps);
     if (rc != DEV_OK) { o[0] = o[1] = o[2] = 0.0; return rc; }
-    const Sides Sd{ rho_L, p_L, a_L, rho_R, p_R, a_R, u_R - u_L };
     double v[4], pre[4];
     quad_fdf(Q, c, Sd, ps, v, true, pre);
     const double us = 0.5 * (u_L + u_R) + 0.5 * (v[1] - v[0]);

@@ -355,6 +355,11 @@ int hydro_gpu_fx_eval(int device, int op, long long n, const double *a, const do
 void hydro_fx_div_seeded_host(long long n, const double *a, const double *b, const float *seed_scale,
                               double *out, unsigned char *ok);
 
+/* The exact solver's convergence test RN(x[i] / y[i]) < tol[i] decided without
+ * the divide (host build): out[i] is the answer where decided[i] = 1. */
+void hydro_fx_ratio_below_host(long long n, const double *x, const double *y, const double *tol,
+                               unsigned char *out, unsigned char *decided);
+
 /* Device build of the exported pointwise numerics over n state pairs:
  * L[4k..4k+3], R[4k..4k+3] = (rho, u, v, p) (the 1D forms read rho, u, p),
  * gas constants from gamma[k] and tol.

@@ -352,3 +352,26 @@ def test_pow_tables_match_their_generator():
         gen.main()
     with open(os.path.join(here, "pow_tables.h")) as f:
         assert buf.getvalue() == f.read()
+
+
+def test_convergence_test_without_divide():
+    """The exact solver's convergence test RN(x / y) < tol, decided by two
+    multiplies where a margin allows: wherever it decides, the answer is that
+    of the IEEE divide, including quotients within a few ulps of tol."""
+    rng = np.random.default_rng(12)
+    n = 400_000
+    tols = np.concatenate([np.full(n // 2, 1e-6), 10.0 ** rng.uniform(-12, -1, n // 2)])
+    y = 10.0 ** rng.uniform(-6, 6, n)
+    # quotients spread around tol, many within a few ulps of it
+    k = rng.integers(-40, 41, n)
+    q = tols * (1.0 + k * 2.0 ** -52) * np.where(rng.random(n) < 0.5, 1.0, 10.0 ** rng.uniform(-3, 3, n))
+    x = q * y
+    x[:1000] = 0.0
+    out, dec = h.fx_ratio_below_host(x, y, tols)
+    ref = (x / y) < tols
+    assert np.array_equal(out[dec], ref[dec])
+    assert dec.mean() > 0.8
+    # outside the guarded range nothing is decided
+    _, d2 = h.fx_ratio_below_host(np.array([1.0, np.nan, 1e301]), np.array([1e-300, 1.0, 1.0]),
+                                  np.array([1e-6, 1e-6, 1e-6]))
+    assert not d2.any()
