@@ -188,6 +188,7 @@ _SIGNATURES = {
     "hydro_gpu_fx_eval": (C.c_int, [C.c_int, C.c_int, C.c_longlong, _dp, _dp, _dp, _dp, C.c_void_p]),
     "hydro_fx_div_seeded_host": (None, [C.c_longlong, _dp, _dp, C.c_void_p, _dp, C.c_void_p]),
     "hydro_fx_ratio_below_host": (None, [C.c_longlong, _dp, _dp, _dp, C.c_void_p, C.c_void_p]),
+    "hydro_fx_quot_le_host": (None, [C.c_longlong, _dp, _dp, _dp, C.c_void_p, C.c_void_p]),
     "hydro_gpu_pointwise_eval": (C.c_int, [C.c_int, C.c_int, C.c_longlong, _dp, C.c_double, _dp, _dp, _dp,
                                            _dp, _P(C.c_int)]),
     "hydro_gpu_device_count": (C.c_int, []),
@@ -857,6 +858,19 @@ def fx_ratio_below_host(x, y, tol):
     dec = np.zeros(x.size, dtype=np.uint8)
     library().hydro_fx_ratio_below_host(x.size, x.ctypes.data_as(_dp), y.ctypes.data_as(_dp),
                                         t.ctypes.data_as(_dp), out.ctypes.data, dec.ctypes.data)
+    return out.astype(bool), dec.astype(bool)
+
+
+def fx_quot_le_host(x, y, z):
+    """The solvers' vacuum-generation test RN(x / y) <= z decided without the
+    divide (host build): (answers, decided flags)."""
+    x = np.ascontiguousarray(x, dtype=np.float64).ravel()
+    y = np.ascontiguousarray(np.broadcast_to(y, x.shape), dtype=np.float64).ravel()
+    z = np.ascontiguousarray(np.broadcast_to(z, x.shape), dtype=np.float64).ravel()
+    out = np.zeros(x.size, dtype=np.uint8)
+    dec = np.zeros(x.size, dtype=np.uint8)
+    library().hydro_fx_quot_le_host(x.size, x.ctypes.data_as(_dp), y.ctypes.data_as(_dp),
+                                    z.ctypes.data_as(_dp), out.ctypes.data, dec.ctypes.data)
     return out.astype(bool), dec.astype(bool)
 
 

@@ -134,6 +134,16 @@ void hydro_fx_ratio_below_host(long long n, const double *x, const double *y, co
     }
 }
 
+void hydro_fx_quot_le_host(long long n, const double *x, const double *y, const double *z,
+                           unsigned char *out, unsigned char *decided)
+{
+    for (long long i = 0; i < n; i++) {
+        bool d;
+        out[i] = quot_le_fast(x[i], y[i], z[i], d) ? 1 : 0;
+        decided[i] = d ? 1 : 0;
+    }
+}
+
 int hydro_gpu_fx_eval(int device, int op, long long n, const double *a, const double *b,
                       double *fast, double *hw, unsigned char *ok)
 {

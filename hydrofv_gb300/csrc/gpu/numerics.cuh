@@ -218,6 +218,50 @@ HD bool ratio_below(double x, double y, double tol)
     return dv(x, y) < tol;
 }
 
+/*
+ * RN(x / y) <= z for x > 0 and y > 0 normal (the vacuum-generation test of
+ * the HLLC and exact solvers: x = 2 (a_L + a_R), y = gamma + 1, z = u_R - u_L),
+ * decided from the exponents alone where they leave no doubt, with integer
+ * operations only (the FP64 step kernels are bound by their FP64 pipe).  With
+ * d = e_x - e_y (unbiased exponents), x / y lies in (2^(d-1), 2^(d+1)), so
+ * RN(x / y) lies in [2^(d-1), 2^(d+1)]; z lies in [2^e_z, 2^(e_z+1)).  So:
+ *   z < 0 (nonzero):   false (the quotient is positive);
+ *   e_z >= d + 1:      RN(x / y) <= 2^(d+1) <= z: true;
+ *   e_z <= d - 2:      z < 2^(d-1) <= RN(x / y): false.
+ * Zero, subnormal, infinite and NaN operands and e_z in {d - 1, d} are not
+ * decided (`decided` false): the caller divides.
+ */
+FXHD bool quot_le_fast(double x, double y, double z, bool &decided)
+{
+    const fx::u64 bx = fx::bits(x), by = fx::bits(y), bz = fx::bits(z);
+    const int ex = (int) (bx >> 52), ey = (int) (by >> 52);           /* sign bit included */
+    const int ez = (int) ((bz >> 52) & 0x7ffu);
+    decided = false;
+    if ((unsigned) (ex - 1) >= 2046u || (unsigned) (ey - 1) >= 2046u) return false;
+    if (bz >> 63) {
+        if ((bz << 1) != 0ull && ez != 0x7ff) decided = true;          /* finite z < 0 */
+        return false;
+    }
+    if ((unsigned) (ez - 1) >= 2046u) return false;
+    const int d = ex - ey;
+    if (ez - 1023 >= d + 1) { decided = true; return true; }
+    if (ez - 1023 <= d - 2) { decided = true; return false; }
+    return false;
+}
+
+template <class R>
+HD bool quot_le(R x, R y, R z) { return le(dv(x, y), z); }
+
+HD bool quot_le(double x, double y, double z)
+{
+#if defined(__CUDA_ARCH__)
+    bool decided;
+    const bool r = quot_le_fast(x, y, z, decided);
+    if (decided) return r;
+#endif
+    return le(dv(x, y), z);
+}
+
 /* Star-pressure guess (PVRS / two-rarefaction / two-shock). */
 template <class R>
 HD R guess_p(const GasConst<R> &c, R rho_L, R u_L, R p_L, R a_L,
@@ -338,7 +382,7 @@ HD int hllc_classify(const GasConst<R> &c, R rho_L, R u_L, R p_L, R rho_R, R u_R
     a_L = lt(R(0), rho_L) ? sound_speed(c, rho_L, p_L) : R(0);
     a_R = lt(R(0), rho_R) ? sound_speed(c, rho_R, p_R) : R(0);
     ppv = R(0);
-    if (le(rho_L, R(0)) || le(rho_R, R(0)) || le(dv((a_L + a_R) * R(2), c.gp1), u_R - u_L))
+    if (le(rho_L, R(0)) || le(rho_R, R(0)) || quot_le((a_L + a_R) * R(2), c.gp1, u_R - u_L))
         return PREG_VACUUM;
     const bool l_above = lt(p_R, p_L);
     const R p_min = l_above ? p_R : p_L;
@@ -471,7 +515,7 @@ HD int hllc_flux_1d(const GasConst<R> &c, R rho_L, R u_L, R p_L, R rho_R, R u_R,
 {
     const R a_L = (rho_L > R(0)) ? sound_speed(c, rho_L, p_L) : R(0);
     const R a_R = (rho_R > R(0)) ? sound_speed(c, rho_R, p_R) : R(0);
-    if (rho_L <= R(0) || rho_R <= R(0) || dv((a_L + a_R) * R(2), c.gp1) <= (u_R - u_L)) {
+    if (rho_L <= R(0) || rho_R <= R(0) || quot_le((a_L + a_R) * R(2), c.gp1, u_R - u_L)) {
         R s[4];
         solve_vacuum(c, rho_L, u_L, R(0), p_L, a_L, rho_R, u_R, R(0), p_R, a_R, R(0), s);
         const R E = s[0] * (R(0.5) * s[1] * s[1] + dv(s[3], s[0] * c.gm1));
@@ -676,7 +720,7 @@ HD int exact_solve_1d(const GasConst<R> &c, R rho_L, R u_L, R p_L, R rho_R, R u_
 {
     const R a_L = (rho_L > R(0)) ? sound_speed(c, rho_L, p_L) : R(0);
     const R a_R = (rho_R > R(0)) ? sound_speed(c, rho_R, p_R) : R(0);
-    if (rho_L <= R(0) || rho_R <= R(0) || dv((a_L + a_R) * R(2), c.gp1) <= (u_R - u_L)) {
+    if (rho_L <= R(0) || rho_R <= R(0) || quot_le((a_L + a_R) * R(2), c.gp1, u_R - u_L)) {
         R s[4];
         solve_vacuum(c, rho_L, u_L, R(0), p_L, a_L, rho_R, u_R, R(0), p_R, a_R, S, s);
         o[0] = s[0]; o[1] = s[1]; o[2] = s[3];

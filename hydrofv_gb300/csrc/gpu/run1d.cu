@@ -326,7 +326,7 @@ __device__ int quad_exact_solve(const Quad &Q, const GasConst<double> &c, double
     const double A_s = dv(2.0, c.gp1 * rho_s);
     const double a_L = __shfl_sync(Q.mask, a_s, Q.base), a_R = __shfl_sync(Q.mask, a_s, Q.base + 1);
     const double A_L = __shfl_sync(Q.mask, A_s, Q.base), A_R = __shfl_sync(Q.mask, A_s, Q.base + 1);
-    if (rho_L <= 0.0 || rho_R <= 0.0 || dv((a_L + a_R) * 2.0, c.gp1) <= (u_R - u_L)) {
+    if (rho_L <= 0.0 || rho_R <= 0.0 || quot_le((a_L + a_R) * 2.0, c.gp1, u_R - u_L)) {
         double s[4];
         solve_vacuum(c, rho_L, u_L, 0.0, p_L, a_L, rho_R, u_R, 0.0, p_R, a_R, S, s);
         o[0] = s[0]; o[1] = s[1]; o[2] = s[3];

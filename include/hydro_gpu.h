@@ -360,6 +360,11 @@ void hydro_fx_div_seeded_host(long long n, const double *a, const double *b, con
 void hydro_fx_ratio_below_host(long long n, const double *x, const double *y, const double *tol,
                                unsigned char *out, unsigned char *decided);
 
+/* The solvers' vacuum-generation test RN(x[i] / y[i]) <= z[i] decided without
+ * the divide (host build): out[i] is the answer where decided[i] = 1. */
+void hydro_fx_quot_le_host(long long n, const double *x, const double *y, const double *z,
+                           unsigned char *out, unsigned char *decided);
+
 /* Device build of the exported pointwise numerics over n state pairs:
  * L[4k..4k+3], R[4k..4k+3] = (rho, u, v, p) (the 1D forms read rho, u, p),
  * gas constants from gamma[k] and tol.

@@ -169,7 +169,7 @@ def test_host_sqrt_special_operands_take_the_fallback():
 
 
 @pytest.mark.gpu
-def test_gpu_division_is_bitwise_ieee():
+def test_gpu_division_is_bitwise_ieee(gpu_available):
     rng = np.random.default_rng(5)
     n = 1 << 22
     sets = [(_doubles(rng, n, 900, 1150), _doubles(rng, n, 900, 1150)),
@@ -188,7 +188,7 @@ def test_gpu_division_is_bitwise_ieee():
 
 
 @pytest.mark.gpu
-def test_gpu_sqrt_is_bitwise_ieee():
+def test_gpu_sqrt_is_bitwise_ieee(gpu_available):
     rng = np.random.default_rng(6)
     x = np.concatenate([_doubles(rng, 1 << 22, 1, 2046, signed=False), _edge_operands(),
                         np.arange(1, 1 << 16, dtype=np.float64) ** 2,
@@ -276,7 +276,7 @@ def test_host_pow_special_operands_take_the_fallback():
 
 
 @pytest.mark.gpu
-def test_gpu_pow_matches_the_host_build_bitwise():
+def test_gpu_pow_matches_the_host_build_bitwise(gpu_available):
     """The device build is the same integer algorithm (no seeds): bit-identical
     to the host build wherever its fast path applies; elsewhere it is the
     hardware pow."""
@@ -324,7 +324,7 @@ def test_host_bit_sign_test_matches_the_product():
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("op", [3, 4, 5], ids=["minmod", "van_leer", "mc"])
-def test_gpu_limiters_match_the_fp64_expressions(op):
+def test_gpu_limiters_match_the_fp64_expressions(gpu_available, op):
     """The device limiters decide the sign test and the minima on the bits;
     the results are the host build's FP64 expressions bit for bit."""
     rng = np.random.default_rng(22 + op)
@@ -375,3 +375,31 @@ def test_convergence_test_without_divide():
     _, d2 = h.fx_ratio_below_host(np.array([1.0, np.nan, 1e301]), np.array([1e-300, 1.0, 1.0]),
                                   np.array([1e-6, 1e-6, 1e-6]))
     assert not d2.any()
+
+
+def test_vacuum_test_without_divide():
+    """The solvers' vacuum-generation test RN(2 (a_L + a_R) / (gamma + 1)) <=
+    u_R - u_L, decided from the exponents without the divide: wherever it
+    decides, the answer is that of the IEEE divide, including quotients within
+    a few ulps of z (which it must leave undecided)."""
+    rng = np.random.default_rng(13)
+    n = 400_000
+    y = rng.choice([2.4, 8.0 / 3.0, 2.2], n)
+    x = 2.0 * (10.0 ** rng.uniform(-3, 2, n))
+    k = rng.integers(-40, 41, n)
+    z = (x / y) * (1.0 + k * 2.0 ** -52)
+    z[: n // 4] = rng.uniform(-3, 3, n // 4)            # typical velocity jumps
+    z[n // 4: n // 4 + 1000] = 0.0
+    z[n // 4 + 1000: n // 4 + 2000] = -0.0
+    x[:500] = 0.0
+    out, dec = h.fx_quot_le_host(x, y, z)
+    ref = (x / y) <= z
+    assert np.array_equal(out[dec], ref[dec])
+    assert dec[: n // 4].mean() > 0.9
+    # NaN and infinite operands and a zero z are left to the divide; a tiny
+    # normal z is decided by its exponent
+    xs = np.array([np.nan, 1.0, np.inf, 1.0, 1.0, 1.0, 0.0])
+    zs = np.array([1.0, np.nan, 1.0, 0.0, -0.0, 1e-300, 1.0])
+    o2, d2 = h.fx_quot_le_host(xs, 2.4, zs)
+    assert d2.tolist() == [False, False, False, False, False, True, False]
+    assert not o2[5]

@@ -23,6 +23,12 @@ from hydrofv_gb300.problems import (Problem2D, apply_bc_2d, mid_points, primitiv
 pytestmark = pytest.mark.gpu
 
 
+@pytest.fixture(autouse=True)
+def _device(gpu_available):
+    """Every test here needs the GPU: skip cleanly where none is visible."""
+    return gpu_available
+
+
 def smooth_problem(nx, ny, bc, limiter, seed=0, g=2, gamma=1.4):
     """Smooth periodic-friendly fields built from a few Fourier modes with
     irrational phases (no exact slope ties)."""
