@@ -678,7 +678,9 @@ def main() -> None:
         "roofline": {"bound": "hbm", "achieved": achieved_gbs, "peak": pk["hbm_gbs"],
                      "unit": "GB/s", "frac": achieved_gbs / pk["hbm_gbs"],
                      "traffic": traffic, "peak_source": pk["source"],
-                     "bytes_per_cell_update": bytes_per_cell},
+                     "bytes_per_cell_update": bytes_per_cell,
+                     "note": "HBM is not the binding roof of this stencil: the step is bound by "
+                             "its FP64 (FP32) pipe, reported in fp_roofline"},
         "fp_roofline": fp_roofline(prec, value, fp64_tflops, fp32_tflops, H),
         "forms": {
             "fp64": {"value": cells * args.steps / (fp64_ms * 1e-3), "ms_per_step": fp64_ms / args.steps,
