@@ -875,7 +875,7 @@ def fx_quot_le_host(x, y, z):
 
 
 POINTWISE_OPS = {"hllc_2d": (0, 4), "guess_p": (1, 1), "exact_flux_1d": (2, 3), "hllc_1d": (3, 3),
-                 "exact_1d": (4, 3)}
+                 "exact_1d": (4, 3), "exact_flux_1d_quad": (5, 3), "exact_1d_quad": (6, 3)}
 
 
 def gpu_pointwise_eval(name, gamma, L, R, aux=None, tol=1e-6, device=0):
@@ -883,13 +883,14 @@ def gpu_pointwise_eval(name, gamma, L, R, aux=None, tol=1e-6, device=0):
     (L, R: (n, 4) arrays of rho, u, v, p; gamma: (n,)): (outputs, return
     codes).  name: "hllc_2d", "hllc_1d", "guess_p" (aux = (n, 2) sound
     speeds a_L, a_R), "exact_flux_1d" or "exact_1d" (aux = (n,) sample
-    speeds).  Return codes: 0, 1 (HLLC wave speed), 3 or 4 (exact solver)."""
+    speeds), or "exact_flux_1d_quad" / "exact_1d_quad" (the same, as the 1D
+    kernel computes them with four lanes per state pair).  Return codes: 0, 1 (HLLC wave speed), 3 or 4 (exact solver)."""
     op, width = POINTWISE_OPS[name]
     g = np.ascontiguousarray(gamma, dtype=np.float64).ravel()
     n = g.size
     L = np.ascontiguousarray(L, dtype=np.float64).reshape(n, 4)
     R = np.ascontiguousarray(R, dtype=np.float64).reshape(n, 4)
-    need = {1: 2, 2: 1, 4: 1}.get(op, 0)
+    need = {1: 2, 2: 1, 4: 1, 5: 1, 6: 1}.get(op, 0)
     a = np.ascontiguousarray(np.zeros(n * max(need, 1)) if aux is None else aux, dtype=np.float64).ravel()
     if a.size < n * need:
         raise ValueError(f"{name} needs {need} auxiliary values per state pair")

@@ -15,6 +15,7 @@
 #include "fp64_int.cuh"
 #include "pow_int.cuh"
 #include "numerics.cuh"
+#include "quad_exact.cuh"
 #include "hydro_gpu.h"
 
 using namespace hydro;
@@ -87,6 +88,35 @@ __global__ void pointwise_kernel(int op, long long n, const double *gamma, doubl
             for (int q = 0; q < 3; q++) out[3 * k + q] = o[q];
         }
         rc[k] = code;
+    }
+}
+
+/* The 1D kernel's four-lane exact solver: four consecutive threads per state
+ * pair (op 5: the flux at x/t = aux[k], op 6: the sampled state). */
+__global__ void pointwise_quad_kernel(int op, long long n, const double *gamma, double tol,
+                                      const double *L, const double *R, const double *aux, double *out,
+                                      int *rc)
+{
+    const Quad Q = make_quad();
+    const long long quads = ((long long) gridDim.x * blockDim.x) >> 2;
+    for (long long k = ((long long) blockIdx.x * blockDim.x + threadIdx.x) >> 2; k < n; k += quads) {
+        const GasConst<double> c = make_gas_const<double>(gamma[k], tol);
+        const double *l = L + 4 * k, *r = R + 4 * k;
+        double o[3];
+        int code;
+        if (op == 5) {
+            double s[3];
+            code = quad_exact_solve(Q, c, l[0], l[1], l[3], r[0], r[1], r[3], aux[k], s);
+            o[0] = s[0] * s[1];
+            o[1] = s[0] * s[1] * s[1] + s[2];
+            o[2] = (s[2] * c.g_gm1 + 0.5 * s[0] * s[1] * s[1]) * s[1];
+        } else {
+            code = quad_exact_solve(Q, c, l[0], l[1], l[3], r[0], r[1], r[3], aux[k], o);
+        }
+        if (Q.q == 0) {
+            for (int q = 0; q < 3; q++) out[3 * k + q] = o[q];
+            rc[k] = code;
+        }
     }
 }
 
@@ -175,11 +205,11 @@ int hydro_gpu_pointwise_eval(int device, int op, long long n, const double *gamm
                              int *rc)
 {
     if (n <= 0) return 0;
-    if (op < 0 || op > 4) return (int) cudaErrorInvalidValue;
+    if (op < 0 || op > 6) return (int) cudaErrorInvalidValue;
     cudaError_t e = cudaSetDevice(device);
     if (e != cudaSuccess) return (int) e;
     const int width = (op == 0) ? 4 : (op == 1) ? 1 : 3;
-    const int naux = (op == 1) ? 2 : (op == 2 || op == 4) ? 1 : 0;
+    const int naux = (op == 1) ? 2 : (op == 2 || op >= 4) ? 1 : 0;
     const size_t nb = (size_t) n * sizeof(double);
     char *slab = nullptr;
     e = cudaMalloc(&slab, (9 + naux + width) * nb + (size_t) n * sizeof(int));
@@ -192,7 +222,8 @@ int hydro_gpu_pointwise_eval(int device, int op, long long n, const double *gamm
     if (e == cudaSuccess) e = cudaMemcpy(dr, R, 4 * nb, cudaMemcpyHostToDevice);
     if (e == cudaSuccess && naux) e = cudaMemcpy(da, aux, naux * nb, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) {
-        pointwise_kernel<<<152, 128>>>(op, n, dg, tol, dl, dr, da, dout, drc);
+        if (op >= 5) pointwise_quad_kernel<<<152, 128>>>(op, n, dg, tol, dl, dr, da, dout, drc);
+        else pointwise_kernel<<<152, 128>>>(op, n, dg, tol, dl, dr, da, dout, drc);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaMemcpy(out, dout, width * nb, cudaMemcpyDeviceToHost);

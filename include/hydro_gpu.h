@@ -376,6 +376,8 @@ void hydro_fx_quot_le_host(long long n, const double *x, const double *y, const 
  *   op 3: solve_flux_hllc_1d (src/riemann_solver_hllc.h:32-44): out[3k..3k+2]
  *   op 4: solve_exact_1d at speed aux[k] (src/riemann_solver_exact.h:37-51):
  *         the sampled (rho, u, p) in out[3k..3k+2]
+ *   op 5, 6: ops 2 and 4 computed as the 1D kernel computes them, four lanes
+ *         per state pair (quad_exact.cuh)
  * rc[k] = 0, or 1 (HLLC wave-speed error), 3 (exact solver: no bracket),
  * 4 (exact solver: bisection did not converge).  These are the functions the
  * step kernels call, compiled for the GPU, so the tests can check them

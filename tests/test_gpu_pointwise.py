@@ -83,6 +83,22 @@ def test_exact_solver_device_against_reference(gpu_available, golden, name, key)
     assert frac >= 0.95, frac
 
 
+@pytest.mark.parametrize("name,key", [("exact_flux_1d", "exact"), ("exact_1d", "exact_state")])
+def test_quad_exact_solver_is_the_single_lane_solver(gpu_available, golden, name, key):
+    """The 1D kernel's four-lane exact solver (quad_exact.cuh) against the
+    one-thread device build of exact_solve_1d on every golden state pair
+    (vacuum generation, TRRS, TSRS, fans, shocks, both sides of every wave):
+    the same bits, and the reference's answers within the exact tolerance."""
+    g = golden
+    m = len(g["speeds"])
+    one, rc1 = H.gpu_pointwise_eval(name, g["gamma"][:m], g["L"][:m], g["R"][:m], aux=g["speeds"])
+    four, rc4 = H.gpu_pointwise_eval(name + "_quad", g["gamma"][:m], g["L"][:m], g["R"][:m], aux=g["speeds"])
+    assert np.array_equal(rc1, rc4)
+    assert np.array_equal(one.view(np.uint64), four.view(np.uint64))
+    assert np.array_equal(rc4 == 0, g[key + "_rc"] == 0)
+    _compare(four, g[key], 1e-12)
+
+
 def test_pointwise_rejects_unknown_op(gpu_available):
     lib = H.library()
     one = np.ones(4)
