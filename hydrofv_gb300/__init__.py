@@ -436,9 +436,10 @@ def run_1d(nx: int, g: int, bounds, gamma: float, W: np.ndarray, U: np.ndarray,
            bc=("transmissive", "transmissive"), integrator="godunov_first_order_1d",
            riemann_solver="riemann_solver_exact", slope_limiter="minmod", cfl=0.9, tf=0.2,
            max_steps=-1, options: HydroGpuOptions | None = None,
-           coord_sys: str = "cartesian_1d") -> RunResult:
+           coord_sys: str = "cartesian_1d", storing: dict | None = None) -> RunResult:
     """Run a 1D problem (W, U: (3, nx+2g)) on a cartesian_1d, cylindrical_1d
-    or spherical_1d grid."""
+    or spherical_1d grid.  storing: {"interval", "output_dir",
+    "store_initial"} turns snapshots on, as for the 2D runs."""
     lib = library()
     h = _SystemHandle(lib, coord_sys, nx, 0, g, bounds, gamma)
     try:
@@ -450,6 +451,13 @@ def run_1d(nx: int, g: int, bounds, gamma: float, W: np.ndarray, U: np.ndarray,
         bcp, ip = _params(lib, list(bc) + [None, None], integrator, riemann_solver,
                           slope_limiter, cfl, keep)
         sp = lib.get_new_storing_param()
+        if storing:
+            sp.is_storing = True
+            sp.store_initial = bool(storing.get("store_initial", False))
+            sp.storing_interval = float(storing["interval"])
+            d = storing["output_dir"].encode()
+            keep.append(d)
+            sp.output_dir = d
         settings = Settings(0, True)
         simp = SimulationParam(tf)
         st = SimulationStatus(0, 0.0, 0.0)

@@ -79,3 +79,57 @@ def test_snapshot_write_error_is_reported(gpu_available, oracle_mod, tmp_path):
                      options=H.default_options(sync_snapshots=sync),
                      storing={"interval": 0.005, "output_dir": str(d) + "/", "store_initial": False})
         assert r.code != 0 and "snapshot" in r.message.lower()
+
+
+def read_bin_1d(path):
+    with open(path, "rb") as f:
+        raw = f.read()
+    assert raw[:8] == b"HYDROFV\0"
+    dim, nx, ny, g = np.frombuffer(raw, np.int32, 4, 8)
+    assert dim == 1
+    steps = int(np.frombuffer(raw, np.int64, 1, 24)[0])
+    t, dt = np.frombuffer(raw, np.float64, 2, 32)
+    W = np.frombuffer(raw, np.float64, 3 * (nx + 2 * g), 48).reshape(3, nx + 2 * g)
+    return steps, t, dt, W
+
+
+@pytest.mark.parametrize("integ,solver", [("godunov_first_order_1d", "riemann_solver_exact"),
+                                          ("muscl_hancock_1d", "riemann_solver_hllc")])
+def test_1d_snapshots_match_oracle(gpu_available, oracle_mod, tmp_path, integ, solver):
+    """1D runs stop the cluster kernel when a snapshot is due and relaunch it
+    after the host has stored it: every snapshot holds the oracle's state
+    after the same number of steps, and storing does not change the run."""
+    O = oracle_mod
+    p = O.sod_1d(200)
+    p.integrator, p.riemann_solver = integ, solver
+    tf, interval = 0.2, 0.05
+    out = str(tmp_path / "snaps")
+    os.makedirs(out)
+    args = dict(bc=p.bc, integrator=p.integrator, riemann_solver=p.riemann_solver,
+                slope_limiter=p.slope_limiter, cfl=p.cfl, tf=tf, max_steps=-1)
+    r = H.run_1d(p.nx, p.g, (p.x_min, p.x_max), p.gamma, p.W, p.U,
+                 storing={"interval": interval, "output_dir": out + "/", "store_initial": True}, **args)
+    plain = H.run_1d(p.nx, p.g, (p.x_min, p.x_max), p.gamma, p.W, p.U, **args)
+    assert r.code == 0 and plain.code == 0, (r.message, plain.message)
+    assert r.num_steps == plain.num_steps
+    assert np.array_equal(r.U, plain.U) and np.array_equal(r.W, plain.W)
+    files = sorted(os.listdir(out))
+    assert len(files) == 5          # initial + one per interval up to tf
+    orc = O.load("oracle")
+    seen = []
+    for f in files:
+        steps, t, dt, W = read_bin_1d(os.path.join(out, f))
+        seen.append(steps)
+        if steps == 0:
+            assert np.array_equal(W, p.W)
+            continue
+        q = p.copy()
+        if steps == r.num_steps:
+            q.max_steps, q.tf = -1, tf
+        else:
+            q.max_steps, q.tf = steps, 1e300
+        ref = orc.run_1d(q)
+        assert ref.num_steps == steps and ref.t == t
+        scale = np.max(np.abs(ref.W), axis=1, keepdims=True)
+        assert np.all(np.abs(W - ref.W) <= 1e-12 * scale)
+    assert seen == sorted(seen) and seen[-1] == r.num_steps
