@@ -420,7 +420,22 @@ __device__ __forceinline__ void mh2d_item(const Mh2dArgs<R> &a, Mh2dShared<R, NT
     __syncthreads();
 
     /* ---- march up the rows ---- */
+    /* FP32: the item's maxima of a + |u| and a + |v| in float (a maximum of
+     * floats is exact, and so is its conversion to double), merged into the
+     * double maxima once per item instead of converting every cell's */
+    float imx_x = -CUDART_INF_F, imx_y = -CUDART_INF_F;
     for (int r = r_begin; r < r_end; r++) {
+        /* FP32: this row's U is loaded before the face solve, which hides its
+         * latency (FP64 keeps those registers: its out-of-line divide, square
+         * root and pow calls would carry them) */
+        R upre[4];
+        if constexpr (sizeof(R) == 4) {
+            if (inner) {
+                const long long pidx = (long long) r * a.pitch + col;
+#pragma unroll
+                for (int q = 0; q < 4; q++) upre[q] = Uin[q][pidx];
+            }
+        }
         load_row(r + 2);
         if (tid == 0) { sm.nT = 0; sm.nS = 0; }
         __syncthreads();
@@ -466,7 +481,9 @@ __device__ __forceinline__ void mh2d_item(const Mh2dArgs<R> &a, Mh2dShared<R, NT
             R Un[4];
 #pragma unroll
             for (int q = 0; q < 4; q++) {
-                R v = Uin[q][idx];
+                R v;
+                if constexpr (sizeof(R) == 4) v = upre[q];
+                else v = Uin[q][idx];
                 if constexpr (sizeof(R) == 8) {
                     v = v + sm.FL[q][tid - 1];
                     v = v - sm.FL[q][tid];
@@ -500,10 +517,15 @@ __device__ __forceinline__ void mh2d_item(const Mh2dArgs<R> &a, Mh2dShared<R, NT
 #pragma unroll
             for (int q = 0; q < 4; q++) Wout[q][idx] = w[q];
             Wout[4][idx] = as;
-            const double sx = (double) (as + fabs(w[1]));
-            const double sy = (double) (as + fabs(w[2]));
-            if (sx > mx_x) mx_x = sx;
-            if (sy > mx_y) mx_y = sy;
+            const R sx = as + fabs(w[1]);
+            const R sy = as + fabs(w[2]);
+            if constexpr (sizeof(R) == 4) {
+                if (sx > imx_x) imx_x = sx;
+                if (sy > imx_y) imx_y = sy;
+            } else {
+                if (sx > mx_x) mx_x = sx;
+                if (sy > mx_y) mx_y = sy;
+            }
 
             /* first ghost row below / above the domain: one-sided update */
             if (r == g) {
@@ -533,6 +555,10 @@ __device__ __forceinline__ void mh2d_item(const Mh2dArgs<R> &a, Mh2dShared<R, NT
             for (int q = 0; q < 4; q++) Uout[q][gi] = Uin[q][gi] + upd(sm.FL[q][sw], Ax);
         }
         __syncthreads();
+    }
+    if constexpr (sizeof(R) == 4) {
+        if ((double) imx_x > mx_x) mx_x = (double) imx_x;
+        if ((double) imx_y > mx_y) mx_y = (double) imx_y;
     }
 }
 
