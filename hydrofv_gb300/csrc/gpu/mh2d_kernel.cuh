@@ -523,8 +523,10 @@ __device__ __forceinline__ void mh2d_item(const Mh2dArgs<R> &a, Mh2dShared<R, NT
                 if (sx > imx_x) imx_x = sx;
                 if (sy > imx_y) imx_y = sy;
             } else {
-                if (sx > mx_x) mx_x = sx;
-                if (sy > mx_y) mx_y = sy;
+                /* FP64: the compares on the bits (integer pipe; IEEE order, NaN
+                 * never larger, as with the FP64 compare) */
+                if (lt(mx_x, sx)) mx_x = sx;
+                if (lt(mx_y, sy)) mx_y = sy;
             }
 
             /* first ghost row below / above the domain: one-sided update */
