@@ -1,0 +1,65 @@
+"""bench.py's output line: the keys and types every run must print.
+
+The GPU arm runs a small grid on the GPU; the reference arm runs on the CPU
+(the CPU implementation of the path on a tiny grid).
+"""
+import json
+import os
+import subprocess
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+BASE_KEYS = {"metric": str, "value": float, "unit": str, "n_gpus": int, "steps": int, "warmup": int,
+             "ms_per_step": float, "higher_is_better": bool, "scaling": str, "dtype": str,
+             "data": str, "config": dict, "e2e": dict}
+
+
+def _run(args, tmp_path):
+    p = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py")] + args, cwd=str(tmp_path),
+                       stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True, timeout=900)
+    assert p.returncode == 0, p.stderr[-3000:]
+    lines = [l for l in p.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1, p.stdout
+    return json.loads(lines[0])
+
+
+def _check_base(d, steps, warmup):
+    for k, t in BASE_KEYS.items():
+        assert k in d, k
+        assert isinstance(d[k], t) or (t is float and isinstance(d[k], int)), (k, d[k])
+    assert "vs_baseline" in d and d["vs_baseline"] is None
+    assert d["steps"] == steps and d["warmup"] >= 3 and warmup >= 0
+    assert d["value"] > 0 and d["ms_per_step"] > 0
+    assert "workload" in d["config"]
+    e = d["e2e"]
+    for k in ("value", "unit", "h2d_bytes_per_step", "d2h_bytes_per_step"):
+        assert k in e, k
+
+
+def test_reference_arm_line(tmp_path):
+    d = _run(["--impl", "reference", "--size", "64", "--steps", "2", "--warmup", "1"], tmp_path)
+    _check_base(d, 2, 1)
+    assert d["impl"] == "reference"
+    cb = d["cpu_baseline"]
+    assert cb["kind"] in ("reference", "port") and cb["cores"] >= 1 and cb["value"] == d["value"]
+    assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["d2h_bytes_per_step"] == 0
+
+
+@pytest.mark.gpu
+def test_gpu_arm_line(gpu_available, tmp_path):
+    d = _run(["--size", "256", "--steps", "5", "--warmup", "3"], tmp_path)
+    _check_base(d, 5, 3)
+    r = d["roofline"]
+    for k in ("bound", "achieved", "peak", "unit", "frac", "traffic"):
+        assert k in r, k
+    assert r["bound"] in ("hbm", "tensor") and r["frac"] == pytest.approx(r["achieved"] / r["peak"])
+    assert d["gpu_launches"] > 0
+    c = d["clocks"]
+    assert {"sm_mhz", "sm_max_mhz", "reasons"} <= set(c)
+    cb = d["cpu_baseline"]
+    for k in ("value", "unit", "cores", "kind", "sample"):
+        assert k in cb, k
+    assert d["e2e"]["h2d_bytes_per_step"] > 0 and d["e2e"]["d2h_bytes_per_step"] > 0
