@@ -66,6 +66,23 @@ def test_bit_identical_to_the_oracle(gpu_available, oracle_mod, case):
     assert np.array_equal(gpu.W[:, g:-g, g:-g].view(np.uint64), ref.W[:, g:-g, g:-g].view(np.uint64))
 
 
+def test_headline_workload_bit_identical(gpu_available, oracle_mod):
+    """The benchmark workload itself -- the 2048 x 2048 shear layer, MC,
+    periodic, 200 steps -- through the drop-in call: the whole padded state,
+    the step count and the clock equal the oracle's bit for bit (the oracle
+    takes ~15 s on 16 host cores)."""
+    O = oracle_mod
+    p = O.shear_layer(2048, steps=200)
+    ref = O.load("oracle").run_2d(p)
+    gpu = run_gpu(p)
+    assert gpu.code == 0 and ref.rc == 0, gpu.message
+    assert gpu.num_steps == ref.num_steps == 200
+    assert gpu.t == ref.t and gpu.dt == ref.dt
+    g = p.g
+    assert np.array_equal(gpu.U[:, g:-g, g:-g].view(np.uint64), ref.U[:, g:-g, g:-g].view(np.uint64))
+    assert np.array_equal(gpu.W[:, g:-g, g:-g].view(np.uint64), ref.W[:, g:-g, g:-g].view(np.uint64))
+
+
 @pytest.mark.parametrize("bc", [("none",) * 4, ("reflective",) * 4, ("transmissive",) * 4,
                                 ("reflective", "transmissive", "periodic", "periodic"),
                                 ("transmissive", "none", "reflective", "transmissive")])
