@@ -6,6 +6,13 @@
 
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <functional>
+#include <map>
+#include <mutex>
+#include <tuple>
+#include <vector>
+
 #include "mh2d_kernel.cuh"
 
 /* Threads per 2D step CTA: a strip of MH2D_THREADS-2 interior columns. */
@@ -40,6 +47,85 @@ inline int mh2d_default_chunk(int nx, int ny, int strip_w, int slots)
         }
     }
     return best;
+}
+
+/*
+ * Guided row chunks: tall items first, short items last.  The step's work
+ * items go to the persistent CTAs in queue order, each CTA taking the next
+ * item when it is done.  Tall items pay their per-item prologue (about half
+ * a row: the rows below the chunk and its first y faces) less often; short
+ * items at the end of the queue keep the last round full.  This models the
+ * queue as greedy list scheduling of items costing (rows + 0.5) x (strip
+ * width + 2 halo columns) on `slots` equal workers, and picks the heights
+ * and the split with the smallest makespan (ties: fewer items).  tail_rows
+ * = 0 is one of the candidates: a single height.
+ */
+inline double mh2d_queue_makespan(int nx, int ny, int strip_w, int slots, int h1, int h2, int tail)
+{
+    std::vector<double> free_at((size_t) slots, 0.0);
+    std::make_heap(free_at.begin(), free_at.end(), std::greater<double>());
+    const int strips = (nx + strip_w - 1) / strip_w;
+    double makespan = 0.0;
+    auto chunk = [&](int rows) {
+        for (int s = 0; s < strips; s++) {
+            const int sw = (s + 1) * strip_w <= nx ? strip_w : nx - s * strip_w;
+            std::pop_heap(free_at.begin(), free_at.end(), std::greater<double>());
+            double &t = free_at.back();
+            t += (rows + 0.5) * (sw + 2) / (double) (strip_w + 2);
+            if (t > makespan) makespan = t;
+            std::push_heap(free_at.begin(), free_at.end(), std::greater<double>());
+        }
+    };
+    const int big = ny - tail;
+    for (int r = 0; r < big; r += h1) chunk(big - r < h1 ? big - r : h1);
+    for (int r = big; r < ny; r += h2) chunk(ny - r < h2 ? ny - r : h2);
+    return makespan;
+}
+
+inline void mh2d_guided_chunks(int nx, int ny, int strip_w, int slots, int &h1, int &h2, int &tail)
+{
+    /* 40 candidate queues besides the single height; one search per shape
+     * (about 4 ms at 2048^2 on one host core), then cached */
+    static const int tall[] = { 16, 24, 32, 48, 64 };
+    static const int short_h[] = { 4, 8 };
+    static const double waves[] = { 0.5, 1.0, 1.5, 2.0 };
+    static std::mutex cache_mutex;
+    static std::map<std::tuple<int, int, int, int>, std::tuple<int, int, int>> cache;
+    const auto key = std::make_tuple(nx, ny, strip_w, slots);
+    {
+        std::lock_guard<std::mutex> lock(cache_mutex);
+        const auto it = cache.find(key);
+        if (it != cache.end()) {
+            std::tie(h1, h2, tail) = it->second;
+            return;
+        }
+    }
+    h1 = mh2d_default_chunk(nx, ny, strip_w, slots);
+    h2 = h1;
+    tail = 0;
+    if (slots <= 0 || strip_w <= 0 || nx <= 0 || ny <= 0) return;
+    const int strips = (nx + strip_w - 1) / strip_w;
+    double best = mh2d_queue_makespan(nx, ny, strip_w, slots, h1, h1, 0);
+    for (int a : tall) {
+        for (int b : short_h) {
+            if (b >= a) continue;
+            for (double w : waves) {
+                /* enough short items for about w rounds of the persistent CTAs */
+                int t = (int) (w * slots / strips) * b;
+                t = ny - ((ny - t) / a) * a;                      /* tall part: whole chunks */
+                if (t <= 0 || t >= ny) continue;
+                const double m = mh2d_queue_makespan(nx, ny, strip_w, slots, a, b, t);
+                if (m < best * (1.0 - 1e-9)) {
+                    best = m;
+                    h1 = a;
+                    h2 = b;
+                    tail = t;
+                }
+            }
+        }
+    }
+    std::lock_guard<std::mutex> lock(cache_mutex);
+    cache[key] = std::make_tuple(h1, h2, tail);
 }
 
 template <class R>

@@ -58,7 +58,9 @@ struct Mh2dArgs {
     GasConst<R> gas;
     int nx, ny, g, pitch;
     int strip_w;             /* interior columns per strip (NT - 2) */
-    int chunk_h;             /* rows per CTA */
+    int chunk_h;             /* rows per work item */
+    int tail_h, tail_rows;   /* the last tail_rows rows go in items of tail_h rows, queued
+                              * after the others (0: every item has chunk_h rows) */
     int bc[4];               /* x_min, x_max, y_min, y_max */
     double dx, dy;           /* System.dx_, dy_ (for dt) */
     double area_x, area_y, vol;
@@ -68,6 +70,42 @@ struct Mh2dArgs {
     R *tape;                 /* adjoint tape of this step (kernels built with TAPE only) */
     long long tape_plane;    /* elements per tape field (padded cells) */
 };
+
+/* Work items of one step: (strip, row chunk) pairs, chunk-major, so the
+ * queue hands out all strips of a chunk before the next chunk.  Rows
+ * [0, ny - tail_rows) come in chunks of chunk_h rows, the rest in chunks of
+ * tail_h rows: the short items come last and fill the persistent CTAs' last
+ * round. */
+template <class R>
+__host__ __device__ inline int mh2d_n_items(const Mh2dArgs<R> &a)
+{
+    const int strips = (a.nx + a.strip_w - 1) / a.strip_w;
+    const int big = a.ny - a.tail_rows;
+    int chunks = (big + a.chunk_h - 1) / a.chunk_h;
+    if (a.tail_rows > 0) chunks += (a.tail_rows + a.tail_h - 1) / a.tail_h;
+    return strips * chunks;
+}
+
+/* Strip and padded row range [r0, r1) of work item `item`. */
+template <class R>
+__host__ __device__ inline void mh2d_item_rows(const Mh2dArgs<R> &a, int item, int &strip, int &r0, int &r1)
+{
+    const int strips = (a.nx + a.strip_w - 1) / a.strip_w;
+    strip = item % strips;
+    const int k = item / strips;
+    const int big = a.ny - a.tail_rows;
+    const int nbig = (big + a.chunk_h - 1) / a.chunk_h;
+    int lo, hi;
+    if (k < nbig) {
+        lo = k * a.chunk_h;
+        hi = (lo + a.chunk_h < big) ? lo + a.chunk_h : big;
+    } else {
+        lo = big + (k - nbig) * a.tail_h;
+        hi = (lo + a.tail_h < a.ny) ? lo + a.tail_h : a.ny;
+    }
+    r0 = a.g + lo;
+    r1 = a.g + hi;
+}
 
 /*
  * Adjoint tape of one step (written by the TAPE build of the step kernel,
@@ -313,14 +351,12 @@ __device__ __forceinline__ void mh2d_item(const Mh2dArgs<R> &a, Mh2dShared<R, NT
     const int tid = threadIdx.x;
     const int g = a.g, nx = a.nx, ny = a.ny;
     const int tx = nx + 2 * g, ty = ny + 2 * g;
-    const int n_strips = (nx + a.strip_w - 1) / a.strip_w;
     const int ymap[4] = { 0, 2, 1, 3 };   /* y fluxes come back as (mass, mom_y, mom_x, energy) */
 
-    const int strip = item % n_strips;
+    int strip, r_begin, r_end;
+    mh2d_item_rows(a, item, strip, r_begin, r_end);
     const int c0 = g + strip * a.strip_w;
     const int sw = min(a.strip_w, nx - strip * a.strip_w);
-    const int r_begin = g + (item / n_strips) * a.chunk_h;
-    const int r_end = min(r_begin + a.chunk_h, g + ny);
     const int col = c0 - 1 + tid;
     const bool x_slot = tid <= sw + 1;
     const bool inner = tid >= 1 && tid <= sw;
@@ -601,7 +637,7 @@ __global__ void __launch_bounds__(NT, (sizeof(R) == 4 ? 8 : 4)) mh2d_step_kernel
 
     __shared__ Mh2dShared<R, NT> sm;
     const int tid = threadIdx.x;
-    const int n_items = ((a.nx + a.strip_w - 1) / a.strip_w) * ((a.ny + a.chunk_h - 1) / a.chunk_h);
+    const int n_items = mh2d_n_items(a);
     double mx_x = -CUDART_INF, mx_y = -CUDART_INF;
     int err = DEV_OK;
 

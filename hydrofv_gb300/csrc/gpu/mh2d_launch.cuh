@@ -148,7 +148,7 @@ cudaError_t mh2d_step_occupancy(int *per_sm);
 template <class R>
 cudaError_t mh2d_launch_step(const Mh2dArgs<R> &a, int limiter, cudaStream_t s)
 {
-    const int n_items = ((a.nx + a.strip_w - 1) / a.strip_w) * ((a.ny + a.chunk_h - 1) / a.chunk_h);
+    const int n_items = mh2d_n_items(a);
     const int grid = (a.grid_ctas > 0 && a.grid_ctas < n_items) ? a.grid_ctas : n_items;
     if (a.first_order) return mh2d_launch_step_lim<R, LIM_MINMOD, 1>(a, grid, s);
     switch (limiter) {
@@ -162,7 +162,7 @@ cudaError_t mh2d_launch_step(const Mh2dArgs<R> &a, int limiter, cudaStream_t s)
 template <class R>
 cudaError_t mh2d_launch_step_tape(const Mh2dArgs<R> &a, int limiter, cudaStream_t s)
 {
-    const int n_items = ((a.nx + a.strip_w - 1) / a.strip_w) * ((a.ny + a.chunk_h - 1) / a.chunk_h);
+    const int n_items = mh2d_n_items(a);
     const int grid = (a.grid_ctas > 0 && a.grid_ctas < n_items) ? a.grid_ctas : n_items;
     switch (limiter) {
     case LIM_MINMOD: return mh2d_launch_tape_lim<R, LIM_MINMOD>(a, grid, s);

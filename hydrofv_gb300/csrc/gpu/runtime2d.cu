@@ -143,8 +143,17 @@ static void setup_args(HydroRun2D *run, Mh2dArgs<R> &a, const HydroGrid2D *grid,
     a.vol = grid->vol;
     a.first_order = (grid->integrator == INTEGRATOR_GODUNOV_FIRST_ORDER_2D) ? 1 : 0;
     a.grid_ctas = mh2d_resident_ctas<R>(grid->limiter, a.first_order, run->device);
-    a.chunk_h = opt->chunk_rows > 0 ? opt->chunk_rows
-                                    : mh2d_default_chunk(a.nx, a.ny, a.strip_w, a.grid_ctas);
+    /* FP64: guided row chunks (measured on the 2048^2 shear layer: 1287 M
+     * against 1257 M with one height).  FP32, at 8 CTAs per SM sharing an SM,
+     * does not fit the model's equal workers (10.8 G against 11.1 G): one
+     * height from the fill model. */
+    if (opt->chunk_rows > 0) {
+        a.chunk_h = opt->chunk_rows;
+    } else if (sizeof(R) == 8) {
+        mh2d_guided_chunks(a.nx, a.ny, a.strip_w, a.grid_ctas, a.chunk_h, a.tail_h, a.tail_rows);
+    } else {
+        a.chunk_h = mh2d_default_chunk(a.nx, a.ny, a.strip_w, a.grid_ctas);
+    }
     a.gravity = grid->gravity;
 }
 
@@ -356,6 +365,7 @@ std::map<std::tuple<int, int, int, int, int>, std::pair<int, int>> g_tune_cache;
 static void set_shape(HydroRun2D *run, int chunk, int ctas)
 {
     run->args.chunk_h = run->args32.chunk_h = chunk;
+    run->args.tail_rows = run->args32.tail_rows = 0;
     run->args.grid_ctas = run->args32.grid_ctas = ctas;
     if (run->graph) {
         cudaGraphExecDestroy(run->graph);
