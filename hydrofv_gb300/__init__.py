@@ -193,6 +193,7 @@ _SIGNATURES = {
                                            _dp, _P(C.c_int)]),
     "hydro_gpu_device_count": (C.c_int, []),
     "hydro_gpu_calibrate": (C.c_int, [C.c_int, _dp, _dp]),
+    "hydro_gpu_chunk_plan": (C.c_int, [C.c_int] * 4 + [_P(C.c_int)] * 4 + [C.c_int]),
     "hydro_gpu_version": (C.c_char_p, []),
     "free_traceback": (None, [_P(ErrorStatus)]),
     "solve_flux_hllc_2d": (ErrorStatus, [_dp] * 4 + [C.c_double] * 10),
@@ -854,6 +855,18 @@ def gpu_fx_eval(op, a, b=None, device=0):
     if rc != 0:
         raise HydroError(rc, "hydro_gpu_fx_eval failed (CUDA error)")
     return fast, hw, ok.astype(bool)
+
+
+def chunk_plan(nx, ny, g=2, slots=608):
+    """The FP64 step's work-item plan: ((h1, h2, tail), rows) with rows an
+    (n_items, 3) array of (strip, r0, r1) as the kernel decodes the items."""
+    lib = library()
+    h1, h2, tail = C.c_int(), C.c_int(), C.c_int()
+    n = lib.hydro_gpu_chunk_plan(nx, ny, g, slots, C.byref(h1), C.byref(h2), C.byref(tail), None, 0)
+    rows = np.zeros((n, 3), dtype=np.int32)
+    lib.hydro_gpu_chunk_plan(nx, ny, g, slots, C.byref(h1), C.byref(h2), C.byref(tail),
+                             rows.ctypes.data_as(_P(C.c_int)), n)
+    return (h1.value, h2.value, tail.value), rows
 
 
 def fx_ratio_below_host(x, y, tol):

@@ -163,6 +163,29 @@ static cudaError_t launch_step(HydroRun2D *run)
                      : mh2d_launch_step<double>(run->args, run->grid.limiter, run->stream);
 }
 
+/* The FP64 step's work-item plan for an nx x ny grid on `slots` resident CTAs
+ * (guided row chunks), and each item's strip and padded rows as the kernel
+ * decodes them (rows: 3 ints per item, or NULL).  Host only; for tests. */
+extern "C" int hydro_gpu_chunk_plan(int nx, int ny, int g, int slots, int *h1, int *h2, int *tail,
+                                    int *rows, int max_items)
+{
+    Mh2dArgs<double> a{};
+    a.nx = nx;
+    a.ny = ny;
+    a.g = g;
+    a.strip_w = MH2D_THREADS - 2;
+    mh2d_guided_chunks(nx, ny, a.strip_w, slots, a.chunk_h, a.tail_h, a.tail_rows);
+    *h1 = a.chunk_h;
+    *h2 = a.tail_h;
+    *tail = a.tail_rows;
+    const int n = mh2d_n_items(a);
+    if (rows) {
+        for (int i = 0; i < n && i < max_items; i++)
+            mh2d_item_rows(a, i, rows[3 * i], rows[3 * i + 1], rows[3 * i + 2]);
+    }
+    return n;
+}
+
 extern "C" int hydro_run2d_create(const HydroGrid2D *grid, const HydroGpuOptions *opt,
                                   HydroRun2D **out, HydroRunOutcome *oc)
 {

@@ -176,6 +176,14 @@ void hydro_gpu_batch_destroy(HydroGpuBatch *batch);
  * for roofline reporting.  Returns 0 on success. */
 int hydro_gpu_calibrate(int device, double *fp64_tflops, double *fp32_tflops);
 
+/* The FP64 step's work items for an nx x ny grid (g ghost layers) on `slots`
+ * resident CTAs: the guided row-chunk plan (h1-row items, then the last
+ * `tail` rows in h2-row items) and, if rows is not NULL, each item's strip
+ * and padded row range [r0, r1) as the kernel decodes it (3 ints per item,
+ * at most max_items).  Returns the number of items.  Host only. */
+int hydro_gpu_chunk_plan(int nx, int ny, int g, int slots, int *h1, int *h2, int *tail, int *rows,
+                         int max_items);
+
 /* ------------------------------------------------------------------ */
 /* Allocation-free run.  No counterpart in the reference.              */
 /* ------------------------------------------------------------------ */

@@ -259,3 +259,28 @@ def test_guess_p_divide_free_ratio_test_matches_reference(oracle_mod):
             ref = orc.guess_p(*args)
             got = lib.guess_p(*args)
             assert (ref == got) or (math.isnan(ref) and math.isnan(got)), (a, ref, got)
+
+
+@pytest.mark.parametrize("nx,ny", [(2048, 2048), (1024, 1024), (8192, 8192), (4096, 1000), (130, 7),
+                                   (3, 260), (1000, 4096), (256, 256)])
+@pytest.mark.parametrize("slots", [152, 608, 1216])
+def test_guided_chunk_plan_covers_every_row_once(hydro_lib, nx, ny, slots):
+    """The FP64 step's work items (guided row chunks: tall items first, the
+    last rows in short items) decoded as the kernel decodes them: every
+    interior row of every strip exactly once, the tall items before the
+    short ones."""
+    import hydrofv_gb300 as H
+    g = 2
+    (h1, h2, tail), rows = H.chunk_plan(nx, ny, g, slots)
+    strips = (nx + 125) // 126
+    assert 0 <= tail < ny and h1 >= 1 and (tail == 0 or 1 <= h2 <= h1)
+    seen = np.zeros((strips, ny), dtype=np.int32)
+    for strip, r0, r1 in rows:
+        assert 0 <= strip < strips and g <= r0 < r1 <= g + ny
+        seen[strip, r0 - g:r1 - g] += 1
+    assert np.all(seen == 1)
+    heights = rows[:, 2] - rows[:, 1]
+    big = rows[:, 1] < g + ny - tail
+    assert np.all(heights[big] <= h1) and np.all(heights[~big] <= max(h2, 1))
+    if tail:
+        assert np.all(np.diff(big.astype(int)) <= 0)      # tall items first
