@@ -1,11 +1,11 @@
-"""The FP32 state form against the FP64 drop-in (the benchmark spec precision form).
+"""The FP32 state form against the FP64 drop-in.
 
 FP32 state, fluxes and limiters; FP64 for the dt reduction, for pressure
 recovery where kinetic energy exceeds half of the total energy, and for
 the conserved totals.  Bars: relative L1 density error against the FP64
-path <= 1e-4 (the benchmark spec's threshold for the 8192^2 blast; here on small
-grids and short runs), and bounded drift of the compensated conserved
-totals.
+path <= 1e-4 (the bar the precision study holds the 8192^2 blast to; here
+on small grids and short runs), and bounded drift of the compensated
+conserved totals.
 """
 import numpy as np
 import pytest

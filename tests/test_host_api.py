@@ -42,7 +42,7 @@ def test_every_declared_function_is_exported(hydro_lib):
     exported = {line.split()[-1] for line in out.splitlines() if " T " in line}
     missing = sorted(declared_functions() - exported)
     assert not missing, missing
-    # the reference's public surface is all there
+    # the reference's public surface (src/hydro.h and the headers it includes) is all there
     for name in ["launch_simulation", "system_init", "free_system_memory",
                  "convert_conserved_to_primitive", "convert_primitive_to_conserved",
                  "finalize_boundary_condition_param", "set_boundary_condition",
