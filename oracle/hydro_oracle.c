@@ -927,6 +927,18 @@ int oracle_run_2d_ex(
     if (G.lim < 0) { set_err(errbuf, errlen, "Slope limiter not recognized."); return VALUE_ERROR; }
     for (int s = 0; s < 4; s++)
         if (G.bc[s] < 0) { set_err(errbuf, errlen, "Boundary condition not recognized."); return VALUE_ERROR; }
+    /* a periodic side needs a periodic opposite side: y pair, then x pair
+     * (src/boundary.c:258-305) */
+    if ((G.bc[2] == BC_PERIODIC || G.bc[3] == BC_PERIODIC) && G.bc[2] != G.bc[3])
+    {
+        set_err(errbuf, errlen, "Periodic boundary condition mismatch for y_min and y_max.");
+        return VALUE_ERROR;
+    }
+    if ((G.bc[0] == BC_PERIODIC || G.bc[1] == BC_PERIODIC) && G.bc[0] != G.bc[1])
+    {
+        set_err(errbuf, errlen, "Periodic boundary condition mismatch for x_min and x_max.");
+        return VALUE_ERROR;
+    }
     G.custom[0] = bc_fn_x_min; G.custom[1] = bc_fn_x_max;
     G.custom[2] = bc_fn_y_min; G.custom[3] = bc_fn_y_max;
     for (int s = 0; s < 4; s++)
@@ -1283,6 +1295,12 @@ int oracle_run_1d_ex(
     if (G.lim < 0) { set_err(errbuf, errlen, "Slope limiter not recognized."); return VALUE_ERROR; }
     G.bc[0] = parse_bc(bc_x_min); G.bc[1] = parse_bc(bc_x_max);
     if (G.bc[0] < 0 || G.bc[1] < 0) { set_err(errbuf, errlen, "Boundary condition not recognized."); return VALUE_ERROR; }
+    if ((G.bc[0] == BC_PERIODIC || G.bc[1] == BC_PERIODIC) && G.bc[0] != G.bc[1])
+    {
+        /* src/boundary.c:290-305 */
+        set_err(errbuf, errlen, "Periodic boundary condition mismatch for x_min and x_max.");
+        return VALUE_ERROR;
+    }
     const int tot = nx + 2 * g;
     double *geo = malloc(sizeof(double) * (size_t) (3 * tot + 1));
     if (!geo) { set_err(errbuf, errlen, "Memory allocation failed."); return MEMORY_ERROR; }

@@ -180,3 +180,42 @@ def test_sod_accuracy_against_reference_exact_solution(oracle_mod):
     rho = np.interp(x, ex["mid_points"], ex["density"])
     err = np.abs(g["W"][0, 2:-2] - rho).mean()
     assert err < 5e-3, err
+
+
+@pytest.mark.parametrize("bc,ok", [(("reflective", "periodic"), False), (("periodic", "transmissive"), False),
+                                   (("periodic", "periodic"), True)])
+def test_periodic_mismatch_rejected_like_the_reference_1d(oracle_mod, bc, ok):
+    """A periodic side needs a periodic opposite side (src/boundary.c:258-305):
+    the restatement returns the reference's error code and message, and
+    agrees with the compiled reference where it exists."""
+    O = oracle_mod
+    from hydrofv_gb300.problems import random_problem_1d
+    p = random_problem_1d(16, 3, bc, "godunov_first_order_1d", "riemann_solver_exact", "minmod", steps=2)
+    for b in [O.load("oracle")] + ([O.load("ref_serial")] if O.reference_available() else []):
+        r = b.run_1d(p)
+        if ok:
+            assert r.rc == 0, r.message
+        else:
+            assert r.rc == 2 and "Periodic boundary condition mismatch for x_min and x_max" in r.message
+
+
+@pytest.mark.parametrize("bc,which", [(("transmissive", "periodic", "periodic", "periodic"), "x_min and x_max"),
+                                      (("periodic", "periodic", "reflective", "periodic"), "y_min and y_max"),
+                                      (("reflective", "periodic", "none", "periodic"), "y_min and y_max"),
+                                      (("periodic",) * 4, None)])
+def test_periodic_mismatch_rejected_like_the_reference_2d(oracle_mod, bc, which):
+    O = oracle_mod
+    from hydrofv_gb300.problems import random_problem_2d
+    p = random_problem_2d(12, 10, 3, bc, "minmod", 2)
+    for b in [O.load("oracle")] + ([O.load("ref")] if O.reference_available() else []):
+        r = b.run_2d(p)
+        if which is None:
+            assert r.rc == 0, r.message
+        else:
+            assert r.rc == 2 and f"Periodic boundary condition mismatch for {which}" in r.message, r.message
+    if which is not None:
+        # the library rejects it on the host, before any GPU work
+        import hydrofv_gb300 as H
+        r = H.run_2d(p.nx, p.ny, p.g, (p.x_min, p.x_max, p.y_min, p.y_max), p.gamma, p.W, p.U, bc=p.bc,
+                     slope_limiter=p.slope_limiter, max_steps=2)
+        assert r.code == 2 and f"Periodic boundary condition mismatch for {which}" in r.message
