@@ -51,3 +51,26 @@ def test_example_fails_loudly_without_a_gpu(tmp_path, hydro_lib):
                        text=True, timeout=120)
     assert p.returncode != 0
     assert "launch_simulation" in p.stdout and "CUDA error" in p.stdout, p.stdout[-2000:]
+
+
+@pytest.mark.skipif(shutil.which("cmake") is None, reason="cmake not available")
+def test_example_builds_with_its_own_cmake(tmp_path, hydro_lib):
+    """The route of the examples' own CMakeLists.txt (add_subdirectory of
+    ../../src, target_link_libraries(... hydro)) with ../../src reaching
+    include/ through a symbolic link: the unmodified file configures, builds
+    and links libhydro_gb300.so."""
+    import hydrofv_gb300 as H
+    src = [s for s in SOURCES if s.endswith("sod_shock_1d.c")]
+    if not src:
+        pytest.skip("sod_shock_1d not in the reference examples")
+    ex = tmp_path / "examples" / "sod_shock_1d"
+    shutil.copytree(os.path.dirname(src[0]), ex)
+    os.symlink(os.path.join(ROOT, "include"), tmp_path / "src")
+    build = tmp_path / "build"
+    for cmd in (["cmake", "-S", str(ex), "-B", str(build)], ["cmake", "--build", str(build)]):
+        p = subprocess.run(cmd, stdout=subprocess.PIPE, stderr=subprocess.STDOUT, text=True, timeout=600)
+        assert p.returncode == 0, p.stdout[-3000:]
+    exe = build / "sod_shock_1d"
+    assert exe.exists()
+    ldd = subprocess.run(["ldd", str(exe)], stdout=subprocess.PIPE, text=True).stdout
+    assert os.path.basename(H.LIB_PATH) in ldd
