@@ -24,6 +24,14 @@
 
 #include "numerics.cuh"
 
+/* `#pragma unroll` for the device compiler only (the host compiler builds
+ * these functions too, and does not know the pragma) */
+#if defined(__CUDA_ARCH__)
+#define HYDRO_UNROLL _Pragma("unroll")
+#else
+#define HYDRO_UNROLL
+#endif
+
 namespace hydro {
 
 /* ---------------------------------------------------------------- limiter */
@@ -555,7 +563,7 @@ HD void recon_cell(int dir, R dtA, const R wm[4], const R w0[4], const R wp[4], 
 {
     R d[4];
     if (dir == 0) {
-#pragma unroll
+HYDRO_UNROLL
         for (int q = 0; q < 4; q++) d[q] = limit_slope<LIM>(w0[q] - wm[q], wp[q] - w0[q]);
         hancock_2d(dtA, dv(dtA, w0[0]), w0[0], w0[1], w0[2], w0[3], a0, d, d[1], lo, hi);
     } else {
@@ -573,7 +581,7 @@ template <int LIM>
 HD int recon_code(const double wm[4], const double w0[4], const double wp[4])
 {
     int code = 0;
-#pragma unroll
+HYDRO_UNROLL
     for (int q = 0; q < 4; q++) {
         double da, db;
         int c;
@@ -598,7 +606,7 @@ HD void recon_cell_vjp(int dir, double dtA, const double wm[4], const double w0[
 {
     double pa[4], pb[4], d[4];
     int code;
-#pragma unroll
+HYDRO_UNROLL
     for (int q = 0; q < 4; q++) d[q] = limit_slope_partials<LIM>(w0[q] - wm[q], wp[q] - w0[q], pa[q], pb[q], code);
     const int in_ = (dir == 0) ? 1 : 2;    /* storage index of the normal velocity */
     const int it_ = (dir == 0) ? 2 : 1;    /* storage index of the tangential velocity */
@@ -625,7 +633,7 @@ HD void recon_cell_vjp(int dir, double dtA, const double wm[4], const double w0[
     const double h = 0.5 * ab * a0;
     own[0] -= h * inv_rho;
     own[3] += h * inv_p;
-#pragma unroll
+HYDRO_UNROLL
     for (int q = 0; q < 4; q++) {
         A[q] = db[q] * pa[q];
         B[q] = db[q] * pb[q];
@@ -656,7 +664,7 @@ HD void recon_cell_forced(int dir, double dtA, const double wm[4], const double 
                           double a0, int code, double lo[4], double hi[4])
 {
     double d[4];
-#pragma unroll
+HYDRO_UNROLL
     for (int q = 0; q < 4; q++) d[q] = limit_slope_forced<LIM>(w0[q] - wm[q], wp[q] - w0[q], (code >> (2 * q)) & 3);
     if (dir == 0) {
         hancock_2d(dtA, dv(dtA, w0[0]), w0[0], w0[1], w0[2], w0[3], a0, d, d[1], lo, hi);

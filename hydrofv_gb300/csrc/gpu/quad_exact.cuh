@@ -60,7 +60,6 @@ static __device__ void quad_fdf(const Quad &Q, const GasConst<double> &c, const 
 {
     const int side = Q.q & 1;
     const bool d = Q.q >= 2;
-    const double rho = side ? S.rho_R : S.rho_L;
     const double p = side ? S.p_R : S.p_L;
     const double a = side ? S.a_R : S.a_L;
     double x, r = 0.0;

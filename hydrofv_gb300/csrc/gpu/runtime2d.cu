@@ -19,7 +19,6 @@
  */
 #include <cuda_runtime.h>
 
-#include <chrono>
 #include <climits>
 #include <cmath>
 #include <cstdio>
@@ -55,12 +54,6 @@ void set_cuda_error(HydroRunOutcome *oc, cudaError_t e, const char *what)
             return -1;                                  \
         }                                               \
     } while (0)
-
-double now_ms()
-{
-    using namespace std::chrono;
-    return duration<double, std::milli>(steady_clock::now().time_since_epoch()).count();
-}
 
 }  // namespace
 
