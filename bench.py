@@ -39,6 +39,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 import numpy as np
@@ -61,19 +62,35 @@ def peaks() -> dict:
     return {"hbm_gbs": 6800.0, "source": "fallback"}
 
 
-def profile_traffic() -> float | None:
-    """DRAM bytes per step launch from the committed ncu summary, scaled to 2048^2."""
-    path = os.path.join(ROOT, "profiles", "mh2d_fp64_traffic.json")
+def profile_traffic(precision: str = "fp64") -> float | None:
+    """DRAM bytes per step launch at 2048^2 from the committed ncu capture
+    (profiles/mh2d_fp64_traffic.json; the FP32 form's in mh2d_fp32_counts.json)."""
+    if precision == "fp64":
+        path = os.path.join(ROOT, "profiles", "mh2d_fp64_traffic.json")
+        key = "dram_bytes_per_launch_2048"
+    else:
+        path = os.path.join(ROOT, "profiles", "mh2d_fp32_counts.json")
+        key = "dram_bytes_per_launch"
     if not os.path.exists(path):
         return None
     with open(path) as f:
         d = json.load(f)
-    return float(d["dram_bytes_per_launch_2048"])
+    return float(d[key]) if key in d else None
 
 
-def profile_fp64_counts() -> dict | None:
-    """FP64 instructions per cell-update of the step kernel (committed ncu counts)."""
-    path = os.path.join(ROOT, "profiles", "mh2d_fp64_counts.json")
+def hbm_roofline(value: float, bytes_per_cell: int, pk: dict, traffic: float | None) -> dict:
+    """The step against measured HBM bandwidth: algorithmic bytes (4 conserved
+    fields read and written per cell-update) per second."""
+    achieved = bytes_per_cell * value / 1e9
+    return {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
+            "frac": achieved / pk["hbm_gbs"], "traffic": traffic, "peak_source": pk["source"],
+            "bytes_per_cell_update": bytes_per_cell}
+
+
+def profile_counts(precision: str) -> dict | None:
+    """FP-pipe instructions per cell-update of the step kernel (committed ncu
+    counts of one launch: profiles/mh2d_fp64_counts.json, mh2d_fp32_counts.json)."""
+    path = os.path.join(ROOT, "profiles", f"mh2d_{precision}_counts.json")
     if not os.path.exists(path):
         return None
     with open(path) as f:
@@ -91,11 +108,10 @@ class ClockSampler:
         self.device = device
         self.proc = None
         self.fh = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_bench_{os.getpid()}.csv")
+        self.path = os.path.join(tempfile.gettempdir(), f"hydro_bench_clocks_{os.getpid()}_{id(self)}.csv")
 
     def __enter__(self):
         try:
-            os.makedirs(os.path.dirname(self.path), exist_ok=True)
             self.fh = open(self.path, "w")
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
@@ -116,6 +132,13 @@ class ClockSampler:
             self.fh.close()
 
     def summary(self) -> dict:
+        try:
+            return self._summary()
+        finally:
+            if os.path.exists(self.path):
+                os.remove(self.path)
+
+    def _summary(self) -> dict:
         if self.proc is None or not os.path.exists(self.path):
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
         sm, smax, reasons = [], [], set()
@@ -184,24 +207,87 @@ def cpu_sample(steps_hint: int, budget_s: float = 12.0) -> dict:
             "seconds": r.seconds, "steps": n}
 
 
-def fp_roofline(prec, value, fp64_tflops, fp32_tflops, H) -> dict:
-    """The binding roof of the FP64 step: its FP64 pipe.  achieved = FP64 warp
-    instructions issued per second (ncu count per cell-update x measured
-    cell-updates/s); peak = the measured FMA rate of hydro_gpu_calibrate as
-    warp instructions per second (every FP64 instruction takes one pipe slot
-    per lane)."""
-    out = {"bound": "fp64_pipe" if prec == H.PRECISION_FP64 else "fp32_pipe",
-           "peak_tflops_fp64": fp64_tflops, "peak_tflops_fp32": fp32_tflops}
-    counts = profile_fp64_counts()
-    if prec == H.PRECISION_FP64 and counts and N_SIDE == 2048:
-        per_cell = counts["fp64_warp_inst_per_cell_update"]
+def fp_roofline(prec, value, fp64_tflops, fp32_tflops, H, workload="shear_layer") -> dict:
+    """The arithmetic roof of the step kernel: its FP64 pipe (FP64 form) or
+    its FP32 pipe (FP32 form).  achieved = FP warp instructions issued per
+    second (ncu count per cell-update x measured cell-updates/s); peak = the
+    FMA rate hydro_gpu_calibrate measures in the same run, as warp
+    instructions per second (one FP64 or FP32 warp instruction takes one pipe
+    slot per lane).  The FP64 pipe binds the FP64 form; the FP32 form is
+    latency-bound below its FP32 roof (issue_active_pct)."""
+    fp64 = prec == H.PRECISION_FP64
+    name = "fp64" if fp64 else "fp32"
+    out = {"bound": f"{name}_pipe", "peak_tflops_fp64": fp64_tflops, "peak_tflops_fp32": fp32_tflops}
+    counts = profile_counts(name)
+    if counts and workload == "shear_layer" and N_SIDE == 2048:
+        per_cell = counts[f"{name}_warp_inst_per_cell_update"]
         achieved = value * per_cell
-        peak = fp64_tflops * 1e12 / 2 / 32
-        out.update({"achieved": achieved, "peak": peak, "unit": "FP64 warp instructions/s",
+        peak = (fp64_tflops if fp64 else fp32_tflops) * 1e12 / 2 / 32
+        out.update({"achieved": achieved, "peak": peak, "unit": f"{name.upper()} warp instructions/s",
                     "frac": achieved / peak, "of": "measured (hydro_gpu_calibrate)",
-                    "fp64_warp_inst_per_cell_update": per_cell,
-                    "fp64_thread_inst_per_cell_update": counts["fp64_thread_inst_per_cell_update"],
+                    f"{name}_warp_inst_per_cell_update": per_cell,
+                    f"{name}_thread_inst_per_cell_update": counts[f"{name}_thread_inst_per_cell_update"],
+                    "issue_active_pct": counts.get("issue_active_pct"),
                     "counts_source": counts["source"]})
+    return out
+
+
+def shear_config(args, ws: int) -> dict:
+    """config of the headline line; the reference arm prints the same dict."""
+    return {"workload": WORKLOAD, "grid": [N_SIDE, N_SIDE], "ghost_cells": 2,
+            "limiter": "monotonized_central", "cfl": 0.8, "boundaries": "periodic",
+            "steps_per_run": args.steps,
+            "l2": "state larger than the 129 MB L2 (no flush needed)" if N_SIDE * N_SIDE >= 1 << 20
+                  else "state fits in L2 (profiling size)",
+            "parallelism": "replicas" if ws > 1 else "single"}
+
+
+BLAST_SIDE = 8192
+
+
+def blast_leg(args, H, device: int, ws: int) -> dict:
+    """The precision study's grid: the 8192^2 point blast (Van Leer,
+    reflective, CFL 0.4), FP64 and FP32 over the line's K steps from the
+    initial condition (W warm-up steps and a rewind first), CUDA-event time
+    of the stepping; relative L1 error of the FP32 state against the FP64
+    state per field, and the conserved-total drift of both."""
+    from hydrofv_gb300.problems import point_blast
+    p = point_blast(BLAST_SIDE, steps=args.steps)
+    cells = p.nx * p.ny
+    out, finals = {}, {}
+    for name, prec in (("fp64", H.PRECISION_FP64), ("fp32", H.PRECISION_FP32)):
+        with H.Solver2D(p.nx, p.ny, p.g, (p.x_min, p.x_max, p.y_min, p.y_max), p.gamma, p.W, p.U,
+                        bc=p.bc, slope_limiter=p.slope_limiter, cfl=p.cfl,
+                        options=H.default_options(device=device, precision=prec)) as s:
+            s.advance(args.warmup)
+            s.restart()
+            tot0 = s.conserved_totals()
+            l0 = s.kernel_launches()
+            barrier(ws)
+            clk = ClockSampler(device)
+            with clk:
+                st, ms = s.advance(args.steps)
+            launches = s.kernel_launches() - l0
+            assert st.num_steps == args.steps, st.num_steps
+            tot1 = s.conserved_totals()
+            finals[name] = s.download()[0]
+        ms = max_over_ranks(ms, ws)
+        drift = (tot1 - tot0) / np.where(tot0 != 0, np.abs(tot0), 1.0)
+        out[name] = {"value": ws * cells * args.steps / (ms * 1e-3), "ms_per_step": ms / args.steps,
+                     "gpu_launches": int(launches), "clocks": clk.summary(),
+                     "conserved_drift": {"mass": float(drift[0]), "energy": float(drift[3])}}
+    g = p.g
+    W64, W32 = finals["fp64"], finals["fp32"]
+    num = np.abs(W32[:, g:-g, g:-g] - W64[:, g:-g, g:-g]).sum(axis=(1, 2))
+    den = np.abs(W64[:, g:-g, g:-g]).sum(axis=(1, 2))
+    l1 = num / den
+    out["fp32"]["speedup_vs_fp64"] = out["fp32"]["value"] / out["fp64"]["value"]
+    out["fp32"]["rel_l1_vs_fp64"] = {"density": float(l1[0]), "velocity_x": float(l1[1]),
+                                     "velocity_y": float(l1[2]), "pressure": float(l1[3])}
+    out["config"] = {"workload": f"point_blast_{BLAST_SIDE}x{BLAST_SIDE}_muscl_hancock_hllc_vl",
+                     "grid": [BLAST_SIDE, BLAST_SIDE], "ghost_cells": p.g, "limiter": p.slope_limiter,
+                     "cfl": p.cfl, "boundaries": p.bc[0], "steps_per_run": args.steps,
+                     "l2": "state larger than the 129 MB L2 (no flush needed)"}
     return out
 
 
@@ -216,8 +302,8 @@ def run_reference_arm(args) -> None:
     kind = "reference" if O.reference_available() else "port"
     backend = O.load("ref" if kind == "reference" else "oracle")
     threads = O.load("oracle").lib.oracle_num_threads()
-    # warm-up: W steps (bounded), then K timed steps from the initial condition
-    warm = O.shear_layer(N_SIDE, steps=min(args.warmup, 3))
+    # warm-up: W steps, then K timed steps from the initial condition
+    warm = O.shear_layer(N_SIDE, steps=args.warmup)
     backend.run_2d(warm)
     p = O.shear_layer(N_SIDE, steps=args.steps)
     r = backend.run_2d(p)
@@ -227,8 +313,7 @@ def run_reference_arm(args) -> None:
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": r.seconds * 1e3 / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "grid": [N_SIDE, N_SIDE], "ghost_cells": 2,
-                   "steps_per_run": args.steps},
+        "config": shear_config(args, ws),
         "cpu_baseline": {"value": value, "unit": "cell-updates/s", "cores": int(threads),
                          "kind": kind,
                          "sample": f"{args.steps} steps of the {N_SIDE}x{N_SIDE} shear layer, "
@@ -536,6 +621,8 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-blast", action="store_true",
+                    help="leave out the 8192^2 point-blast leg of the default line (profiling runs)")
     ap.add_argument("--size", type=int, default=N_SIDE,
                     help="grid side (the headline workload is 2048; smaller sizes are for profiling)")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"],
@@ -650,6 +737,11 @@ def main() -> None:
     e2e_s = max_over_ranks(e2e_s, ws)
     e2e_value = ws * cells * args.steps / e2e_s
 
+    # ---- the precision study's grid beside the headline: 8192^2 point blast ----
+    blast = None
+    if args.workload == "shear_layer" and not args.no_blast:
+        blast = blast_leg(args, H, device, ws)
+
     if rank != 0:
         return
 
@@ -667,8 +759,8 @@ def main() -> None:
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if prec == H.PRECISION_FP64 else "f32",
         "data": f"synthetic (seeded {args.workload})",
-        "config": {"workload": WORKLOAD if args.workload == "shear_layer" and prec == H.PRECISION_FP64
-                   else f"{args.workload}_{N_SIDE}x{N_SIDE}_{args.precision}",
+        "config": shear_config(args, ws) if args.workload == "shear_layer" and prec == H.PRECISION_FP64 else
+                  {"workload": f"{args.workload}_{N_SIDE}x{N_SIDE}_{args.precision}",
                    "grid": [N_SIDE, N_SIDE], "ghost_cells": 2,
                    "limiter": p.slope_limiter, "cfl": p.cfl, "boundaries": p.bc[0],
                    "steps_per_run": args.steps,
@@ -681,7 +773,7 @@ def main() -> None:
                      "bytes_per_cell_update": bytes_per_cell,
                      "note": "HBM is not the binding roof of this stencil: the step is bound by "
                              "its FP64 (FP32) pipe, reported in fp_roofline"},
-        "fp_roofline": fp_roofline(prec, value, fp64_tflops, fp32_tflops, H),
+        "fp_roofline": fp_roofline(prec, value, fp64_tflops, fp32_tflops, H, args.workload),
         "forms": {
             "fp64": {"value": cells * args.steps / (fp64_ms * 1e-3), "ms_per_step": fp64_ms / args.steps,
                      "conserved_drift": drift_main if prec == H.PRECISION_FP64 else drift_o},
@@ -689,7 +781,12 @@ def main() -> None:
                      "speedup_vs_fp64": fp64_ms / fp32_ms,
                      "rel_l1_vs_fp64": {"density": l1[0], "velocity_x": l1[1],
                                         "velocity_y": l1[2], "pressure": l1[3]},
-                     "conserved_drift": drift_main if prec == H.PRECISION_FP32 else drift_o},
+                     "conserved_drift": drift_main if prec == H.PRECISION_FP32 else drift_o,
+                     "fp_roofline": fp_roofline(H.PRECISION_FP32, cells * args.steps / (fp32_ms * 1e-3),
+                                                fp64_tflops, fp32_tflops, H, args.workload),
+                     "roofline": hbm_roofline(cells * args.steps / (fp32_ms * 1e-3), BYTES_PER_CELL_FP64 // 2,
+                                              pk, profile_traffic("fp32") if args.workload == "shear_layer"
+                                              and N_SIDE == 2048 else None)},
         },
         "e2e": {"value": e2e_value, "unit": "cell-updates/s",
                 "h2d_bytes_per_step": e2e_stats["h2d_bytes"] / args.steps,
@@ -700,6 +797,8 @@ def main() -> None:
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
     }
+    if blast is not None:
+        line["forms"]["point_blast_8192"] = blast
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_sample(args.steps)
     print(json.dumps(line))

@@ -132,6 +132,8 @@ _SIGNATURES = {
     "set_boundary_condition": (ErrorStatus, [_P(BoundaryConditionParam), _P(System)]),
     "convert_primitive_to_conserved": (ErrorStatus, [_P(System)]),
     "convert_conserved_to_primitive": (ErrorStatus, [_P(System)]),
+    "add_geometry_source_term": (ErrorStatus, [_P(BoundaryConditionParam), _P(System), C.c_double]),
+    "add_gravity_source_term_2d": (ErrorStatus, [_P(BoundaryConditionParam), _P(System), C.c_double]),
     "get_new_integrator_param": (IntegratorParam, []),
     "finalize_integrator_param": (ErrorStatus, [_P(IntegratorParam)]),
     "get_new_storing_param": (StoringParam, []),

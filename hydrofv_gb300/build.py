@@ -38,6 +38,7 @@ CUDA_SOURCES = [
     ("gpu/runtime2d.cu", []),
     ("gpu/runtime_batch.cu", []),
     ("gpu/host_numerics.cu", ["--fmad=false"]),
+    ("gpu/source_term_host.cu", ["--fmad=false"]),
     ("gpu/calibrate.cu", []),
     ("gpu/noalloc2d.cu", []),
     ("gpu/run1d.cu", ["--fmad=false"]),
@@ -53,7 +54,6 @@ C_SOURCES = [
     "host/utils.c",
     "host/storing.c",
     "host/progress_bar.c",
-    "host/source_term.c",
     "host/integrate_gpu.c",
 ]
 

@@ -536,14 +536,7 @@ __device__ __forceinline__ void mh2d_item(const Mh2dArgs<R> &a, Mh2dShared<R, NT
             }
             if constexpr (GRAV) {
                 /* gravity source, RK4 on energy (src/source_term.c:185-240) */
-                const R pf = (R) (-dt * a.gravity);
-                const R km = pf * Un[0];
-                const R k1 = pf * Un[2];
-                const R k2 = pf * (Un[2] + R(0.5) * km);
-                const R k3 = k2;
-                const R k4 = pf * (Un[2] + km);
-                Un[2] = Un[2] + km;
-                Un[3] = Un[3] + dv(k1 + R(2) * k2 + R(2) * k3 + k4, R(6));
+                gravity_kick((R) (-dt * a.gravity), Un[0], Un[2], Un[3]);
 #pragma unroll
                 for (int q = 0; q < 4; q++) Uout[q][idx] = Un[q];
             }

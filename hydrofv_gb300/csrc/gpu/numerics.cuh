@@ -841,6 +841,60 @@ HD double from_ordered_bits(unsigned long long e)
     return x;
 }
 
+/* ---------------------------------------------------------------------- */
+/* Source terms (src/source_term.c).  One cell's update each, shared by    */
+/* the step kernels and the exported host functions.                       */
+/* ---------------------------------------------------------------------- */
+
+/* Rates of the cylindrical / spherical geometry source for density rho,
+ * momentum density sm and energy density se; pf = -alpha V / r
+ * (src/source_term.c:32-43). */
+template <class R>
+HD void geometry_rates(R pf, R gm1, R rho, R sm, R se, R &dm, R &dmom, R &de)
+{
+    const R p = gm1 * (se - dv(R(0.5) * sm * sm, rho));
+    dm = pf * sm;
+    dmom = dv(pf * sm * sm, rho);
+    de = dv(pf * sm * (se + p), rho);
+}
+
+/* RK4 step of the geometry source on one cell's totals (m, mom, E) with
+ * volume vol and density rho (src/source_term.c:91-165); pf as above. */
+template <class R>
+HD void geometry_source_rk4(R pf, R gm1, R vol, R dt, R rho, R &m, R &mom, R &E)
+{
+    R k1m, k1p, k1e, k2m, k2p, k2e, k3m, k3p, k3e, k4m, k4p, k4e;
+    geometry_rates(pf, gm1, rho, dv(mom, vol), dv(E, vol), k1m, k1p, k1e);
+    R tm = m + R(0.5) * dt * k1m, tp = mom + R(0.5) * dt * k1p, te = E + R(0.5) * dt * k1e;
+    geometry_rates(pf, gm1, dv(tm, vol), dv(tp, vol), dv(te, vol), k2m, k2p, k2e);
+    tm = m + R(0.5) * dt * k2m;
+    tp = mom + R(0.5) * dt * k2p;
+    te = E + R(0.5) * dt * k2e;
+    geometry_rates(pf, gm1, dv(tm, vol), dv(tp, vol), dv(te, vol), k3m, k3p, k3e);
+    tm = m + dt * k3m;
+    tp = mom + dt * k3p;
+    te = E + dt * k3e;
+    geometry_rates(pf, gm1, dv(tm, vol), dv(tp, vol), dv(te, vol), k4m, k4p, k4e);
+    m = m + dv(dt * (k1m + R(2) * k2m + R(2) * k3m + k4m), R(6));
+    mom = mom + dv(dt * (k1p + R(2) * k2p + R(2) * k3p + k4p), R(6));
+    E = E + dv(dt * (k1e + R(2) * k2e + R(2) * k3e + k4e), R(6));
+}
+
+/* The gravity kick on one cell's totals with pf = -dt g: the momentum
+ * change pf m is exact (the mass does not change), the energy takes the RK4
+ * sum (src/source_term.c:213-236). */
+template <class R>
+HD void gravity_kick(R pf, R mass, R &mom_y, R &E)
+{
+    const R km = pf * mass;
+    const R k1 = pf * mom_y;
+    const R k2 = pf * (mom_y + R(0.5) * km);
+    const R k3 = k2;
+    const R k4 = pf * (mom_y + km);
+    mom_y = mom_y + km;
+    E = E + dv(k1 + R(2) * k2 + R(2) * k3 + k4, R(6));
+}
+
 }  // namespace hydro
 
 #endif

@@ -106,16 +106,6 @@ __device__ double van_der_corput(long long n)
     return result;
 }
 
-/* src/source_term.c:25-39 */
-__device__ __forceinline__ void geometry_rates(double pf, double gm1, double rho, double sm, double se,
-                                               double &dm, double &dmom, double &de)
-{
-    const double p = gm1 * (se - dv(0.5 * sm * sm, rho));
-    dm = pf * sm;
-    dmom = dv(pf * sm * sm, rho);
-    de = dv(pf * sm * (se + p), rho);
-}
-
 /* The cluster's threads: a global index and count for the cell and face loops. */
 struct Lanes {
     int gt, GT;
@@ -449,22 +439,11 @@ __global__ void __launch_bounds__(kThreads) run1d_kernel(const Run1dArgs a)
             for (int i = g + L.gt; i < g + n; i += L.GT) {
                 const double vol = a.vol[i];
                 const double m = U[0][i], mom = U[1][i], E = U[2][i], rho = W[0][i];
-                const double pf = dv(-a.alpha * vol, a.mid[i]);
-                double k1m, k1p, k1e, k2m, k2p, k2e, k3m, k3p, k3e, k4m, k4p, k4e;
-                geometry_rates(pf, gm1, rho, dv(mom, vol), dv(E, vol), k1m, k1p, k1e);
-                double tm = m + 0.5 * dt * k1m, tp = mom + 0.5 * dt * k1p, te = E + 0.5 * dt * k1e;
-                geometry_rates(pf, gm1, dv(tm, vol), dv(tp, vol), dv(te, vol), k2m, k2p, k2e);
-                tm = m + 0.5 * dt * k2m;
-                tp = mom + 0.5 * dt * k2p;
-                te = E + 0.5 * dt * k2e;
-                geometry_rates(pf, gm1, dv(tm, vol), dv(tp, vol), dv(te, vol), k3m, k3p, k3e);
-                tm = m + dt * k3m;
-                tp = mom + dt * k3p;
-                te = E + dt * k3e;
-                geometry_rates(pf, gm1, dv(tm, vol), dv(tp, vol), dv(te, vol), k4m, k4p, k4e);
-                U[0][i] = m + dv(dt * (k1m + 2.0 * k2m + 2.0 * k3m + k4m), 6.0);
-                U[1][i] = mom + dv(dt * (k1p + 2.0 * k2p + 2.0 * k3p + k4p), 6.0);
-                U[2][i] = E + dv(dt * (k1e + 2.0 * k2e + 2.0 * k3e + k4e), 6.0);
+                double mm = m, mp = mom, me = E;
+                geometry_source_rk4(dv(-a.alpha * vol, a.mid[i]), gm1, vol, dt, rho, mm, mp, me);
+                U[0][i] = mm;
+                U[1][i] = mp;
+                U[2][i] = me;
             }
             cl.sync();
             convert_all(a, U, W, ntot, L);

@@ -28,6 +28,9 @@
 
 enum { OK = 0, FAILURE = 1, VALUE_ERROR = 2, POINTER_ERROR = 3, MEMORY_ERROR = 4,
        NOT_IMPLEMENTED_ERROR = 6 };
+/* Internal codes of the exact solver's two failures; public_code() and
+ * solver_message() turn them into the reference's code and message. */
+enum { ERR_EXACT_BRACKET = 101, ERR_EXACT_BISECTION = 102 };
 enum { LIM_MINMOD = 1, LIM_VAN_LEER = 2, LIM_MC = 3 };
 enum { BC_NONE = 1, BC_REFLECTIVE = 2, BC_TRANSMISSIVE = 3, BC_PERIODIC = 4, BC_CUSTOM = 5 };
 enum { SOLVER_EXACT = 1, SOLVER_HLLC = 2 };
@@ -39,6 +42,23 @@ enum { SOLVER_EXACT = 1, SOLVER_HLLC = 2 };
 static void set_err(char *buf, int len, const char *msg)
 {
     if (buf && len > 0) snprintf(buf, (size_t) len, "%s", msg);
+}
+
+/* The reference's return code for a solver failure: both exact-solver
+ * failures raise FAILURE (src/riemann_solver_exact.c:702-707, :745-754), the
+ * HLLC failure VALUE_ERROR (src/riemann_solver_hllc.c:372-375). */
+static int public_code(int rc)
+{
+    return (rc == ERR_EXACT_BRACKET || rc == ERR_EXACT_BISECTION) ? FAILURE : rc;
+}
+
+/* The reference's message for a failed Riemann solve. */
+static const char *solver_message(int rc)
+{
+    if (rc == ERR_EXACT_BRACKET) return "Failed to bracket the root for bisection method.";
+    if (rc == ERR_EXACT_BISECTION)
+        return "Bisection method did not converge after 5001 iterations for exact riemann solver.";
+    return "Invalid wave speed for the HLLC riemann solver. Possible fix: use a smaller CFL.";
 }
 
 /* ---------------------------------------------------------------- numerics */
@@ -398,7 +418,7 @@ static int exact_p_star(double gamma, double rho_L, double u_L, double p_L, doub
                     break;
                 }
             }
-            if (f_lo * f_hi >= 0.0) return FAILURE;
+            if (f_lo * f_hi >= 0.0) return ERR_EXACT_BRACKET;
         }
     }
     int count = 0;
@@ -414,7 +434,7 @@ static int exact_p_star(double gamma, double rho_L, double u_L, double p_L, doub
         if (fm * f_lo < 0.0) { p_hi = pm; f_hi = fm; }
         else { p_lo = pm; f_lo = fm; }
         count++;
-        if (count > BISECTION_MAX_ITER) return FAILURE;
+        if (count > BISECTION_MAX_ITER) return ERR_EXACT_BISECTION;
     }
 }
 
@@ -1331,13 +1351,72 @@ int oracle_run_1d_ex(
                 boundary_1d(&G);
             }
         }
-        if (rc != OK) { set_err(errbuf, errlen, "Riemann solver failed."); status = rc; break; }
+        if (rc != OK) { set_err(errbuf, errlen, solver_message(rc)); status = public_code(rc); break; }
         geometry_source_1d(&G, step);
         *t += step;
         (*num_steps)++;
     }
     free(geo);
     return status;
+}
+
+/* ------------------------------------------------- source-term exports */
+
+/* add_geometry_source_term (src/source_term.c:45-183) on a cylindrical_1d
+ * (coord 2) or spherical_1d (coord 3) grid: W and U padded, in place;
+ * transmissive / reflective / periodic sides as in the 1D runs. */
+int oracle_geometry_source_1d(int coord, int nx, int g, double x_min, double x_max, double gamma,
+                              double dt, const char *bc_x_min, const char *bc_x_max,
+                              double *rho, double *u, double *p,
+                              double *mass, double *mom_x, double *energy)
+{
+    if (coord != 2 && coord != 3) return VALUE_ERROR;
+    Grid1 G;
+    G.nx = nx; G.g = g; G.gamma = gamma;
+    G.dx = (x_max - x_min) / (nx + 2 * g);
+    G.tol = 1e-6;
+    G.alpha = (coord == 2) ? 1.0 : 2.0;
+    G.lim = LIM_MINMOD;
+    G.solver = SOLVER_EXACT;
+    G.bc[0] = parse_bc(bc_x_min); G.bc[1] = parse_bc(bc_x_max);
+    if (G.bc[0] < 0 || G.bc[1] < 0) return VALUE_ERROR;
+    const int tot = nx + 2 * g;
+    double *geo = malloc(sizeof(double) * (size_t) (3 * tot + 1));
+    if (!geo) return MEMORY_ERROR;
+    G.A = geo; G.V = geo + tot + 1; G.X = geo + 2 * tot + 1;
+    geometry_1d(&G, x_min, coord);
+    G.W[0] = rho; G.W[1] = u; G.W[2] = p;
+    G.U[0] = mass; G.U[1] = mom_x; G.U[2] = energy;
+    geometry_source_1d(&G, dt);
+    free(geo);
+    return OK;
+}
+
+/* add_gravity_source_term_2d (src/source_term.c:185-259) on a Cartesian 2D
+ * grid with built-in sides: W and U padded, in place. */
+int oracle_gravity_source_2d(int nx, int ny, int g, double x_min, double x_max, double y_min,
+                             double y_max, double gamma, double gravity, double dt,
+                             const char *bc_x_min, const char *bc_x_max, const char *bc_y_min,
+                             const char *bc_y_max,
+                             double *rho, double *u, double *v, double *p,
+                             double *mass, double *mom_x, double *mom_y, double *energy)
+{
+    Grid G;
+    memset(&G, 0, sizeof G);
+    G.nx = nx; G.ny = ny; G.g = g; G.tx = nx + 2 * g;
+    G.gamma = gamma;
+    G.dx = (x_max - x_min) / (nx + 2 * g);
+    G.dy = (y_max - y_min) / (ny + 2 * g);
+    G.A_x = G.dy; G.A_y = G.dx; G.vol = G.dx * G.dy;
+    G.bc[0] = parse_bc(bc_x_min); G.bc[1] = parse_bc(bc_x_max);
+    G.bc[2] = parse_bc(bc_y_min); G.bc[3] = parse_bc(bc_y_max);
+    for (int s = 0; s < 4; s++)
+        if (G.bc[s] < 0 || G.bc[s] == BC_CUSTOM) return VALUE_ERROR;
+    G.gravity = gravity;
+    G.W[0] = rho; G.W[1] = u; G.W[2] = v; G.W[3] = p;
+    G.U[0] = mass; G.U[1] = mom_x; G.U[2] = mom_y; G.U[3] = energy;
+    gravity_2d(&G, dt);
+    return OK;
 }
 
 /* ------------------------------------------------------- pointwise exports */
@@ -1352,7 +1431,7 @@ int oracle_exact_flux_1d(double gamma, double rho_L, double u_L, double p_L,
                          double rho_R, double u_R, double p_R, double tol, double speed,
                          double *out3)
 {
-    return exact_flux_1d(gamma, rho_L, u_L, p_L, rho_R, u_R, p_R, tol, speed, out3);
+    return public_code(exact_flux_1d(gamma, rho_L, u_L, p_L, rho_R, u_R, p_R, tol, speed, out3));
 }
 
 int oracle_hllc_1d(double gamma, double rho_L, double u_L, double p_L,
@@ -1366,7 +1445,19 @@ int oracle_hllc_1d(double gamma, double rho_L, double u_L, double p_L,
 int oracle_exact_1d(double gamma, double rho_L, double u_L, double p_L,
                     double rho_R, double u_R, double p_R, double tol, double speed, double *out3)
 {
-    return exact_state_1d(gamma, rho_L, u_L, p_L, rho_R, u_R, p_R, tol, speed, out3);
+    return public_code(exact_state_1d(gamma, rho_L, u_L, p_L, rho_R, u_R, p_R, tol, speed, out3));
+}
+
+/* Which way solve_exact_1d ends: 0 solved, 1 "Failed to bracket the root"
+ * (src/riemann_solver_exact.c:702-707), 2 bisection not converged
+ * (:745-754); the message for the last two is copied into errbuf. */
+int oracle_exact_status(double gamma, double rho_L, double u_L, double p_L,
+                        double rho_R, double u_R, double p_R, double tol, char *errbuf, int errlen)
+{
+    double out3[3];
+    const int rc = exact_state_1d(gamma, rho_L, u_L, p_L, rho_R, u_R, p_R, tol, 0.0, out3);
+    set_err(errbuf, errlen, rc == OK ? "" : solver_message(rc));
+    return rc == ERR_EXACT_BRACKET ? 1 : rc == ERR_EXACT_BISECTION ? 2 : 0;
 }
 
 double oracle_guess_p(double gamma, double rho_L, double u_L, double p_L, double a_L,

@@ -75,6 +75,23 @@ int oracle_exact_1d(double gamma, double rho_L, double u_L, double p_L,
 double oracle_guess_p(double gamma, double rho_L, double u_L, double p_L, double a_L,
                       double rho_R, double u_R, double p_R, double a_R, double tol);
 int oracle_limit_slope(int limiter_flag, double a, double b, double *out);
+/* 0 solved, 1 bracket failure, 2 bisection not converged (message in errbuf). */
+int oracle_exact_status(double gamma, double rho_L, double u_L, double p_L,
+                        double rho_R, double u_R, double p_R, double tol, char *errbuf, int errlen);
+
+/* The source terms on their own (src/source_term.c:45-259): the RK4 update,
+ * then U -> W and the ghost fill, in place on padded arrays.  coord: 2
+ * cylindrical_1d, 3 spherical_1d. */
+int oracle_geometry_source_1d(int coord, int nx, int g, double x_min, double x_max, double gamma,
+                              double dt, const char *bc_x_min, const char *bc_x_max,
+                              double *rho, double *u, double *p,
+                              double *mass, double *mom_x, double *energy);
+int oracle_gravity_source_2d(int nx, int ny, int g, double x_min, double x_max, double y_min,
+                             double y_max, double gamma, double gravity, double dt,
+                             const char *bc_x_min, const char *bc_x_max, const char *bc_y_min,
+                             const char *bc_y_max,
+                             double *rho, double *u, double *v, double *p,
+                             double *mass, double *mom_x, double *mom_y, double *energy);
 
 /* Number of OpenMP threads the 2D loops use (for the CPU-baseline report). */
 int oracle_num_threads(void);

@@ -33,14 +33,25 @@ _dp = C.POINTER(C.c_double)
 _i64p = C.POINTER(C.c_longlong)
 
 
+# The reference's sources as `make stage` copies them (git-ignored; present
+# wherever the reference tree was, or wherever the working tree was carried).
+REF_SRC = os.path.join(REFDIR, "src")
+REF_EXAMPLES = os.path.join(REFDIR, "examples")
+
+
 def build(with_reference: bool | None = None) -> None:
-    """Compile the restatement (and the reference, when its tree exists)."""
+    """Compile the restatement, stage the reference's sources where its tree
+    exists, and compile the reference from the staged copy when there is one.
+    HYDRO_REF_ROOT names another reference tree to stage from."""
     subprocess.run(["make", "-s", "-C", HERE], check=True)
-    ref_src = os.environ.get("HYDRO_REF_SRC", "/root/reference/src")
+    stage = ["make", "-s", "-C", HERE, "stage"]
+    if os.environ.get("HYDRO_REF_ROOT"):
+        stage.append("REF_ROOT=" + os.environ["HYDRO_REF_ROOT"])
+    subprocess.run(stage, check=True)
     if with_reference is None:
-        with_reference = os.path.isdir(ref_src)
+        with_reference = os.path.isdir(REF_SRC)
     if with_reference:
-        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={ref_src}"], check=True)
+        subprocess.run(["make", "-s", "-C", HERE, "ref"], check=True)
 
 
 _libs: dict[str, C.CDLL] = {}
@@ -85,6 +96,15 @@ def _bind(lib: C.CDLL, prefix: str) -> C.CDLL:
     f = getattr(lib, prefix + "limit_slope")
     f.restype = C.c_int
     f.argtypes = [C.c_int, C.c_double, C.c_double, _dp]
+    f = getattr(lib, prefix + "geometry_source_1d")
+    f.restype = C.c_int
+    f.argtypes = [C.c_int] * 3 + [C.c_double] * 4 + [C.c_char_p] * 2 + [_dp] * 6
+    f = getattr(lib, prefix + "gravity_source_2d")
+    f.restype = C.c_int
+    f.argtypes = [C.c_int] * 3 + [C.c_double] * 7 + [C.c_char_p] * 4 + [_dp] * 8
+    f = getattr(lib, prefix + "exact_status")
+    f.restype = C.c_int
+    f.argtypes = [C.c_double] * 8 + [C.c_char_p, C.c_int]
     return lib
 
 
@@ -192,6 +212,33 @@ class Backend:
         out = np.zeros(3)
         rc = getattr(self.lib, self.prefix + "exact_1d")(gamma, *L, *R, tol, speed, _ptr(out))
         return rc, out
+
+    def exact_status(self, gamma, L, R, tol=1e-6):
+        """How solve_exact_1d ends: (0 solved | 1 bracket failure | 2 bisection
+        not converged, message)."""
+        err = C.create_string_buffer(4096)
+        kind = getattr(self.lib, self.prefix + "exact_status")(gamma, *L, *R, tol, err, len(err))
+        return kind, err.value.decode(errors="replace")
+
+    def geometry_source_1d(self, prob: Problem1D, W: np.ndarray, U: np.ndarray, dt: float):
+        """add_geometry_source_term on copies of (W, U): (rc, W, U)."""
+        W = np.ascontiguousarray(W, dtype=np.float64).copy()
+        U = np.ascontiguousarray(U, dtype=np.float64).copy()
+        coord = {"cylindrical_1d": 2, "spherical_1d": 3}[prob.coord_sys]
+        rc = getattr(self.lib, self.prefix + "geometry_source_1d")(
+            coord, prob.nx, prob.g, prob.x_min, prob.x_max, prob.gamma, dt,
+            prob.bc[0].encode(), prob.bc[1].encode(), *[_ptr(a) for a in W], *[_ptr(a) for a in U])
+        return rc, W, U
+
+    def gravity_source_2d(self, prob: Problem2D, W: np.ndarray, U: np.ndarray, dt: float):
+        """add_gravity_source_term_2d on copies of (W, U): (rc, W, U)."""
+        W = np.ascontiguousarray(W, dtype=np.float64).copy()
+        U = np.ascontiguousarray(U, dtype=np.float64).copy()
+        rc = getattr(self.lib, self.prefix + "gravity_source_2d")(
+            prob.nx, prob.ny, prob.g, prob.x_min, prob.x_max, prob.y_min, prob.y_max, prob.gamma,
+            float(prob.gravity), dt, *[b.encode() for b in prob.bc],
+            *[_ptr(a) for a in W], *[_ptr(a) for a in U])
+        return rc, W, U
 
     def guess_p(self, gamma, rho_L, u_L, p_L, a_L, rho_R, u_R, p_R, a_R, tol=1e-6):
         return getattr(self.lib, self.prefix + "guess_p")(

@@ -20,6 +20,7 @@
 #include <string.h>
 
 #include "hydro.h"
+#include "source_term.h"
 
 static long long g_stop_after_steps = -1;
 
@@ -69,12 +70,10 @@ static int finish(ErrorStatus e, char *errbuf, int errlen, int fixed_stop)
             snprintf(errbuf, (size_t) errlen, "%s", e.traceback);
         }
     }
+    /* the step-count sentinel is the one FAILURE without a traceback */
+    const int sentinel = fixed_stop && e.return_code == FAILURE && !e.traceback;
     free_traceback(&e);
-    if (fixed_stop && e.return_code == FAILURE && !e.traceback)
-    {
-        return 0;
-    }
-    return e.return_code;
+    return sentinel ? 0 : e.return_code;
 }
 
 /*
@@ -326,6 +325,95 @@ int ref_exact_1d(double gamma, double rho_L, double u_L, double p_L,
     int rc = e.return_code;
     free_traceback(&e);
     return rc;
+}
+
+/* solve_exact_1d's way out, as oracle_exact_status: 0 solved, 1 bracket
+ * failure, 2 bisection not converged, told apart by the reference's own
+ * traceback text, which is copied into errbuf. */
+int ref_exact_status(double gamma, double rho_L, double u_L, double p_L,
+                     double rho_R, double u_R, double p_R, double tol, char *errbuf, int errlen)
+{
+    double out3[3];
+    ErrorStatus e = solve_exact_1d(&out3[0], &out3[1], &out3[2], gamma,
+                                   rho_L, u_L, p_L, rho_R, u_R, p_R, tol, 0.0, 0);
+    int kind = 0;
+    if (errbuf && errlen > 0) errbuf[0] = '\0';
+    if (e.return_code != SUCCESS)
+    {
+        kind = (e.traceback && strstr(e.traceback, "Failed to bracket")) ? 1 : 2;
+        if (errbuf && errlen > 0 && e.traceback) snprintf(errbuf, (size_t) errlen, "%s", e.traceback);
+    }
+    free_traceback(&e);
+    return kind;
+}
+
+/* The reference's own add_geometry_source_term / add_gravity_source_term_2d
+ * on a System set up by its system_init, arrays copied in and out (same
+ * argument order as the oracle's source-term exports). */
+int ref_geometry_source_1d(int coord, int nx, int g, double x_min, double x_max, double gamma,
+                           double dt, const char *bc_x_min, const char *bc_x_max,
+                           double *rho, double *u, double *p,
+                           double *mass, double *mom_x, double *energy)
+{
+    System system = get_new_system_struct();
+    system.coord_sys = (coord == 2) ? "cylindrical_1d" : "spherical_1d";
+    system.gamma = gamma;
+    system.x_min = x_min;
+    system.x_max = x_max;
+    system.num_cells_x = nx;
+    system.num_ghost_cells_side = g;
+    ErrorStatus e = system_init(&system);
+    if (e.return_code != SUCCESS) return finish(e, NULL, 0, 0);
+    const size_t n = (size_t) (nx + 2 * g);
+    double *fields[6] = { system.density_, system.velocity_x_, system.pressure_,
+                          system.mass_, system.momentum_x_, system.energy_ };
+    double *arrays[6] = { rho, u, p, mass, mom_x, energy };
+    for (int q = 0; q < 6; q++) memcpy(fields[q], arrays[q], n * sizeof(double));
+    BoundaryConditionParam bcp = get_new_boundary_condition_param();
+    bcp.boundary_condition_x_min = bc_x_min;
+    bcp.boundary_condition_x_max = bc_x_max;
+    e = finalize_boundary_condition_param(&system, &bcp);
+    if (e.return_code == SUCCESS) e = add_geometry_source_term(&bcp, &system, dt);
+    for (int q = 0; q < 6; q++) memcpy(arrays[q], fields[q], n * sizeof(double));
+    free_system_memory(&system);
+    return finish(e, NULL, 0, 0);
+}
+
+int ref_gravity_source_2d(int nx, int ny, int g, double x_min, double x_max, double y_min,
+                          double y_max, double gamma, double gravity, double dt,
+                          const char *bc_x_min, const char *bc_x_max, const char *bc_y_min,
+                          const char *bc_y_max,
+                          double *rho, double *u, double *v, double *p,
+                          double *mass, double *mom_x, double *mom_y, double *energy)
+{
+    System system = get_new_system_struct();
+    system.coord_sys = "cartesian_2d";
+    system.gamma = gamma;
+    system.x_min = x_min;
+    system.x_max = x_max;
+    system.y_min = y_min;
+    system.y_max = y_max;
+    system.num_cells_x = nx;
+    system.num_cells_y = ny;
+    system.num_ghost_cells_side = g;
+    system.gravity = gravity;
+    ErrorStatus e = system_init(&system);
+    if (e.return_code != SUCCESS) return finish(e, NULL, 0, 0);
+    const size_t n = (size_t) (nx + 2 * g) * (size_t) (ny + 2 * g);
+    double *fields[8] = { system.density_, system.velocity_x_, system.velocity_y_, system.pressure_,
+                          system.mass_, system.momentum_x_, system.momentum_y_, system.energy_ };
+    double *arrays[8] = { rho, u, v, p, mass, mom_x, mom_y, energy };
+    for (int q = 0; q < 8; q++) memcpy(fields[q], arrays[q], n * sizeof(double));
+    BoundaryConditionParam bcp = get_new_boundary_condition_param();
+    bcp.boundary_condition_x_min = bc_x_min;
+    bcp.boundary_condition_x_max = bc_x_max;
+    bcp.boundary_condition_y_min = bc_y_min;
+    bcp.boundary_condition_y_max = bc_y_max;
+    e = finalize_boundary_condition_param(&system, &bcp);
+    if (e.return_code == SUCCESS) e = add_gravity_source_term_2d(&bcp, &system, dt);
+    for (int q = 0; q < 8; q++) memcpy(arrays[q], fields[q], n * sizeof(double));
+    free_system_memory(&system);
+    return finish(e, NULL, 0, 0);
 }
 
 double ref_guess_p(double gamma, double rho_L, double u_L, double p_L, double a_L,

@@ -63,3 +63,15 @@ def test_gpu_arm_line(gpu_available, tmp_path):
     for k in ("value", "unit", "cores", "kind", "sample"):
         assert k in cb, k
     assert d["e2e"]["h2d_bytes_per_step"] > 0 and d["e2e"]["d2h_bytes_per_step"] > 0
+    # both forms carry their arithmetic and HBM roofs; the precision study's
+    # 8192^2 point blast rides along on the default workload
+    forms = d["forms"]
+    assert forms["fp32"]["roofline"]["bound"] == "hbm"
+    assert "bound" in forms["fp32"]["fp_roofline"]
+    blast = forms["point_blast_8192"]
+    assert blast["fp64"]["value"] > 0 and blast["fp32"]["value"] > 0
+    assert set(blast["fp32"]["rel_l1_vs_fp64"]) == {"density", "velocity_x", "velocity_y", "pressure"}
+    assert blast["fp32"]["rel_l1_vs_fp64"]["density"] < 1e-4
+    # the reference arm reports the same workload under the same config
+    r = _run(["--impl", "reference", "--size", "256", "--steps", "5", "--warmup", "3"], tmp_path)
+    assert r["config"] == d["config"] and r["warmup"] == d["warmup"] and r["steps"] == d["steps"]

@@ -11,6 +11,7 @@ import ctypes as C
 import os
 import re
 import subprocess
+import sys
 
 import numpy as np
 import pytest
@@ -19,7 +20,10 @@ import hydrofv_gb300 as H
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 INCLUDE = os.path.join(ROOT, "include")
-REF_SRC = "/root/reference/src"
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+import oracle as O  # noqa: E402
+
+REF_SRC = O.REF_SRC   # the reference's headers, staged by `make -C oracle stage`
 
 
 def declared_functions():

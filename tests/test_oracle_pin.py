@@ -8,8 +8,8 @@
 * The library's exported pointwise numerics (host builds of the kernels'
   templates) are checked against the same golden pointwise vectors.
 * Sod at t = 0.2 is checked for accuracy against the exact solution the
-  reference ships (examples/sod_shock_1d/sol_cartesian_1d_0.2.npz) when the
-  reference tree is present.
+  reference ships (examples/sod_shock_1d/sol_cartesian_1d_0.2.npz) where
+  the reference tree was staged (oracle/_ref/examples).
 """
 import ctypes as C
 import hashlib
@@ -167,7 +167,10 @@ def test_library_pointwise_exports_match_golden(hydro_lib):
         assert bits_equal(np.array(got), g["limited"][f - 1])
 
 
-SOD_EXACT = "/root/reference/examples/sod_shock_1d/sol_cartesian_1d_0.2.npz"
+import oracle as _O  # noqa: E402
+
+# the exact Sod solution the reference ships, in the staged copy of its tree
+SOD_EXACT = os.path.join(_O.REF_EXAMPLES, "sod_shock_1d", "sol_cartesian_1d_0.2.npz")
 
 
 @pytest.mark.skipif(not os.path.exists(SOD_EXACT), reason="reference tree not present")

@@ -5,18 +5,23 @@ include/ and linked to libhydro_gb300.so (the reference links the same
 sources to its `hydro` target, examples/*/CMakeLists.txt:14-23).  On a
 machine without a GPU the program must fail loudly inside launch_simulation
 with the CUDA error, in the reference's traceback format: there is no CPU
-fallback.  The programs are read from the reference tree, so the test skips
-where that tree is absent.
+fallback.  The programs are read from the staged copy of the reference tree
+(oracle/_ref/examples, made by `make -C oracle stage`), so the test skips
+where there is none.
 """
 import glob
 import os
 import shutil
 import subprocess
+import sys
 
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-EXAMPLES = os.environ.get("HYDRO_REF_EXAMPLES", "/root/reference/examples")
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+import oracle as O  # noqa: E402
+
+EXAMPLES = O.REF_EXAMPLES
 SOURCES = sorted(glob.glob(os.path.join(EXAMPLES, "*", "*.c")))
 
 pytestmark = pytest.mark.skipif(not SOURCES or shutil.which("gcc") is None,

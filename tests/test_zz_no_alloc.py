@@ -7,8 +7,13 @@ in a static array shared by every call.  This test drives it through the C
 ABI on consecutive calls with different grids -- so a call starts from
 whatever the previous one left in the array -- and checks each result
 against hydro_gpu_launch_simulation on the same input, with the tolerance
-the other parity tests use.  It also checks that an oversized grid is
-refused with a clear error.
+the other parity tests use, over both limiters' code paths and the
+boundary kinds the entry point parses itself (including periodic sides).
+A run that ends in a device error (an unstable CFL number) must return the
+same code, message, status and state as the regular entry point.  Around
+repeated calls the device's free memory must not move: the entry point
+allocates nothing.  It also checks that an oversized grid is refused with a
+clear error.
 
 Collected last on purpose (file name), so a run that stops at the first
 failure has already run every other test.
@@ -59,6 +64,16 @@ def run_noalloc(p):
         h.close()
 
 
+def device_free_bytes():
+    """Free device memory as the driver reports it, for the context that the
+    library's calls made current on this thread."""
+    cuda = C.CDLL("libcuda.so.1")
+    free, total = C.c_size_t(0), C.c_size_t(0)
+    rc = cuda.cuMemGetInfo_v2(C.byref(free), C.byref(total))
+    assert rc == 0, f"cuMemGetInfo_v2 returned {rc}"
+    return free.value
+
+
 def run_regular(p):
     return H.run_2d(p.nx, p.ny, p.g, (p.x_min, p.x_max, p.y_min, p.y_max), p.gamma, p.W, p.U,
                     bc=p.bc, integrator=p.integrator, riemann_solver=p.riemann_solver,
@@ -70,13 +85,18 @@ def rel_l1(a, b, g):
     return np.abs(ia - ib).sum(axis=(1, 2)) / np.abs(ib).sum(axis=(1, 2))
 
 
-def test_noalloc_matches_regular_entry_point_on_consecutive_calls(gpu_available):
-    problems = [
+def consecutive_problems():
+    return [
         shear_layer(96, steps=30),
         random_problem_2d(150, 100, 5, ("reflective", "transmissive", "none", "reflective"),
                           "van_leer", 25, smooth=True),
+        random_problem_2d(120, 90, 3, ("periodic",) * 4, "minmod", 20, smooth=True),
         shear_layer(96, steps=30),
     ]
+
+
+def test_noalloc_matches_regular_entry_point_on_consecutive_calls(gpu_available):
+    problems = consecutive_problems()
     for p in problems:
         assert (p.nx + 2 * p.g) * (p.ny + 2 * p.g) <= MAX_CELLS
         rc, msg, W, U, st = run_noalloc(p)
@@ -96,3 +116,41 @@ def test_noalloc_rejects_grids_above_the_limit(gpu_available):
     assert rc == 2  # VALUE_ERROR
     assert "exceeds the no-allocation limit" in msg
     assert st.num_steps == 0
+
+
+def test_noalloc_device_error_matches_regular_entry_point(gpu_available):
+    """An unstable CFL number drives the point blast into HLLC's invalid wave
+    speed at step 21: the code, the reference's message, the status and the
+    state at the start of the failing step agree with the regular entry
+    point, and a following call on the same array runs cleanly."""
+    from hydrofv_gb300.problems import point_blast
+    p = point_blast(32, steps=80)
+    p.cfl = 2.0
+    rc, msg, W, U, st = run_noalloc(p)
+    ref = run_regular(p)
+    assert ref.code == 2 and rc == 2, (ref.code, rc, msg)
+    assert "Invalid wave speed for the HLLC riemann solver. Possible fix: use a smaller CFL." in msg
+    assert st.num_steps == ref.num_steps == 21
+    assert st.t == ref.t and st.dt == ref.dt
+    assert np.all(rel_l1(U, ref.U, p.g) <= REL_L1_TOL)
+    assert np.all(rel_l1(W, ref.W, p.g) <= REL_L1_TOL)
+    q = shear_layer(64, steps=10)
+    rc, msg, W, U, st = run_noalloc(q)
+    ref = run_regular(q)
+    assert rc == 0 and st.num_steps == ref.num_steps == 10, msg
+    assert np.all(rel_l1(U, ref.U, q.g) <= REL_L1_TOL)
+
+
+def test_noalloc_calls_leave_device_memory_unchanged(gpu_available):
+    """A first round of calls creates the CUDA context and loads every kernel
+    the later calls launch (module loading is lazy and takes device memory
+    on a kernel's first launch); after that, repeated calls must not change
+    the device's free memory."""
+    problems = consecutive_problems()
+    for p in problems:
+        assert run_noalloc(p)[0] == 0
+    before = device_free_bytes()
+    for _ in range(2):
+        for p in problems:
+            assert run_noalloc(p)[0] == 0
+    assert device_free_bytes() == before
