@@ -439,10 +439,12 @@ def run_1d(nx: int, g: int, bounds, gamma: float, W: np.ndarray, U: np.ndarray,
            bc=("transmissive", "transmissive"), integrator="godunov_first_order_1d",
            riemann_solver="riemann_solver_exact", slope_limiter="minmod", cfl=0.9, tf=0.2,
            max_steps=-1, options: HydroGpuOptions | None = None,
-           coord_sys: str = "cartesian_1d", storing: dict | None = None) -> RunResult:
+           coord_sys: str = "cartesian_1d", storing: dict | None = None,
+           verbose: int = 0) -> RunResult:
     """Run a 1D problem (W, U: (3, nx+2g)) on a cartesian_1d, cylindrical_1d
     or spherical_1d grid.  storing: {"interval", "output_dir",
-    "store_initial"} turns snapshots on, as for the 2D runs."""
+    "store_initial"} turns snapshots on, as for the 2D runs; verbose is
+    Settings.verbose (> 0: the exact solver's bisection warnings)."""
     lib = library()
     h = _SystemHandle(lib, coord_sys, nx, 0, g, bounds, gamma)
     try:
@@ -461,7 +463,7 @@ def run_1d(nx: int, g: int, bounds, gamma: float, W: np.ndarray, U: np.ndarray,
             d = storing["output_dir"].encode()
             keep.append(d)
             sp.output_dir = d
-        settings = Settings(0, True)
+        settings = Settings(verbose, True)
         simp = SimulationParam(tf)
         st = SimulationStatus(0, 0.0, 0.0)
         opt = options if options is not None else lib.hydro_gpu_default_options()

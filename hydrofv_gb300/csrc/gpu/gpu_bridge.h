@@ -30,6 +30,9 @@ typedef struct HydroRunOutcome
     int code;
     int where;
     char message[256];
+    /* exact Riemann solves whose bisection passed 500 (k+1) iterations
+     * (HydroStepControl.bisect_marks of a 1D run) */
+    unsigned int bisect_marks[10];
 } HydroRunOutcome;
 
 /* A 2D Cartesian problem as the kernels see it. */

@@ -8,6 +8,8 @@
  * arithmetic.  The time loop never calls them: launch_simulation runs on the
  * GPU.  Host code here is compiled with -ffp-contract=off.
  */
+#include <cstdio>
+
 #include "hydro.h"
 #include "numerics.cuh"
 
@@ -27,6 +29,21 @@ ErrorStatus exact_error(int rc)
         return WRAP_RAISE_ERROR(FAILURE, "Failed to bracket the root for bisection method.");
     return WRAP_RAISE_ERROR(FAILURE,
                             "Bisection method did not converge after 5001 iterations for exact riemann solver.");
+}
+
+/* The reference's verbose warnings of one exact solve, in its order: one per
+ * 500 bisection iterations (src/riemann_solver_exact.c:736-744). */
+void bisection_warnings(const unsigned int marks[kBisectionMarks], int verbose)
+{
+    if (verbose <= 0) return;
+    for (int k = 0; k < kBisectionMarks; k++)
+        for (unsigned int n = 0; n < marks[k]; n++) {
+            char buf[128];
+            snprintf(buf, sizeof buf,
+                     "Bisection method did not converge after %d iterations for exact riemann solver.",
+                     500 * (k + 1));
+            WRAP_RAISE_WARNING(buf);
+        }
 }
 
 }  // namespace
@@ -116,10 +133,11 @@ ErrorStatus solve_exact_1d(double *sol_rho, double *sol_u, double *sol_p, const 
                            const double rho_R, const double u_R, const double p_R,
                            const double tol, const double speed, const int verbose)
 {
-    (void) verbose;
     const GasConst<double> c = make_gas_const<double>(gamma, tol);
     double o[3];
-    const int rc = exact_solve_1d(c, rho_L, u_L, p_L, rho_R, u_R, p_R, speed, o);
+    unsigned int marks[kBisectionMarks] = {};
+    const int rc = exact_solve_1d(c, rho_L, u_L, p_L, rho_R, u_R, p_R, speed, o, marks);
+    bisection_warnings(marks, verbose);
     if (rc != DEV_OK) return exact_error(rc);
     *sol_rho = o[0];
     *sol_u = o[1];
@@ -133,10 +151,11 @@ ErrorStatus solve_flux_exact_1d(double *flux_mass, double *flux_momentum, double
                                 const double p_R, const double tol, const double speed,
                                 const int verbose)
 {
-    (void) verbose;
     const GasConst<double> c = make_gas_const<double>(gamma, tol);
     double F[3];
-    const int rc = exact_flux_1d(c, rho_L, u_L, p_L, rho_R, u_R, p_R, speed, F);
+    unsigned int marks[kBisectionMarks] = {};
+    const int rc = exact_flux_1d(c, rho_L, u_L, p_L, rho_R, u_R, p_R, speed, F, marks);
+    bisection_warnings(marks, verbose);
     *flux_mass = F[0];
     *flux_momentum = F[1];
     *flux_energy = F[2];

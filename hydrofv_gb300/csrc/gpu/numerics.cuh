@@ -598,11 +598,28 @@ HD R exact_f(const GasConst<R> &c, R rho_L, R u_L, R p_L, R a_L, R rho_R, R u_R,
     return exact_fK(c, rho_L, p_L, a_L, ps) + exact_fK(c, rho_R, p_R, a_R, ps) + (u_R - u_L);
 }
 
+/* Bisection iterations at which the reference warns when Settings.verbose
+ * > 0 ("Bisection method did not converge after %d iterations", every 500
+ * iterations, src/riemann_solver_exact.c:736-744): marks[k] counts the
+ * solves that passed 500 (k + 1) iterations.  The caller prints the
+ * warnings; a null pointer counts nothing. */
+constexpr int kBisectionMarks = 10;
+
+HD void note_bisection_mark(unsigned int *marks, int count)
+{
+    if (marks == nullptr || count % 500 != 0) return;
+#if defined(__CUDA_ARCH__)
+    atomicAdd(&marks[count / 500 - 1], 1u);
+#else
+    marks[count / 500 - 1] += 1u;
+#endif
+}
+
 /* Newton-Raphson (<= 100 iterations) with a bracketed bisection fallback
  * (<= 5000 iterations): every loop is bounded. */
 template <class R>
 HD int exact_p_star(const GasConst<R> &c, R rho_L, R u_L, R p_L, R a_L,
-                    R rho_R, R u_R, R p_R, R a_R, R *out)
+                    R rho_R, R u_R, R p_R, R a_R, R *out, unsigned int *marks = nullptr)
 {
     const R pg = guess_p(c, rho_L, u_L, p_L, a_L, rho_R, u_R, p_R, a_R);
     bool bracket = false;
@@ -654,6 +671,7 @@ HD int exact_p_star(const GasConst<R> &c, R rho_L, R u_L, R p_L, R a_L,
         const R fm = exact_f(c, rho_L, u_L, p_L, a_L, rho_R, u_R, p_R, a_R, pm);
         if (fm * f_lo < R(0)) { p_hi = pm; f_hi = fm; }
         else { p_lo = pm; f_lo = fm; }
+        note_bisection_mark(marks, count);
     }
     return DEV_ERR_EXACT_BISECTION;
 }
@@ -716,7 +734,7 @@ HD void exact_sample(const GasConst<R> &c, R rho_L, R u_L, R p_L, R a_L,
 /* Exact solution sampled at x/t = S (src/riemann_solver_exact.c:332-469).
  * o = (rho, u, p).  On a p* failure o is zeroed and the error returned. */
 template <class R>
-HD int exact_solve_1d(const GasConst<R> &c, R rho_L, R u_L, R p_L, R rho_R, R u_R, R p_R, R S, R o[3])
+HD int exact_solve_1d(const GasConst<R> &c, R rho_L, R u_L, R p_L, R rho_R, R u_R, R p_R, R S, R o[3], unsigned int *marks = nullptr)
 {
     const R a_L = (rho_L > R(0)) ? sound_speed(c, rho_L, p_L) : R(0);
     const R a_R = (rho_R > R(0)) ? sound_speed(c, rho_R, p_R) : R(0);
@@ -727,7 +745,7 @@ HD int exact_solve_1d(const GasConst<R> &c, R rho_L, R u_L, R p_L, R rho_R, R u_
         return DEV_OK;
     }
     R ps = R(0);
-    const int rc = exact_p_star(c, rho_L, u_L, p_L, a_L, rho_R, u_R, p_R, a_R, &ps);
+    const int rc = exact_p_star(c, rho_L, u_L, p_L, a_L, rho_R, u_R, p_R, a_R, &ps, marks);
     if (rc != DEV_OK) { o[0] = o[1] = o[2] = R(0); return rc; }
     const R us = R(0.5) * (u_L + u_R)
                + R(0.5) * (exact_fK(c, rho_R, p_R, a_R, ps) - exact_fK(c, rho_L, p_L, a_L, ps));
@@ -737,10 +755,11 @@ HD int exact_solve_1d(const GasConst<R> &c, R rho_L, R u_L, R p_L, R rho_R, R u_
 
 /* Exact Godunov flux at x/t = S (src/riemann_solver_exact.c:471-510). */
 template <class R>
-HD int exact_flux_1d(const GasConst<R> &c, R rho_L, R u_L, R p_L, R rho_R, R u_R, R p_R, R S, R F[3])
+HD int exact_flux_1d(const GasConst<R> &c, R rho_L, R u_L, R p_L, R rho_R, R u_R, R p_R, R S, R F[3],
+                     unsigned int *marks = nullptr)
 {
     R s[3];
-    const int rc = exact_solve_1d(c, rho_L, u_L, p_L, rho_R, u_R, p_R, S, s);
+    const int rc = exact_solve_1d(c, rho_L, u_L, p_L, rho_R, u_R, p_R, S, s, marks);
     F[0] = s[0] * s[1];
     F[1] = s[0] * s[1] * s[1] + s[2];
     F[2] = (s[2] * c.g_gm1 + R(0.5) * s[0] * s[1] * s[1]) * s[1];

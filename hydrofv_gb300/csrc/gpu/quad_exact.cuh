@@ -91,7 +91,8 @@ __device__ __forceinline__ double quad_f(const Quad &Q, const GasConst<double> &
 
 /* exact_p_star (numerics.cuh) with the function evaluations shared by the quad. */
 static __device__ int quad_p_star(const Quad &Q, const GasConst<double> &c, const Sides &S, double rho_L, double u_L,
-                           double p_L, double a_L, double rho_R, double u_R, double p_R, double a_R, double *out)
+                           double p_L, double a_L, double rho_R, double u_R, double p_R, double a_R, double *out,
+                           unsigned int *marks)
 {
     const double pg = guess_p(c, rho_L, u_L, p_L, a_L, rho_R, u_R, p_R, a_R);
     bool bracket = false;
@@ -147,6 +148,7 @@ static __device__ int quad_p_star(const Quad &Q, const GasConst<double> &c, cons
         const double fm = quad_f(Q, c, S, pm);
         if (fm * f_lo < 0.0) { p_hi = pm; f_hi = fm; }
         else { p_lo = pm; f_lo = fm; }
+        if (Q.q == 0) note_bisection_mark(marks, count);
     }
     return DEV_ERR_EXACT_BISECTION;
 }
@@ -212,7 +214,8 @@ static __device__ void quad_sample(const GasConst<double> &c, double rho_L, doub
 
 /* exact_solve_1d (numerics.cuh) on a quad: the state sampled at x/t = S. */
 static __device__ int quad_exact_solve(const Quad &Q, const GasConst<double> &c, double rho_L, double u_L, double p_L,
-                                double rho_R, double u_R, double p_R, double S, double o[3])
+                                double rho_R, double u_R, double p_R, double S, double o[3],
+                                unsigned int *marks = nullptr)
 {
     /* lanes 0, 2 the left side, 1, 3 the right: the sound speed (exact_solve_1d's
      * a_L, a_R) and the shock coefficient A of exact_fK / exact_dfK */
@@ -230,7 +233,7 @@ static __device__ int quad_exact_solve(const Quad &Q, const GasConst<double> &c,
     }
     const Sides Sd{ rho_L, p_L, a_L, rho_R, p_R, a_R, u_R - u_L, A_L, A_R };
     double ps = 0.0;
-    const int rc = quad_p_star(Q, c, Sd, rho_L, u_L, p_L, a_L, rho_R, u_R, p_R, a_R, &ps);
+    const int rc = quad_p_star(Q, c, Sd, rho_L, u_L, p_L, a_L, rho_R, u_R, p_R, a_R, &ps, marks);
     if (rc != DEV_OK) { o[0] = o[1] = o[2] = 0.0; return rc; }
     double v[4], pre[4];
     quad_fdf(Q, c, Sd, ps, v, true, pre);
@@ -241,10 +244,10 @@ static __device__ int quad_exact_solve(const Quad &Q, const GasConst<double> &c,
 
 /* exact_flux_1d (numerics.cuh) on a quad, at x/t = 0. */
 static __device__ int quad_exact_flux(const Quad &Q, const GasConst<double> &c, double rl, double ul, double pl,
-                               double rr, double ur, double pr, double F[3])
+                               double rr, double ur, double pr, double F[3], unsigned int *marks = nullptr)
 {
     double s[3];
-    const int rc = quad_exact_solve(Q, c, rl, ul, pl, rr, ur, pr, 0.0, s);
+    const int rc = quad_exact_solve(Q, c, rl, ul, pl, rr, ur, pr, 0.0, s, marks);
     F[0] = s[0] * s[1];
     F[1] = s[0] * s[1] * s[1] + s[2];
     F[2] = (s[2] * c.g_gm1 + 0.5 * s[0] * s[1] * s[1]) * s[1];

@@ -308,8 +308,10 @@ __global__ void __launch_bounds__(kThreads) run1d_kernel(const Run1dArgs a)
                 const double speed = left ? dv(theta * a.dx, dt) : dv((theta - 1.0) * a.dx, dt);
                 double o[3];
                 const int rc = kQuadExact
-                    ? quad_exact_solve(Q, a.gas, T[0][l], T[1][l], T[2][l], T[0][r], T[1][r], T[2][r], speed, o)
-                    : exact_solve_1d(a.gas, T[0][l], T[1][l], T[2][l], T[0][r], T[1][r], T[2][r], speed, o);
+                    ? quad_exact_solve(Q, a.gas, T[0][l], T[1][l], T[2][l], T[0][r], T[1][r], T[2][r], speed, o,
+                                       a.ctrl->bisect_marks)
+                    : exact_solve_1d(a.gas, T[0][l], T[1][l], T[2][l], T[0][r], T[1][r], T[2][r], speed, o,
+                                     a.ctrl->bisect_marks);
                 if (!kQuadExact || Q.q == 0) {
                     if (rc != DEV_OK) atomicCAS(&errs[buf], 0, rc);
                     W[0][i] = o[0];
@@ -353,8 +355,8 @@ __global__ void __launch_bounds__(kThreads) run1d_kernel(const Run1dArgs a)
                 const int il = a.scheme == 1 ? i : i - 1;
                 const double rl = sl[0][il], ul = sl[1][il], pl = sl[2][il];
                 const double rr = sr[0][i], ur = sr[1][i], pr = sr[2][i];
-                const int rc = quad ? quad_exact_flux(Q, a.gas, rl, ul, pl, rr, ur, pr, F)
-                             : a.solver == 1 ? exact_flux_1d(a.gas, rl, ul, pl, rr, ur, pr, 0.0, F)
+                const int rc = quad ? quad_exact_flux(Q, a.gas, rl, ul, pl, rr, ur, pr, F, a.ctrl->bisect_marks)
+                             : a.solver == 1 ? exact_flux_1d(a.gas, rl, ul, pl, rr, ur, pr, 0.0, F, a.ctrl->bisect_marks)
                                              : hllc_flux_1d(a.gas, rl, ul, pl, rr, ur, pr, F);
                 if (!quad || Q.q == 0) {
                     if (rc != DEV_OK && a.scheme == 0) atomicCAS(&errs[buf], 0, rc);
@@ -533,6 +535,7 @@ extern "C" int hydro_run1d(const HydroGrid1D *grid, double *const Wh[3], double 
     int rc = -1;
     Run1dArgs a;
     memset(&a, 0, sizeof a);
+    memset(&c, 0, sizeof c);
     cudaLaunchConfig_t lcfg = {};
     cudaLaunchAttribute lattr;
     memset(&lattr, 0, sizeof lattr);
@@ -652,6 +655,7 @@ done:
     oc->t = c.t;
     oc->dt = c.dt;
     oc->store_count = c.store_count;
+    for (int k = 0; k < 10; k++) oc->bisect_marks[k] = c.bisect_marks[k];
     if (stats) {
         stats->h2d_ms = ms_h2d;
         stats->step_ms = ms_steps;

@@ -33,6 +33,9 @@ typedef struct HydroStepControl {
     /* smax[k % 3] = ordered-bit maxima of (a+|u|, a+|v|) over the interior of
      * the state that step k starts from. */
     unsigned long long smax[3][2];
+    /* bisect_marks[k]: exact Riemann solves whose bisection passed 500 (k+1)
+     * iterations (the reference's verbose warnings; 1D runs only) */
+    unsigned int bisect_marks[10];
 } HydroStepControl;
 
 /* Per-run stepping parameters (kernel arguments, constant for a run; the

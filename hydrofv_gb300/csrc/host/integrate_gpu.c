@@ -75,6 +75,25 @@ const char *hydro_gpu_version(void)
 /* ------------------------------------------------------- error mapping */
 
 /* Turn a bridge outcome into the reference's ErrorStatus. */
+/* The reference warns every 500 bisection iterations of its exact Riemann
+ * solver when Settings.verbose > 0 (src/riemann_solver_exact.c:736-744).
+ * The 1D kernel counts the solves that passed each mark; the warnings are
+ * printed after the run, mark by mark (for a single slow solve, the
+ * reference's order). */
+static void bisection_warnings(const Settings *settings, const HydroRunOutcome *oc)
+{
+    if (!settings || settings->verbose <= 0) return;
+    for (int k = 0; k < 10; k++)
+        for (unsigned int n = 0; n < oc->bisect_marks[k]; n++)
+        {
+            char buf[128];
+            snprintf(buf, sizeof buf,
+                     "Bisection method did not converge after %d iterations for exact riemann solver.",
+                     500 * (k + 1));
+            WRAP_RAISE_WARNING(buf);
+        }
+}
+
 static ErrorStatus outcome_error(const HydroRunOutcome *oc)
 {
     switch (oc->kind)
@@ -428,6 +447,7 @@ static ErrorStatus run_1d(
     HydroRunOutcome oc;
     const int rc = hydro_run1d(&grid, W, U, &params, simp->tf, opt->max_steps, sp->store_count_,
                                snapshot_cb, &ctx, opt, &oc, stats);
+    bisection_warnings(settings, &oc);
     status->num_steps = oc.num_steps;
     status->t = oc.t;
     status->dt = oc.dt;

@@ -151,7 +151,7 @@ ErrorStatus store_snapshot(
     PUT(g_status, "simulation_time", H5T_NATIVE_DOUBLE, scalar, &st->t);
     PUT(g_status, "dt", H5T_NATIVE_DOUBLE, scalar, &st->dt);
     PUT(g_fields, "density", H5T_NATIVE_DOUBLE, field, s->density_);
-    PUT(g_fields, is2d ? "velocity_x" : "velocity", H5T_NATIVE_DOUBLE, field, s->velocity_x_);
+    PUT(g_fields, "velocity_x", H5T_NATIVE_DOUBLE, field, s->velocity_x_);
     if (is2d) PUT(g_fields, "velocity_y", H5T_NATIVE_DOUBLE, field, s->velocity_y_);
     PUT(g_fields, "pressure", H5T_NATIVE_DOUBLE, field, s->pressure_);
     PUT(g_params, "x_min", H5T_NATIVE_DOUBLE, scalar, &s->x_min);

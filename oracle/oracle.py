@@ -102,6 +102,9 @@ def _bind(lib: C.CDLL, prefix: str) -> C.CDLL:
     f = getattr(lib, prefix + "gravity_source_2d")
     f.restype = C.c_int
     f.argtypes = [C.c_int] * 3 + [C.c_double] * 7 + [C.c_char_p] * 4 + [_dp] * 8
+    if prefix == "ref_":
+        lib.ref_set_verbose.restype = None
+        lib.ref_set_verbose.argtypes = [C.c_int]
     f = getattr(lib, prefix + "exact_status")
     f.restype = C.c_int
     f.argtypes = [C.c_double] * 8 + [C.c_char_p, C.c_int]

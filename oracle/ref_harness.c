@@ -23,6 +23,14 @@
 #include "source_term.h"
 
 static long long g_stop_after_steps = -1;
+static int g_verbose = 0;
+
+/* Settings.verbose of the runs and solves that follow (the reference's
+ * exact solver warns every 500 bisection iterations when it is > 0). */
+void ref_set_verbose(int verbose)
+{
+    g_verbose = verbose;
+}
 
 StoringParam get_new_storing_param(void)
 {
@@ -148,7 +156,7 @@ int ref_run_2d_ex(
     }
     g_stop_after_steps = max_steps;
 
-    Settings settings = { .verbose = 0, .no_progress_bar = true };
+    Settings settings = { .verbose = g_verbose, .no_progress_bar = true };
     SimulationParam simp = { .tf = (max_steps >= 0) ? 1e300 : tf };
     SimulationStatus st = { 0, 0.0, 0.0 };
 
@@ -265,7 +273,7 @@ int ref_run_1d_ex(
     }
     g_stop_after_steps = max_steps;
 
-    Settings settings = { .verbose = 0, .no_progress_bar = true };
+    Settings settings = { .verbose = g_verbose, .no_progress_bar = true };
     SimulationParam simp = { .tf = (max_steps >= 0) ? 1e300 : tf };
     SimulationStatus st = { 0, 0.0, 0.0 };
 
@@ -301,7 +309,7 @@ int ref_exact_flux_1d(double gamma, double rho_L, double u_L, double p_L,
                       double rho_R, double u_R, double p_R, double tol, double speed, double *out3)
 {
     ErrorStatus e = solve_flux_exact_1d(&out3[0], &out3[1], &out3[2], gamma,
-                                        rho_L, u_L, p_L, rho_R, u_R, p_R, tol, speed, 0);
+                                        rho_L, u_L, p_L, rho_R, u_R, p_R, tol, speed, g_verbose);
     int rc = e.return_code;
     free_traceback(&e);
     return rc;
@@ -321,7 +329,7 @@ int ref_exact_1d(double gamma, double rho_L, double u_L, double p_L,
                  double rho_R, double u_R, double p_R, double tol, double speed, double *out3)
 {
     ErrorStatus e = solve_exact_1d(&out3[0], &out3[1], &out3[2], gamma,
-                                   rho_L, u_L, p_L, rho_R, u_R, p_R, tol, speed, 0);
+                                   rho_L, u_L, p_L, rho_R, u_R, p_R, tol, speed, g_verbose);
     int rc = e.return_code;
     free_traceback(&e);
     return rc;
@@ -335,7 +343,7 @@ int ref_exact_status(double gamma, double rho_L, double u_L, double p_L,
 {
     double out3[3];
     ErrorStatus e = solve_exact_1d(&out3[0], &out3[1], &out3[2], gamma,
-                                   rho_L, u_L, p_L, rho_R, u_R, p_R, tol, 0.0, 0);
+                                   rho_L, u_L, p_L, rho_R, u_R, p_R, tol, 0.0, g_verbose);
     int kind = 0;
     if (errbuf && errlen > 0) errbuf[0] = '\0';
     if (e.return_code != SUCCESS)

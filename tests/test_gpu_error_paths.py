@@ -273,3 +273,37 @@ def test_c_program_gets_the_error_through_launch_simulation(gpu_available, oracl
     assert float(raw[16:24].view(np.float64)[0]) == ref.dt
     state = raw[24:].view(np.float64).reshape(6, total)
     assert same_bits(state[:3], done.W) and same_bits(state[3:], done.U)
+
+
+def _bisection_warnings(text):
+    import re
+    return [int(m) for m in re.findall(r"Bisection method did not converge after (\d+) iterations", text)]
+
+
+@pytest.mark.parametrize("verbose", [0, 1])
+def test_verbose_run_prints_the_bisection_warnings(gpu_available, oracle_mod, capfd, verbose):
+    """Settings.verbose > 0: the failing face of the pressure-scaled Sod tube
+    passes 500, 1000, ... 5000 bisection iterations before the error, and
+    the run prints the reference's ten warnings; with verbose = 0 none.  The
+    reference's own run is the comparison where it was built."""
+    O = oracle_mod
+    p = sod(O, 100, 200)
+    p.W[2] *= 1e12
+    p.U = conserved_1d(O, p)
+    capfd.readouterr()
+    gpu = H.run_1d(p.nx, p.g, (p.x_min, p.x_max), p.gamma, p.W, p.U, bc=p.bc, integrator=p.integrator,
+                   riemann_solver=p.riemann_solver, slope_limiter=p.slope_limiter, cfl=p.cfl, tf=p.tf,
+                   max_steps=p.max_steps, verbose=verbose)
+    got = _bisection_warnings(capfd.readouterr().err)
+    assert gpu.code == FAILURE and gpu.num_steps == 1
+    want = list(range(500, 5001, 500)) if verbose else []
+    assert got == want
+    if verbose and O.reference_available():
+        ref = O.load("ref_serial")
+        ref.lib.ref_set_verbose(1)
+        try:
+            r = ref.run_1d(p)
+            assert r.rc == FAILURE and r.num_steps == 1
+            assert _bisection_warnings(capfd.readouterr().err) == got
+        finally:
+            ref.lib.ref_set_verbose(0)

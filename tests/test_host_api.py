@@ -288,3 +288,34 @@ def test_guided_chunk_plan_covers_every_row_once(hydro_lib, nx, ny, slots):
     assert np.all(heights[big] <= h1) and np.all(heights[~big] <= max(h2, 1))
     if tail:
         assert np.all(np.diff(big.astype(int)) <= 0)      # tall items first
+
+
+def _bisection_warnings(text):
+    """The iteration counts of the exact solver's warnings in stderr text."""
+    return [int(m) for m in re.findall(r"Bisection method did not converge after (\d+) iterations", text)]
+
+
+def test_exact_solver_verbose_warnings_like_the_reference(hydro_lib, oracle_mod, capfd):
+    """solve_exact_1d with verbose > 0 warns every 500 bisection iterations
+    (src/riemann_solver_exact.c:736-744): a collision at pressures near 1e12,
+    where the bisection cannot reach its absolute tolerance, prints ten
+    warnings (500 ... 5000) before failing; verbose = 0 prints none."""
+    L = (0.11595095827026866, 1130033.0105304043, 550729744742.7017)
+    R = (0.002907116592475837, 4172977.0479090274, 4571920669538.1)
+    out = [C.c_double() for _ in range(3)]
+    for verbose, want in ((1, list(range(500, 5001, 500))), (0, [])):
+        capfd.readouterr()
+        code, msg = H._consume(hydro_lib, hydro_lib.solve_exact_1d(
+            *[C.pointer(o) for o in out], 1.4, *L, *R, 1e-6, 0.0, verbose))
+        assert code == 1 and "Bisection method did not converge after 5001 iterations" in msg
+        assert _bisection_warnings(capfd.readouterr().err) == want
+    O = oracle_mod
+    if O.reference_available():
+        ref = O.load("ref_serial")
+        ref.lib.ref_set_verbose(1)
+        try:
+            capfd.readouterr()
+            assert ref.exact_status(1.4, L, R)[0] == 2
+            assert _bisection_warnings(capfd.readouterr().err) == list(range(500, 5001, 500))
+        finally:
+            ref.lib.ref_set_verbose(0)
