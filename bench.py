@@ -386,14 +386,74 @@ def run_ensemble(args, H, device, ws, rank) -> None:
     print(json.dumps(line))
 
 
+def adjoint_checks(ad, p, seed, grad, n_dirs: int, rng_seed: int = 2024) -> dict:
+    """Checks of dJ/dW0 on n_dirs seeded random directions in (rho, p): the
+    dot-product test against the tangent-linear model, central differences
+    (eps 1e-6) of the branch-frozen replay, and of the free replay (dt
+    frozen, branches free) with the number of steps whose branch signature
+    flipped under either perturbation."""
+    import math
+    interior = np.zeros(p.W.shape[1:], dtype=bool)
+    interior[p.g:-p.g, p.g:-p.g] = True
+
+    def dot(a, b):
+        return math.fsum((a[:, interior] * b[:, interior]).ravel())
+
+    from hydrofv_gb300.problems import right_half_density_squared
+    checks = {"dot_product_rel": [], "fd_frozen_rel": [], "fd_free_rel": [], "fd_free_flipped_steps": []}
+    rng = np.random.default_rng(rng_seed)
+    _, base_sig = ad.replay(p.W) if n_dirs else (None, None)
+    eps = 1e-6
+    for _ in range(n_dirs):
+        d = np.zeros_like(p.W)
+        d[0] = rng.normal(size=d[0].shape) * np.abs(p.W[0])
+        d[3] = rng.normal(size=d[3].shape) * np.abs(p.W[3])
+        d[:, ~interior] = 0.0
+        an = dot(grad, d)
+        _, dwN = ad.tangent(d)
+        checks["dot_product_rel"].append(abs(dot(seed, dwN) - an) / abs(an))
+        jp = right_half_density_squared(p, ad.replay_frozen(p.W + eps * d))[0]
+        jm = right_half_density_squared(p, ad.replay_frozen(p.W - eps * d))[0]
+        checks["fd_frozen_rel"].append(abs((jp - jm) / (2 * eps) - an) / abs(an))
+        Wp, sp = ad.replay(p.W + eps * d)
+        Wm, sm = ad.replay(p.W - eps * d)
+        fd = (right_half_density_squared(p, Wp)[0] - right_half_density_squared(p, Wm)[0]) / (2 * eps)
+        checks["fd_free_rel"].append(abs(fd - an) / abs(an))
+        checks["fd_free_flipped_steps"].append(int(((sp != base_sig) | (sm != base_sig)).sum()))
+    # the free map's central differences against eps on the first two
+    # directions: where the error does not shrink with eps, the map jumps
+    # (Riemann regime switches of the star-pressure guess), not only kinks
+    rng = np.random.default_rng(rng_seed)
+    by_eps = {}
+    for k in range(min(2, n_dirs)):
+        d = np.zeros_like(p.W)
+        d[0] = rng.normal(size=d[0].shape) * np.abs(p.W[0])
+        d[3] = rng.normal(size=d[3].shape) * np.abs(p.W[3])
+        d[:, ~interior] = 0.0
+        an = dot(grad, d)
+        for e in (1e-6, 1e-8, 1e-10):
+            Wp, sp = ad.replay(p.W + e * d)
+            Wm, sm = ad.replay(p.W - e * d)
+            fd = (right_half_density_squared(p, Wp)[0] - right_half_density_squared(p, Wm)[0]) / (2 * e)
+            by_eps.setdefault(f"{e:.0e}", []).append(
+                {"rel": abs(fd - an) / abs(an), "flipped_steps": int(((sp != base_sig) | (sm != base_sig)).sum())})
+    checks["fd_free_by_eps"] = by_eps
+    unflipped = [r for r, f in zip(checks["fd_free_rel"], checks["fd_free_flipped_steps"]) if f == 0]
+    checks["fd_free_rel_max_unflipped"] = max(unflipped) if unflipped else None
+    checks["directions_unflipped"] = len(unflipped)
+    checks["eps"] = eps
+    checks["directions"] = n_dirs
+    return checks
+
+
 def run_adjoint(args, H, device, ws, rank) -> None:
     """Discrete adjoint of the shear layer (MC, periodic, FP64): forward pass
     with checkpoints, then the reverse pass (segment recomputation + reverse
     sweep) for dJ/dW0, J = sum_{x > 0.5} rho^2 V at the last step.  Checks
-    on --fd-directions seeded random directions in (rho, p): the dot-product
-    test against the tangent-linear model, central differences (eps 1e-6)
-    of the branch-frozen replay, and of the free replay with its branch flips."""
-    import math
+    on --fd-directions seeded random directions (adjoint_checks).  The same
+    checks run on a differentiable variant of the state: rho and p carry
+    seeded relative noise of amplitude --rho-p-noise, so no limiter of those
+    fields sits at its a = b = 0 kink and the free map has a derivative."""
     from hydrofv_gb300.problems import right_half_density_squared, shear_layer
     side = args.size if args.size != 2048 else 1024
     steps = args.steps
@@ -401,11 +461,6 @@ def run_adjoint(args, H, device, ws, rank) -> None:
     p = shear_layer(side, steps=steps)
     cells = p.nx * p.ny
     opts = H.default_options(device=device)
-    interior = np.zeros(p.W.shape[1:], dtype=bool)
-    interior[p.g:-p.g, p.g:-p.g] = True
-
-    def dot(a, b):
-        return math.fsum((a[:, interior] * b[:, interior]).ravel())
 
     with H.Adjoint2D(p, steps=steps, checkpoint_every=K, options=opts) as ad:
         for _ in range(max(1, args.warmup // 3)):
@@ -425,27 +480,19 @@ def run_adjoint(args, H, device, ws, rank) -> None:
         st = ad.stats()
         launches = st["kernel_launches"] - l0
         back_ms = st["recompute_ms"] + st["vjp_ms"]
-        checks = {"dot_product_rel": [], "fd_frozen_rel": [], "fd_free_rel": [], "fd_free_flipped_steps": []}
-        rng = np.random.default_rng(2024)
-        _, base_sig = ad.replay(p.W) if args.fd_directions else (None, None)
-        eps = 1e-6
-        for _ in range(args.fd_directions):
-            d = np.zeros_like(p.W)
-            d[0] = rng.normal(size=d[0].shape) * np.abs(p.W[0])
-            d[3] = rng.normal(size=d[3].shape) * np.abs(p.W[3])
-            d[:, ~interior] = 0.0
-            an = dot(grad, d)
-            _, dwN = ad.tangent(d)
-            checks["dot_product_rel"].append(abs(dot(seed, dwN) - an) / abs(an))
-            jp = right_half_density_squared(p, ad.replay_frozen(p.W + eps * d))[0]
-            jm = right_half_density_squared(p, ad.replay_frozen(p.W - eps * d))[0]
-            checks["fd_frozen_rel"].append(abs((jp - jm) / (2 * eps) - an) / abs(an))
-            Wp, sp = ad.replay(p.W + eps * d)
-            Wm, sm = ad.replay(p.W - eps * d)
-            fd = (right_half_density_squared(p, Wp)[0] - right_half_density_squared(p, Wm)[0]) / (2 * eps)
-            checks["fd_free_rel"].append(abs(fd - an) / abs(an))
-            checks["fd_free_flipped_steps"].append(int(((sp != base_sig) | (sm != base_sig)).sum()))
+        checks = adjoint_checks(ad, p, seed, grad, args.fd_directions)
         st_all = ad.stats()
+    variant = None
+    if args.rho_p_noise > 0.0 and args.fd_directions > 0:
+        q = shear_layer(side, steps=steps, rho_p_noise=args.rho_p_noise)
+        with H.Adjoint2D(q, steps=steps, checkpoint_every=K, options=opts) as ad:
+            WN = ad.forward()
+            Jq, seed_q = right_half_density_squared(q, WN)
+            grad_q = ad.backward(seed_q)
+            stq = ad.stats()
+            variant = {"rho_p_noise": args.rho_p_noise, "J": Jq,
+                       "backward_vs_forward": (stq["recompute_ms"] + stq["vjp_ms"]) / stq["forward_ms"],
+                       "checks": adjoint_checks(ad, q, seed_q, grad_q, args.fd_directions)}
     if rank != 0:
         return
     line = {
@@ -465,8 +512,8 @@ def run_adjoint(args, H, device, ws, rank) -> None:
                      "reverse_sweep_vs_forward": st["vjp_ms"] / st_f["forward_ms"],
                      "recompute_mismatches": st["recompute_mismatches"],
                      "device_bytes": st_all["device_bytes"]},
-        "checks": dict(checks, eps=eps, directions=args.fd_directions,
-                       tangent_ms=st_all["tangent_ms"], replay_ms=st_all["replay_ms"]),
+        "checks": dict(checks, tangent_ms=st_all["tangent_ms"], replay_ms=st_all["replay_ms"]),
+        "differentiable_variant": variant,
         "e2e": {"value": ws * cells * steps / wall, "unit": "cell-steps/s",
                 "h2d_bytes_per_step": 4 * p.W[0].size * 8 / steps,
                 "d2h_bytes_per_step": 4 * p.W[0].size * 8 / steps,
@@ -637,6 +684,8 @@ def main() -> None:
     ap.add_argument("--checkpoint-every", type=int, default=50, help="adjoint checkpoint interval")
     ap.add_argument("--fd-directions", type=int, default=2,
                     help="adjoint: random directions checked by dot product and finite differences")
+    ap.add_argument("--rho-p-noise", type=float, default=1e-3,
+                    help="adjoint: relative noise on rho and p of the differentiable variant (0: none)")
     ap.add_argument("--autotune", action="store_true",
                     help="let the library time work-item shapes before stepping")
     ap.add_argument("--compare", action="store_true",

@@ -24,6 +24,9 @@ BUILD = os.path.join(PKG, "_build")
 LIB = os.path.join(PKG, "libhydro_gb300.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# Extra nvcc flags for every CUDA translation unit, e.g. a tile-shape define
+# (-DMH2D_THREADS_FP64=96 -DMH2D_CTAS_FP64=6) when sweeping launch shapes.
+EXTRA_NVCC = os.environ.get("HYDRO_NVCC_FLAGS", "").split()
 INCLUDES = ["-I" + os.path.join(ROOT, "include"), "-I" + os.path.join(CSRC, "gpu"),
             "-I" + os.path.join(CSRC, "host")]
 
@@ -102,7 +105,7 @@ def build(verbose: bool = False, force: bool = False) -> str:
         path = os.path.join(CSRC, src)
         obj = _obj(src)
         if force or _stale(obj, [path, __file__] + headers):
-            jobs.append([nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", *extra, *INCLUDES,
+            jobs.append([nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", *extra, *EXTRA_NVCC, *INCLUDES,
                          "-Xcompiler", "-fPIC,-ffp-contract=off,-Wall",
                          "-Xptxas", "-v", "-c", path, "-o", obj])
     for src in C_SOURCES:

@@ -1113,7 +1113,7 @@ extern "C" int hydro_adj2d_create(const HydroGrid2D *grid, const HydroGpuOptions
     pa.ny = grid->ny;
     pa.g = grid->g;
     pa.pitch = tx;
-    pa.strip_w = MH2D_THREADS - 2;
+    pa.strip_w = mh2d_threads<double>() - 2;
     for (int s = 0; s < 4; s++) pa.bc[s] = grid->bc[s];
     pa.dx = grid->dx;
     pa.dy = grid->dy;

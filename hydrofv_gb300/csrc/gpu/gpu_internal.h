@@ -15,8 +15,6 @@
 
 #include "mh2d_kernel.cuh"
 
-/* Threads per 2D step CTA: a strip of MH2D_THREADS-2 interior columns. */
-#define MH2D_THREADS 128
 
 namespace hydro {
 

@@ -47,7 +47,32 @@
 #include "numerics.cuh"
 #include "step_control.h"
 
+/* Threads per 2D step CTA (a strip of threads - 2 interior columns) and the
+ * CTAs per SM each state precision is compiled for (launch bounds).  FP64:
+ * 4 CTAs of 128 threads (128 registers); FP32: 8 CTAs of 128 (64 registers,
+ * a few spills; the FP32 form is latency bound, and at 8 per SM the 1088
+ * work items of a 2048^2 grid run in one wave: 7.4 -> 10.5 G
+ * cell-updates/s). */
+#ifndef MH2D_THREADS_FP64
+#define MH2D_THREADS_FP64 128
+#endif
+#ifndef MH2D_CTAS_FP64
+#define MH2D_CTAS_FP64 4
+#endif
+#ifndef MH2D_THREADS_FP32
+#define MH2D_THREADS_FP32 128
+#endif
+#ifndef MH2D_CTAS_FP32
+#define MH2D_CTAS_FP32 8
+#endif
+
 namespace hydro {
+
+template <class R>
+constexpr int mh2d_threads() { return sizeof(R) == 8 ? MH2D_THREADS_FP64 : MH2D_THREADS_FP32; }
+
+/* The same, for host code that holds the precision as a flag. */
+inline int mh2d_threads_for(bool fp32) { return fp32 ? MH2D_THREADS_FP32 : MH2D_THREADS_FP64; }
 
 template <class R>
 struct Mh2dArgs {
@@ -140,15 +165,19 @@ struct TapeCtx {
     }
 };
 
-/* Load W at padded (r, c), remapping ghost cells to their source.  Ghost
- * cells of custom (host callback) sides are read as stored: the host wrote
- * them after the previous step. */
+/* Where W at padded (r, c) comes from: the stored cell (rr, cc), with the
+ * sign of u (neg = 1) or v (neg = 2) flipped, or (cons) converted from the
+ * stored U of (rr, cc).  Ghost cells map to their source; ghost cells of
+ * custom (host callback) sides are read as stored: the host wrote them
+ * after the previous step. */
 template <class R>
-__device__ __forceinline__ void fetch_w(const Mh2dArgs<R> &a, const R *const *Win,
-                                        const R *const *Uin, bool raw, int r, int c, R w[5])
+__device__ __forceinline__ void w_source(const Mh2dArgs<R> &a, bool raw, int r, int c, int &rr, int &cc,
+                                         int &neg, bool &cons)
 {
-    int rr = r, cc = c, neg = 0;
-    bool cons = false;
+    rr = r;
+    cc = c;
+    neg = 0;
+    cons = false;
     if (!raw) {
         const int g = a.g, nx = a.nx, ny = a.ny;
         int f = 0, k = 0;
@@ -174,6 +203,16 @@ __device__ __forceinline__ void fetch_w(const Mh2dArgs<R> &a, const R *const *Wi
             else if (f != BC_CUSTOM) { rr = g + ny - 1 - k; neg = (f == BC_REFLECTIVE) ? 2 : 0; }
         }
     }
+}
+
+/* Load W at padded (r, c), remapping ghost cells to their source (w_source). */
+template <class R>
+__device__ __forceinline__ void fetch_w(const Mh2dArgs<R> &a, const R *const *Win,
+                                        const R *const *Uin, bool raw, int r, int c, R w[5])
+{
+    int rr, cc, neg;
+    bool cons;
+    w_source(a, raw, r, c, rr, cc, neg, cons);
     const long long idx = (long long) rr * a.pitch + cc;
     if (cons) {
         cons_to_prim_2d_guarded(a.gas, (R) a.vol, Uin[0][idx], Uin[1][idx], Uin[2][idx], Uin[3][idx], w);
@@ -186,6 +225,28 @@ __device__ __forceinline__ void fetch_w(const Mh2dArgs<R> &a, const R *const *Wi
     if (neg == 2) w[2] = -w[2];
 }
 
+/* Asynchronous 4-byte global -> shared copies (cp.async, no register
+ * staging), grouped per ring row: commit after a row's copies, wait until
+ * at most N groups of this thread are still in flight. */
+__device__ __forceinline__ void cp_async4(void *smem, const void *gmem)
+{
+    const unsigned s = (unsigned) __cvta_generic_to_shared(smem);
+    unsigned long long g;
+    asm volatile("cvta.to.global.u64 %0, %1;" : "=l"(g) : "l"(gmem));
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(s), "l"(g) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_commit()
+{
+    asm volatile("cp.async.commit_group;" ::: "memory");
+}
+
+template <int N>
+__device__ __forceinline__ void cp_async_wait()
+{
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
 __device__ __forceinline__ void record_error(HydroStepControl *ctrl, int code, int where)
 {
     if (atomicCAS(&ctrl->error_code, 0, code) == 0) ctrl->error_cell = where;
@@ -194,7 +255,10 @@ __device__ __forceinline__ void record_error(HydroStepControl *ctrl, int code, i
 /* Shared memory of one CTA: the W row ring and one batch of faces. */
 template <class R, int NT>
 struct Mh2dShared {
-    R ring[3][5][NT + 2];       /* W rows (rho, u, v, p, a), columns c0-2 .. c0+NT-1 */
+    /* rows in the ring: FP32 keeps a fourth so the row after next can be
+     * copied in asynchronously while the current row is solved */
+    static constexpr int RING = sizeof(R) == 4 ? 4 : 3;
+    R ring[RING][5][NT + 2];    /* W rows (rho, u, v, p, a), columns c0-2 .. c0+NT-1 */
     R FL[4][2 * NT];            /* left face states; overwritten by the face flux */
     R FR[4][2 * NT];            /* right face states */
     R aL[2 * NT], aR[2 * NT];   /* sound speeds of the face states */
@@ -368,12 +432,13 @@ __device__ __forceinline__ void mh2d_item(const Mh2dArgs<R> &a, Mh2dShared<R, NT
      * side (x work); rows outside need only the strip's own columns.  Cells
      * outside the padded grid (first order with one ghost layer) are never
      * read and are not loaded. */
+    constexpr int RING = Mh2dShared<R, NT>::RING;
     auto load_row = [&](int r) {
         if (r < 0 || r >= ty) return;
         const bool full = (r >= r_begin && r < r_end);
         const int lo = full ? 0 : 2;
         const int hi = full ? sw + 3 : sw + 1;
-        const int s = r % 3;
+        const int s = r % RING;
         for (int u = tid; u < NT + 2; u += NT) {
             const int c = c0 - 2 + u;
             if (u >= lo && u <= hi && c >= 0 && c < tx) {
@@ -385,10 +450,43 @@ __device__ __forceinline__ void mh2d_item(const Mh2dArgs<R> &a, Mh2dShared<R, NT
         }
     };
 
+    /* FP32: the same row, with every cell that is a plain copy of a stored
+     * cell (interior cells, periodic and mirror images without a sign
+     * flip) copied by cp.async; the others are loaded as in load_row.
+     * Always commits one group (possibly empty), so a wait for all but the
+     * latest group means "all rows but the one issued last". */
+    auto load_row_async = [&](int r) {
+        if (r >= 0 && r < ty) {
+            const bool full = (r >= r_begin && r < r_end);
+            const int lo = full ? 0 : 2;
+            const int hi = full ? sw + 3 : sw + 1;
+            const int s = r % RING;
+            for (int u = tid; u < NT + 2; u += NT) {
+                const int c = c0 - 2 + u;
+                if (u >= lo && u <= hi && c >= 0 && c < tx) {
+                    int rr, cc, neg;
+                    bool cons;
+                    w_source(a, raw, r, c, rr, cc, neg, cons);
+                    if (!cons && neg == 0) {
+                        const long long idx = (long long) rr * a.pitch + cc;
+#pragma unroll
+                        for (int q = 0; q < 5; q++) cp_async4(&sm.ring[s][q][u], &Win[q][idx]);
+                    } else {
+                        R w[5];
+                        fetch_w(a, Win, Uin, raw, r, c, w);
+#pragma unroll
+                        for (int q = 0; q < 5; q++) sm.ring[s][q][u] = w[q];
+                    }
+                }
+            }
+        }
+        cp_async_commit();
+    };
+
     /* y reconstruction of this thread's cell in row r, (rho, v, u, p) order */
     auto recon_y = [&](int r, R lo[4], R hi[4]) {
         const int u = tid + 1;
-        const int sb = (r + 2) % 3, sc = r % 3, st = (r + 1) % 3;
+        const int sb = (r + RING - 1) % RING, sc = r % RING, st = (r + 1) % RING;
         const R rho = sm.ring[sc][0][u], vx = sm.ring[sc][1][u], vy = sm.ring[sc][2][u];
         const R p = sm.ring[sc][3][u], as = sm.ring[sc][4][u];
         if (FIRST_ORDER) {
@@ -431,6 +529,7 @@ __device__ __forceinline__ void mh2d_item(const Mh2dArgs<R> &a, Mh2dShared<R, NT
     if (inner) recon_y(r_begin - 1, tmp_lo, prev_hi);
     __syncthreads();
     load_row(r_begin + 1);
+    if constexpr (RING == 4) load_row_async(r_begin + 2);
     if (tid == 0) { sm.nT = 0; sm.nS = 0; }
     __syncthreads();
     if (inner) {
@@ -472,7 +571,15 @@ __device__ __forceinline__ void mh2d_item(const Mh2dArgs<R> &a, Mh2dShared<R, NT
                 for (int q = 0; q < 4; q++) upre[q] = Uin[q][pidx];
             }
         }
-        load_row(r + 2);
+        if constexpr (RING == 4) {
+            /* issue the row after next (the last one this item reads is
+             * r_end + 1), then wait for row r + 2, issued one row ago */
+            if (r + 3 <= r_end + 1) load_row_async(r + 3);
+            else cp_async_commit();
+            cp_async_wait<1>();
+        } else {
+            load_row(r + 2);
+        }
         if (tid == 0) { sm.nT = 0; sm.nS = 0; }
         __syncthreads();
 
@@ -486,7 +593,7 @@ __device__ __forceinline__ void mh2d_item(const Mh2dArgs<R> &a, Mh2dShared<R, NT
         }
         if (x_slot) {
             R xl[4], xh[4];
-            recon_x(r % 3, xl, xh);
+            recon_x(r % RING, xl, xh);
             if (tid <= sw) {
 #pragma unroll
                 for (int q = 0; q < 4; q++) sm.FL[q][tid] = xh[q];
@@ -587,6 +694,7 @@ __device__ __forceinline__ void mh2d_item(const Mh2dArgs<R> &a, Mh2dShared<R, NT
         }
         __syncthreads();
     }
+    if constexpr (RING == 4) cp_async_wait<0>();   /* nothing in flight into the next item's ring */
     if constexpr (sizeof(R) == 4) {
         if ((double) imx_x > mx_x) mx_x = (double) imx_x;
         if ((double) imx_y > mx_y) mx_y = (double) imx_y;
@@ -599,12 +707,9 @@ __device__ __forceinline__ void mh2d_item(const Mh2dArgs<R> &a, Mh2dShared<R, NT
  * SMs that finish early take more work (the FP64 pipe of an SM is shared by
  * its CTAs).
  */
-/* FP64: 4 CTAs per SM (128 registers; the FP64 pipe is the bound).  FP32:
- * 8 CTAs per SM (64 registers, a few spills): the FP32 form is latency
- * bound, and at 8 per SM the 1088 work items of a 2048^2 grid run in one
- * wave (measured 7.4 -> 10.5 G cell-updates/s). */
 template <class R, int LIM, int NT, int FIRST_ORDER, bool TAPE = false, bool GRAV = false>
-__global__ void __launch_bounds__(NT, (sizeof(R) == 4 ? 8 : 4)) mh2d_step_kernel(const Mh2dArgs<R> a)
+__global__ void __launch_bounds__(NT, (sizeof(R) == 4 ? MH2D_CTAS_FP32 : MH2D_CTAS_FP64))
+mh2d_step_kernel(const Mh2dArgs<R> a)
 {
     static_assert(NT % 32 == 0, "NT must be a whole number of warps");
     HydroStepControl *ctrl = a.ctrl;
@@ -782,7 +887,8 @@ __device__ __forceinline__ void instance_bookkeeping(HydroStepControl *ctrl, con
  * items.
  */
 template <class R, int LIM, int NT, int FIRST_ORDER>
-__global__ void __launch_bounds__(NT, (sizeof(R) == 4 ? 8 : 4)) mh2d_batch_step_kernel(const Mh2dBatchArgs<R> b)
+__global__ void __launch_bounds__(NT, (sizeof(R) == 4 ? MH2D_CTAS_FP32 : MH2D_CTAS_FP64))
+mh2d_batch_step_kernel(const Mh2dBatchArgs<R> b)
 {
     __shared__ Mh2dShared<R, NT> sm;
     __shared__ int s_inst, s_local, s_go, s_last;

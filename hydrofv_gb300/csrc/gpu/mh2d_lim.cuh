@@ -15,31 +15,31 @@ template <class R, int LIM, int FIRST_ORDER>
 cudaError_t mh2d_launch_step_lim(const Mh2dArgs<R> &a, int grid, cudaStream_t s)
 {
     if (a.gravity != 0.0)
-        mh2d_step_kernel<R, LIM, MH2D_THREADS, FIRST_ORDER, false, true><<<grid, MH2D_THREADS, 0, s>>>(a);
+        mh2d_step_kernel<R, LIM, mh2d_threads<R>(), FIRST_ORDER, false, true><<<grid, mh2d_threads<R>(), 0, s>>>(a);
     else
-        mh2d_step_kernel<R, LIM, MH2D_THREADS, FIRST_ORDER><<<grid, MH2D_THREADS, 0, s>>>(a);
+        mh2d_step_kernel<R, LIM, mh2d_threads<R>(), FIRST_ORDER><<<grid, mh2d_threads<R>(), 0, s>>>(a);
     return cudaGetLastError();
 }
 
 template <class R, int LIM>
 cudaError_t mh2d_launch_tape_lim(const Mh2dArgs<R> &a, int grid, cudaStream_t s)
 {
-    mh2d_step_kernel<R, LIM, MH2D_THREADS, 0, true><<<grid, MH2D_THREADS, 0, s>>>(a);
+    mh2d_step_kernel<R, LIM, mh2d_threads<R>(), 0, true><<<grid, mh2d_threads<R>(), 0, s>>>(a);
     return cudaGetLastError();
 }
 
 template <class R, int LIM, int FIRST_ORDER>
 cudaError_t mh2d_launch_batch_lim(const Mh2dBatchArgs<R> &b, int grid, cudaStream_t s)
 {
-    mh2d_batch_step_kernel<R, LIM, MH2D_THREADS, FIRST_ORDER><<<grid, MH2D_THREADS, 0, s>>>(b);
+    mh2d_batch_step_kernel<R, LIM, mh2d_threads<R>(), FIRST_ORDER><<<grid, mh2d_threads<R>(), 0, s>>>(b);
     return cudaGetLastError();
 }
 
 template <class R, int LIM, int FIRST_ORDER>
 cudaError_t mh2d_step_occupancy(int *per_sm)
 {
-    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, mh2d_step_kernel<R, LIM, MH2D_THREADS, FIRST_ORDER>,
-                                                         MH2D_THREADS, 0);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, mh2d_step_kernel<R, LIM, mh2d_threads<R>(), FIRST_ORDER>,
+                                                         mh2d_threads<R>(), 0);
 }
 
 }  // namespace hydro

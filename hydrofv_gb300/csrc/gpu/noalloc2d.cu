@@ -190,7 +190,7 @@ extern "C" int hydro_gpu_muscl_hancock_2d_noalloc(
     a.ny = ny;
     a.g = g;
     a.pitch = (int) tx;
-    a.strip_w = MH2D_THREADS - 2;
+    a.strip_w = mh2d_threads<double>() - 2;
     a.chunk_h = 64;
     for (int k = 0; k < 4; k++) a.bc[k] = bc[k];
     a.dx = s->dx_;

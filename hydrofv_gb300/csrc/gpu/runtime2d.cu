@@ -127,7 +127,7 @@ static void setup_args(HydroRun2D *run, Mh2dArgs<R> &a, const HydroGrid2D *grid,
     a.ny = grid->ny;
     a.g = grid->g;
     a.pitch = run->tx;
-    a.strip_w = MH2D_THREADS - 2;
+    a.strip_w = mh2d_threads<R>() - 2;
     for (int s = 0; s < 4; s++) a.bc[s] = grid->bc[s];
     a.dx = grid->dx;
     a.dy = grid->dy;
@@ -166,7 +166,7 @@ extern "C" int hydro_gpu_chunk_plan(int nx, int ny, int g, int slots, int *h1, i
     a.nx = nx;
     a.ny = ny;
     a.g = g;
-    a.strip_w = MH2D_THREADS - 2;
+    a.strip_w = mh2d_threads<double>() - 2;
     mh2d_guided_chunks(nx, ny, a.strip_w, slots, a.chunk_h, a.tail_h, a.tail_rows);
     *h1 = a.chunk_h;
     *h2 = a.tail_h;

@@ -102,7 +102,7 @@ static void build_args(HydroBatch2D *b, std::vector<Mh2dArgs<R>> &av)
         a.ny = g.ny;
         a.g = g.g;
         a.pitch = g.nx + 2 * g.g;
-        a.strip_w = MH2D_THREADS - 2;
+        a.strip_w = mh2d_threads<R>() - 2;
         a.chunk_h = b->opt.chunk_rows > 0 ? b->opt.chunk_rows : 32;
         for (int s = 0; s < 4; s++) a.bc[s] = g.bc[s];
         a.dx = g.dx;
@@ -174,7 +174,8 @@ extern "C" int hydro_batch2d_create(const HydroGrid2D *grids, int n, const Hydro
         b->off[k] = total;
         total += 22 * b->ncell[k];
         max_cells = std::max(max_cells, b->ncell[k]);
-        const int items = ((g.nx + MH2D_THREADS - 3) / (MH2D_THREADS - 2)) * ((g.ny + chunk_h - 1) / chunk_h);
+        const int nt = mh2d_threads_for(b->fp32);
+        const int items = ((g.nx + nt - 3) / (nt - 2)) * ((g.ny + chunk_h - 1) / chunk_h);
         b->item_off[k + 1] = b->item_off[k] + items;
     }
     if (b->item_off[n] <= 0 || (long long) b->item_off[n] > INT_MAX / 2) {
@@ -319,7 +320,8 @@ static int set_chunk(HydroBatch2D *b, int chunk, int ctas, HydroRunOutcome *oc)
     for (int k = 0; k < b->n; k++) {
         const int nx = b->fp32 ? b->a32[k].nx : b->a64[k].nx;
         const int ny = b->fp32 ? b->a32[k].ny : b->a64[k].ny;
-        b->item_off[k + 1] = b->item_off[k] + ((nx + MH2D_THREADS - 3) / (MH2D_THREADS - 2)) * ((ny + chunk - 1) / chunk);
+        const int nt = mh2d_threads_for(b->fp32);
+        b->item_off[k + 1] = b->item_off[k] + ((nx + nt - 3) / (nt - 2)) * ((ny + chunk - 1) / chunk);
         if (b->fp32) b->a32[k].chunk_h = chunk;
         else b->a64[k].chunk_h = chunk;
     }

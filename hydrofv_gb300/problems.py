@@ -167,11 +167,17 @@ def mid_points(lo: float, hi: float, n: int, g: int) -> np.ndarray:
 
 
 def shear_layer(n: int, g: int = 2, seed: int = 2024, steps: int = 200,
-                limiter: str = "monotonized_central") -> Problem2D:
+                limiter: str = "monotonized_central", rho_p_noise: float = 0.0) -> Problem2D:
     """Shear layer on [0,1]^2, periodic, gamma=5/3: rho=2, vx=+0.5 for
     |y-0.5|<0.25 else rho=1, vx=-0.5; p=2.5; vy=0.01 sin(4 pi x); seeded
     uniform noise U[-1e-3, 1e-3] on vx then vy (row-major over the interior).
-    MUSCL-Hancock + HLLC + MC, CFL 0.8, fixed step count."""
+    MUSCL-Hancock + HLLC + MC, CFL 0.8, fixed step count.
+
+    rho_p_noise > 0 also multiplies rho and p by 1 + U[-a, a] (a second
+    seeded stream, so the velocity noise is unchanged): with piecewise
+    constant rho and uniform p every limiter of those fields sits at its
+    a = b = 0 kink, where the step has no derivative; the noise moves them
+    off it."""
     gamma = 5.0 / 3.0
     N = n + 2 * g
     x = mid_points(0.0, 1.0, n, g)
@@ -190,13 +196,18 @@ def shear_layer(n: int, g: int = 2, seed: int = 2024, steps: int = 200,
     W[1][I] = vx[I] + noise_x
     W[2][I] = vy[I] + noise_y
     W[3][I] = 2.5
+    if rho_p_noise > 0.0:
+        rng2 = np.random.default_rng(seed + 1)
+        W[0][I] *= 1.0 + rng2.uniform(-rho_p_noise, rho_p_noise, size=(n, n))
+        W[3][I] *= 1.0 + rng2.uniform(-rho_p_noise, rho_p_noise, size=(n, n))
     bc = ("periodic",) * 4
     apply_bc_2d(W, g, n, n, bc)
     dx = 1.0 / N
     U = primitive_to_conserved_2d(W, gamma, dx * dx)
+    name = f"shear_layer_{n}" + (f"_noise{rho_p_noise:g}" if rho_p_noise > 0.0 else "")
     return Problem2D(n, n, g, 0.0, 1.0, 0.0, 1.0, gamma, W, U, bc,
                      "muscl_hancock_2d", "riemann_solver_hllc", limiter,
-                     cfl=0.8, tf=1e300, max_steps=steps, name=f"shear_layer_{n}")
+                     cfl=0.8, tf=1e300, max_steps=steps, name=name)
 
 
 def point_blast(n: int, g: int = 2, steps: int = 1000) -> Problem2D:
