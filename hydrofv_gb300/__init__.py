@@ -141,6 +141,7 @@ _SIGNATURES = {
     "launch_simulation": (ErrorStatus, [_P(BoundaryConditionParam), _P(System), _P(IntegratorParam),
                                         _P(StoringParam), _P(Settings), _P(SimulationParam),
                                         _P(SimulationStatus)]),
+    "hydro_gpu_trim_device_memory": (C.c_int, [C.c_int]),
     "hydro_gpu_default_options": (HydroGpuOptions, []),
     "hydro_gpu_set_process_options": (None, [_P(HydroGpuOptions)]),
     "hydro_gpu_launch_simulation": (ErrorStatus, [_P(BoundaryConditionParam), _P(System),

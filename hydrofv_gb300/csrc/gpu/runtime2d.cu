@@ -179,6 +179,69 @@ extern "C" int hydro_gpu_chunk_plan(int nx, int ny, int g, int slots, int *h1, i
     return n;
 }
 
+/*
+ * Device memory of the 2D runs comes from one stream-ordered pool per device
+ * that keeps what a finished run freed (release threshold: no limit).  A
+ * program that calls launch_simulation repeatedly therefore does not map and
+ * unmap its 0.7 GB (2048^2, FP64) of state on every call; the memory stays
+ * with the process until hydro_gpu_trim_device_memory() or exit.
+ */
+static std::mutex g_pool_mutex;
+static std::map<int, cudaMemPool_t> g_pools;
+
+static cudaError_t device_pool(int dev, cudaMemPool_t *out)
+{
+    std::lock_guard<std::mutex> lock(g_pool_mutex);
+    auto it = g_pools.find(dev);
+    if (it != g_pools.end()) {
+        *out = it->second;
+        return cudaSuccess;
+    }
+    cudaMemPoolProps props;
+    memset(&props, 0, sizeof props);
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    cudaMemPool_t pool;
+    cudaError_t e = cudaMemPoolCreate(&pool, &props);
+    if (e != cudaSuccess) return e;
+    unsigned long long keep = ~0ull;
+    e = cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    if (e != cudaSuccess) {
+        cudaMemPoolDestroy(pool);
+        return e;
+    }
+    g_pools[dev] = pool;
+    *out = pool;
+    return cudaSuccess;
+}
+
+/* Stream-ordered allocation from the device's pool on the run's stream. */
+static cudaError_t pool_alloc(HydroRun2D *run, void **p, size_t bytes)
+{
+    cudaMemPool_t pool;
+    const cudaError_t e = device_pool(run->device, &pool);
+    if (e != cudaSuccess) return e;
+    return cudaMallocFromPoolAsync(p, bytes, pool, run->stream);
+}
+
+extern "C" int hydro_gpu_trim_device_memory(int device)
+{
+    cudaMemPool_t pool;
+    {
+        std::lock_guard<std::mutex> lock(g_pool_mutex);
+        auto it = g_pools.find(device);
+        if (it == g_pools.end()) return 0;
+        pool = it->second;
+    }
+    if (cudaSetDevice(device) != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess ||
+        cudaMemPoolTrimTo(pool, 0) != cudaSuccess) {
+        cudaGetLastError();
+        return -1;
+    }
+    return 0;
+}
+
 extern "C" int hydro_run2d_create(const HydroGrid2D *grid, const HydroGpuOptions *opt,
                                   HydroRun2D **out, HydroRunOutcome *oc)
 {
@@ -225,8 +288,10 @@ extern "C" int hydro_run2d_create(const HydroGrid2D *grid, const HydroGpuOptions
 
     /* 8 (U) + 10 (W) + 4 (snapshot) fields; the initial copy is separate */
     const size_t nfield = 22;
-    CK(cudaMalloc(&run->slab, nfield * run->ncell * run->elem), "cudaMalloc(state)");
-    if (run->fp32) CK(cudaMalloc(&run->stage_d, 4 * run->ncell * sizeof(double)), "cudaMalloc(staging)");
+    CK(pool_alloc(run, &run->slab, nfield * run->ncell * run->elem), "cudaMallocFromPoolAsync(state)");
+    if (run->fp32)
+        CK(pool_alloc(run, reinterpret_cast<void **>(&run->stage_d), 4 * run->ncell * sizeof(double)),
+           "cudaMallocFromPoolAsync(staging)");
     CK(cudaMalloc(&run->totals_d, 4 * sizeof(double)), "cudaMalloc(totals)");
     CK(cudaMalloc(&run->ctrl_d, sizeof(HydroStepControl)), "cudaMalloc(control)");
     CK(cudaMallocHost(&run->ctrl_h, sizeof(HydroStepControl)), "cudaMallocHost(control)");
@@ -303,7 +368,7 @@ extern "C" int hydro_run2d_upload(HydroRun2D *run, double *const W[4], double *c
         CK(cudaMemcpyAsync(fieldU(run, 1, q), u0[q], fbytes, cudaMemcpyDeviceToDevice, run->stream), "D2D U");
     if (keep_initial) {
         if (!run->init_slab) {
-            CK(cudaMalloc(&run->init_slab, 8 * fbytes), "cudaMalloc(initial state)");
+            CK(pool_alloc(run, &run->init_slab, 8 * fbytes), "cudaMallocFromPoolAsync(initial state)");
             for (int q = 0; q < 4; q++) {
                 run->init_U[q] = static_cast<char *>(run->init_slab) + q * fbytes;
                 run->init_W[q] = static_cast<char *>(run->init_slab) + (4 + q) * fbytes;
@@ -393,7 +458,7 @@ static int ensure_initial_copy(HydroRun2D *run, HydroRunOutcome *oc)
 {
     const size_t fbytes = run->ncell * run->elem;
     if (!run->init_slab) {
-        CK(cudaMalloc(&run->init_slab, 8 * fbytes), "cudaMalloc(initial state)");
+        CK(pool_alloc(run, &run->init_slab, 8 * fbytes), "cudaMallocFromPoolAsync(initial state)");
         for (int q = 0; q < 4; q++) {
             run->init_U[q] = static_cast<char *>(run->init_slab) + q * fbytes;
             run->init_W[q] = static_cast<char *>(run->init_slab) + (4 + q) * fbytes;
@@ -885,9 +950,13 @@ extern "C" void hydro_run2d_destroy(HydroRun2D *run)
     if (run->graph) cudaGraphExecDestroy(run->graph);
     for (auto &e : run->ev)
         if (e) cudaEventDestroy(e);
-    cudaFree(run->slab);
-    cudaFree(run->init_slab);
-    cudaFree(run->stage_d);
+    if (run->stream) {
+        /* back to the pool, in stream order (the stream is idle here) */
+        if (run->slab) cudaFreeAsync(run->slab, run->stream);
+        if (run->init_slab) cudaFreeAsync(run->init_slab, run->stream);
+        if (run->stage_d) cudaFreeAsync(run->stage_d, run->stream);
+        cudaStreamSynchronize(run->stream);
+    }
     cudaFree(run->totals_d);
     cudaFree(run->ctrl_d);
     if (run->ctrl_h) cudaFreeHost(run->ctrl_h);

@@ -398,6 +398,13 @@ int hydro_gpu_pointwise_eval(int device, int op, long long n, const double *gamm
 /* Number of visible CUDA devices (0 when none; never fails). */
 int hydro_gpu_device_count(void);
 
+/* The 2D runs take their device memory from a per-device stream-ordered
+ * pool that keeps what a finished run freed, so repeated launches do not
+ * map and unmap their state each call.  This hands the cached memory of
+ * `device` back to the driver (after the device is idle); 0 on success.
+ * No counterpart in the reference, which has no device memory. */
+int hydro_gpu_trim_device_memory(int device);
+
 /* Library version string. */
 const char *hydro_gpu_version(void);
 

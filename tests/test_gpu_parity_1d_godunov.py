@@ -163,3 +163,23 @@ def test_geometry_and_random_choice_against_oracle(gpu_available, oracle_mod, co
     # Paths without pow are bit-exact.
     assert np.all(rel_l1_1d(r.U, ref.U, p.g) <= REL_L1_TOL)
     assert np.all(rel_l1_1d(r.W, ref.W, p.g) <= REL_L1_TOL)
+
+
+@pytest.mark.parametrize("integrator,solver,limiter", [("godunov_first_order_1d", "riemann_solver_exact", "minmod"),
+                                                       ("muscl_hancock_1d", "riemann_solver_hllc", "van_leer")])
+def test_sod_against_the_compiled_reference(gpu_available, oracle_mod, integrator, solver, limiter):
+    """The Sod tube against the unmodified reference (serial build, compiled
+    on this machine from its staged sources): the whole padded state within
+    the parity tolerance (the exact solver's pow is glibc's there)."""
+    O = oracle_mod
+    if not O.reference_available():
+        pytest.skip("reference not compiled here (make -C oracle stage ref)")
+    p = O.sod_1d(400)
+    p.integrator, p.riemann_solver, p.slope_limiter = integrator, solver, limiter
+    ref = O.load("ref_serial").run_1d(p)
+    gpu = run1(p)
+    assert gpu.code == 0 and ref.rc == 0, gpu.message
+    assert gpu.num_steps == ref.num_steps
+    assert gpu.t == pytest.approx(ref.t, rel=1e-14)
+    assert np.all(rel_l1_1d(gpu.U, ref.U, p.g) <= REL_L1_TOL)
+    assert np.all(rel_l1_1d(gpu.W, ref.W, p.g) <= REL_L1_TOL)

@@ -195,3 +195,54 @@ def test_fp32_gravity_and_custom_rejection(gpu_available, oracle_mod):
     q = O.lid_driven_cavity(16, g=3, steps=4)
     r = run_gpu(q, options=H.default_options(precision=H.PRECISION_FP32))
     assert r.code != 0 and "FP64" in r.message
+
+
+# ----------------------------------------------------------- the reference itself
+
+@pytest.mark.parametrize("case", ["shear_layer", "point_blast", "four_quadrant", "godunov_periodic"])
+def test_against_the_compiled_reference(gpu_available, oracle_mod, case):
+    """The GPU run against the unmodified reference, compiled on this machine
+    from its staged sources (oracle/_ref), not only against the
+    restatement: interior state, step count and clock bit for bit."""
+    O = oracle_mod
+    if not O.reference_available():
+        pytest.skip("reference not compiled here (make -C oracle stage ref)")
+    if case == "shear_layer":
+        p = O.shear_layer(256, steps=60)
+    elif case == "point_blast":
+        p = O.point_blast(192, steps=80)
+    elif case == "four_quadrant":
+        p = O.four_quadrant(128, np.random.default_rng(4), steps=60)
+    else:
+        p = O.random_problem_2d(70, 50, 9, ("periodic",) * 4, "minmod", 30, smooth=True,
+                                integrator="godunov_first_order_2d")
+    ref = O.load("ref").run_2d(p)
+    gpu = run_gpu(p)
+    assert gpu.code == 0 and ref.rc == 0, (gpu.message, ref.message)
+    assert gpu.num_steps == ref.num_steps and gpu.t == ref.t and gpu.dt == ref.dt
+    g = p.g
+    if case == "four_quadrant":
+        # two-rarefaction faces take pow; glibc's misrounds ~0.1% of them
+        assert np.all(O.rel_l1(gpu.U, ref.U, g) <= REL_L1_TOL)
+    else:
+        assert np.array_equal(gpu.U[:, g:-g, g:-g].view(np.uint64), ref.U[:, g:-g, g:-g].view(np.uint64))
+        assert np.array_equal(gpu.W[:, g:-g, g:-g].view(np.uint64), ref.W[:, g:-g, g:-g].view(np.uint64))
+
+
+def test_repeated_launches_reuse_device_memory(gpu_available, oracle_mod):
+    """Consecutive launches take their state from the device memory the
+    previous one handed back to the library's pool (no fresh mapping each
+    call): results stay identical across calls, and after
+    hydro_gpu_trim_device_memory hands the cache back, the next call
+    allocates again and still agrees."""
+    O = oracle_mod
+    p = O.shear_layer(96, steps=25)
+    ref = O.load("oracle").run_2d(p)
+    outs = [run_gpu(p) for _ in range(3)]
+    assert H.library().hydro_gpu_trim_device_memory(0) == 0
+    outs.append(run_gpu(p))
+    for gpu in outs:
+        assert gpu.code == 0 and gpu.num_steps == ref.num_steps
+        assert np.array_equal(gpu.U, outs[0].U, equal_nan=True)
+        assert np.array_equal(gpu.W, outs[0].W, equal_nan=True)   # corners: NaN
+    assert_parity(p, outs[0], ref)
