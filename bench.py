@@ -774,16 +774,23 @@ def main() -> None:
     # ---- end to end through the drop-in call (host arrays in and out) ----
     # The System and parameter structs are set up outside the timed region, as
     # a program calling the reference API holds them; the timed region is the
-    # hydro_gpu_launch_simulation call: upload, steps, download.
+    # hydro_gpu_launch_simulation call: upload, steps, download.  Three calls
+    # from the same initial state (reloaded between calls, outside the timed
+    # region); the median is reported: the host side of the pageable copies
+    # varies from call to call (one download seen at 7 ms against 1.5 ms).
+    e2e_calls = []
     with H.Simulation2D(p.nx, p.ny, p.g, bounds, p.gamma, p.W, p.U, bc=p.bc,
                         slope_limiter=p.slope_limiter, cfl=p.cfl, tf=p.tf, max_steps=args.steps,
                         options=H.default_options(device=device, precision=prec)) as sim:
-        barrier(ws)
-        t0 = time.perf_counter()
-        code, msg, _, e2e_stats = sim.launch()
-        e2e_s = time.perf_counter() - t0
-    assert code == 0, msg
-    e2e_s = max_over_ranks(e2e_s, ws)
+        for _ in range(3):
+            sim.load(p.W, p.U)
+            barrier(ws)
+            t0 = time.perf_counter()
+            code, msg, _, stats_k = sim.launch()
+            secs = time.perf_counter() - t0
+            assert code == 0, msg
+            e2e_calls.append((max_over_ranks(secs, ws), stats_k))
+    e2e_s, e2e_stats = sorted(e2e_calls, key=lambda c: c[0])[1]
     e2e_value = ws * cells * args.steps / e2e_s
 
     # ---- the precision study's grid beside the headline: 8192^2 point blast ----
@@ -841,8 +848,9 @@ def main() -> None:
                 "h2d_bytes_per_step": e2e_stats["h2d_bytes"] / args.steps,
                 "d2h_bytes_per_step": e2e_stats["d2h_bytes"] / args.steps,
                 "seconds": e2e_s, "h2d_ms": e2e_stats["h2d_ms"], "d2h_ms": e2e_stats["d2h_ms"],
-                "note": "one hydro_gpu_launch_simulation call on host System arrays: upload, "
-                        "K steps, download (copies inside the timed call)"},
+                "calls_seconds": [c[0] for c in e2e_calls],
+                "note": "hydro_gpu_launch_simulation on host System arrays: upload, K steps, "
+                        "download (copies inside the timed call); median of 3 calls"},
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
     }
