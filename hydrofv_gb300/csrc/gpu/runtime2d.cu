@@ -28,6 +28,7 @@
 #include <new>
 #include <thread>
 #include <tuple>
+#include <vector>
 
 #include "gpu_bridge.h"
 #include "gpu_internal.h"
@@ -225,17 +226,84 @@ static cudaError_t pool_alloc(HydroRun2D *run, void **p, size_t bytes)
     return cudaMallocFromPoolAsync(p, bytes, pool, run->stream);
 }
 
+/*
+ * The per-run CUDA objects that do not depend on the grid -- the stream, the
+ * timing events, the device and pinned host control blocks and the totals
+ * buffer -- are kept per device when a run ends and handed to the next one
+ * (creating them, pinned host memory above all, took most of a drop-in
+ * call's ~2 ms of set-up).  At most kKeptRuns sets per device.
+ */
+struct RunResources {
+    cudaStream_t stream;
+    cudaEvent_t ev[6];
+    HydroStepControl *ctrl_d;
+    HydroStepControl *ctrl_h;
+    double *totals_d;
+};
+static constexpr size_t kKeptRuns = 4;
+static std::mutex g_res_mutex;
+static std::map<int, std::vector<RunResources>> g_res;
+
+static bool take_resources(HydroRun2D *run)
+{
+    std::lock_guard<std::mutex> lock(g_res_mutex);
+    auto &v = g_res[run->device];
+    if (v.empty()) return false;
+    const RunResources r = v.back();
+    v.pop_back();
+    run->stream = r.stream;
+    for (int k = 0; k < 6; k++) run->ev[k] = r.ev[k];
+    run->ctrl_d = r.ctrl_d;
+    run->ctrl_h = r.ctrl_h;
+    run->totals_d = r.totals_d;
+    return true;
+}
+
+/* Keep the run's resources for the next run (its stream is idle); false if
+ * they are incomplete or the device already keeps enough. */
+static bool keep_resources(HydroRun2D *run)
+{
+    if (!run->stream || !run->ctrl_d || !run->ctrl_h || !run->totals_d) return false;
+    for (auto e : run->ev)
+        if (!e) return false;
+    std::lock_guard<std::mutex> lock(g_res_mutex);
+    auto &v = g_res[run->device];
+    if (v.size() >= kKeptRuns) return false;
+    RunResources r;
+    r.stream = run->stream;
+    for (int k = 0; k < 6; k++) r.ev[k] = run->ev[k];
+    r.ctrl_d = run->ctrl_d;
+    r.ctrl_h = run->ctrl_h;
+    r.totals_d = run->totals_d;
+    v.push_back(r);
+    return true;
+}
+
 extern "C" int hydro_gpu_trim_device_memory(int device)
 {
-    cudaMemPool_t pool;
+    std::vector<RunResources> kept;
+    {
+        std::lock_guard<std::mutex> lock(g_res_mutex);
+        kept.swap(g_res[device]);
+    }
+    cudaMemPool_t pool = nullptr;
     {
         std::lock_guard<std::mutex> lock(g_pool_mutex);
         auto it = g_pools.find(device);
-        if (it == g_pools.end()) return 0;
-        pool = it->second;
+        if (it != g_pools.end()) pool = it->second;
     }
-    if (cudaSetDevice(device) != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess ||
-        cudaMemPoolTrimTo(pool, 0) != cudaSuccess) {
+    if (cudaSetDevice(device) != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) {
+        cudaGetLastError();
+        return -1;
+    }
+    for (auto &r : kept) {
+        for (auto e : r.ev) cudaEventDestroy(e);
+        cudaFree(r.totals_d);
+        cudaFree(r.ctrl_d);
+        cudaFreeHost(r.ctrl_h);
+        cudaStreamDestroy(r.stream);
+    }
+    if (pool && cudaMemPoolTrimTo(pool, 0) != cudaSuccess) {
         cudaGetLastError();
         return -1;
     }
@@ -283,8 +351,14 @@ extern "C" int hydro_run2d_create(const HydroGrid2D *grid, const HydroGpuOptions
     *out = run;
 
     CK(cudaSetDevice(run->device), "cudaSetDevice");
-    CK(cudaStreamCreateWithFlags(&run->stream, cudaStreamNonBlocking), "cudaStreamCreate");
-    for (auto &e : run->ev) CK(cudaEventCreate(&e), "cudaEventCreate");
+    if (!take_resources(run)) {
+        CK(cudaStreamCreateWithFlags(&run->stream, cudaStreamNonBlocking), "cudaStreamCreate");
+        for (auto &e : run->ev) CK(cudaEventCreate(&e), "cudaEventCreate");
+        CK(cudaMalloc(&run->totals_d, 4 * sizeof(double)), "cudaMalloc(totals)");
+        CK(cudaMalloc(&run->ctrl_d, sizeof(HydroStepControl)), "cudaMalloc(control)");
+        CK(cudaMallocHost(&run->ctrl_h, sizeof(HydroStepControl)), "cudaMallocHost(control)");
+    }
+    memset(run->ctrl_h, 0, sizeof(HydroStepControl));
 
     /* 8 (U) + 10 (W) + 4 (snapshot) fields; the initial copy is separate */
     const size_t nfield = 22;
@@ -292,10 +366,6 @@ extern "C" int hydro_run2d_create(const HydroGrid2D *grid, const HydroGpuOptions
     if (run->fp32)
         CK(pool_alloc(run, reinterpret_cast<void **>(&run->stage_d), 4 * run->ncell * sizeof(double)),
            "cudaMallocFromPoolAsync(staging)");
-    CK(cudaMalloc(&run->totals_d, 4 * sizeof(double)), "cudaMalloc(totals)");
-    CK(cudaMalloc(&run->ctrl_d, sizeof(HydroStepControl)), "cudaMalloc(control)");
-    CK(cudaMallocHost(&run->ctrl_h, sizeof(HydroStepControl)), "cudaMallocHost(control)");
-    memset(run->ctrl_h, 0, sizeof(HydroStepControl));
     if (run->fp32) {
         carve<float>(run, run->args32);
         setup_args<float>(run, run->args32, grid, opt);
@@ -948,20 +1018,23 @@ extern "C" void hydro_run2d_destroy(HydroRun2D *run)
     if (run->snap_ready) cudaEventDestroy(run->snap_ready);
     if (run->snap_copied) cudaEventDestroy(run->snap_copied);
     if (run->graph) cudaGraphExecDestroy(run->graph);
-    for (auto &e : run->ev)
-        if (e) cudaEventDestroy(e);
+    bool idle = false;
     if (run->stream) {
         /* back to the pool, in stream order (the stream is idle here) */
         if (run->slab) cudaFreeAsync(run->slab, run->stream);
         if (run->init_slab) cudaFreeAsync(run->init_slab, run->stream);
         if (run->stage_d) cudaFreeAsync(run->stage_d, run->stream);
-        cudaStreamSynchronize(run->stream);
+        idle = cudaStreamSynchronize(run->stream) == cudaSuccess;
     }
-    cudaFree(run->totals_d);
-    cudaFree(run->ctrl_d);
-    if (run->ctrl_h) cudaFreeHost(run->ctrl_h);
     if (run->snap_h) cudaFreeHost(run->snap_h);
-    if (run->stream) cudaStreamDestroy(run->stream);
+    if (!(idle && cudaGetLastError() == cudaSuccess && keep_resources(run))) {
+        for (auto &e : run->ev)
+            if (e) cudaEventDestroy(e);
+        cudaFree(run->totals_d);
+        cudaFree(run->ctrl_d);
+        if (run->ctrl_h) cudaFreeHost(run->ctrl_h);
+        if (run->stream) cudaStreamDestroy(run->stream);
+    }
     delete run;
 }
 

@@ -13,6 +13,7 @@
  * There is no CPU fallback: a CUDA failure is reported as an error.
  */
 #include <math.h>
+#include <pthread.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -94,6 +95,29 @@ static void bisection_warnings(const Settings *settings, const HydroRunOutcome *
         }
 }
 
+/* HYDRO_GPU_TRACE set (to anything but "0"): a 2D launch prints the host
+ * wall time of each of its phases to stderr (set-up, upload, begin,
+ * stepping, download, teardown), so a caller can see where a drop-in call's
+ * time goes beyond the stepping. */
+static int trace_enabled(void)
+{
+    static int cached = -1;
+    if (cached < 0)
+    {
+        const char *v = getenv("HYDRO_GPU_TRACE");
+        cached = (v && v[0] && strcmp(v, "0") != 0) ? 1 : 0;
+    }
+    return cached;
+}
+
+static void trace_phase(const char *what, double *t_last)
+{
+    if (!trace_enabled()) return;
+    const double now = hydro_get_current_time();
+    fprintf(stderr, "hydro_gpu: %-9s %9.3f ms\n", what, (now - *t_last) * 1e3);
+    *t_last = now;
+}
+
 static ErrorStatus outcome_error(const HydroRunOutcome *oc)
 {
     switch (oc->kind)
@@ -114,11 +138,61 @@ static ErrorStatus outcome_error(const HydroRunOutcome *oc)
 
 /* -------------------------------------------------------- 2D set-up */
 
+/* 1 if a[lo, hi) all equal v: branch-free blocks the compiler vectorises,
+ * with an early exit between blocks. */
+static int all_equal(const double *a, long long lo, long long hi, double v)
+{
+    for (long long b = lo; b < hi; b += 4096)
+    {
+        const long long e = (b + 4096 < hi) ? b + 4096 : hi;
+        int bad = 0;
+        for (long long k = b; k < e; k++) bad |= (a[k] != v);
+        if (bad) return 0;
+    }
+    return 1;
+}
+
+typedef struct UniformPart
+{
+    const double *a;
+    long long lo, hi;
+    int ok;
+} UniformPart;
+
+static void *uniform_part(void *arg)
+{
+    UniformPart *p = arg;
+    p->ok = all_equal(p->a, p->lo, p->hi, p->a[0]);
+    return NULL;
+}
+
+/* 1 if every a[k] equals a[0].  The 2D grids' volumes are one array per
+ * cell (33.7 MB at 2048^2), so large arrays are split over a few host
+ * threads: the scan was most of a drop-in call's set-up time. */
 static int uniform(const double *a, long long n)
 {
-    for (long long k = 1; k < n; k++)
-        if (a[k] != a[0]) return 0;
-    return 1;
+    enum { PARTS = 8 };
+    if (n < (1LL << 20)) return all_equal(a, 1, n, a[0]);
+    UniformPart part[PARTS];
+    pthread_t tid[PARTS];
+    int started[PARTS];
+    for (int k = 0; k < PARTS; k++)
+    {
+        part[k].a = a;
+        part[k].lo = n * k / PARTS;
+        part[k].hi = n * (k + 1) / PARTS;
+        part[k].ok = 1;
+        started[k] = (k > 0) && pthread_create(&tid[k], NULL, uniform_part, &part[k]) == 0;
+        if (k > 0 && !started[k]) uniform_part(&part[k]);
+    }
+    uniform_part(&part[0]);
+    int ok = part[0].ok;
+    for (int k = 1; k < PARTS; k++)
+    {
+        if (started[k]) pthread_join(tid[k], NULL);
+        ok &= part[k].ok;
+    }
+    return ok;
 }
 
 /* Checks shared by the 2D integrators; fills grid. */
@@ -284,10 +358,14 @@ static ErrorStatus run_2d(
     bctx.system = *s;
     bctx.status = make_success_error_status();
 
+    double t_phase = t_start;
     int rc = hydro_run2d_create(&grid, opt, &run, &oc);
     if (rc == 0 && has_custom(&grid)) rc = hydro_run2d_set_host_bc(run, host_bc_cb, &bctx, &oc);
+    trace_phase("set-up", &t_phase);
     if (rc == 0) rc = hydro_run2d_upload(run, W, U, 0, &oc);
+    trace_phase("upload", &t_phase);
     if (rc == 0) rc = hydro_run2d_begin(run, &params, simp->tf, opt->max_steps, sp->store_count_, &oc);
+    trace_phase("begin", &t_phase);
     int advanced = 0;
     HydroRunOutcome aoc;
     memset(&aoc, 0, sizeof aoc);
@@ -297,6 +375,7 @@ static ErrorStatus run_2d(
         rc = hydro_run2d_advance(run, snapshot_cb, &ctx, &aoc, NULL);
         if (rc != 0) oc = aoc;
     }
+    trace_phase("stepping", &t_phase);
     /* Whatever happened, hand back the last consistent state. */
     if (advanced)
     {
@@ -314,8 +393,10 @@ static ErrorStatus run_2d(
             }
         }
     }
+    trace_phase("download", &t_phase);
     if (stats && run) hydro_run2d_stats(run, stats);
     hydro_run2d_destroy(run);
+    trace_phase("teardown", &t_phase);
     if (!settings->no_progress_bar) update_progress_bar(&bar, status->t, true);
     if (stats) stats->total_ms = (hydro_get_current_time() - t_start) * 1e3;
 

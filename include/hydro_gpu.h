@@ -399,10 +399,11 @@ int hydro_gpu_pointwise_eval(int device, int op, long long n, const double *gamm
 int hydro_gpu_device_count(void);
 
 /* The 2D runs take their device memory from a per-device stream-ordered
- * pool that keeps what a finished run freed, so repeated launches do not
- * map and unmap their state each call.  This hands the cached memory of
- * `device` back to the driver (after the device is idle); 0 on success.
- * No counterpart in the reference, which has no device memory. */
+ * pool that keeps what a finished run freed, and keep a few runs' streams,
+ * events and pinned control blocks, so repeated launches neither map and
+ * unmap their state nor create those objects each call.  This hands all of
+ * it for `device` back to the driver (after the device is idle); 0 on
+ * success.  No counterpart in the reference, which has no device memory. */
 int hydro_gpu_trim_device_memory(int device);
 
 /* Library version string. */

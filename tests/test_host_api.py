@@ -319,3 +319,28 @@ def test_exact_solver_verbose_warnings_like_the_reference(hydro_lib, oracle_mod,
             assert _bisection_warnings(capfd.readouterr().err) == list(range(500, 5001, 500))
         finally:
             ref.lib.ref_set_verbose(0)
+
+
+@pytest.mark.parametrize("side,where", [(40, "last"), (1100, "first"), (1100, "middle"), (1100, "last")])
+def test_non_uniform_volumes_are_rejected_before_any_gpu_work(hydro_lib, side, where):
+    """The 2D path needs the uniform face areas and cell volumes system_init
+    sets; a System whose volume array was changed in any cell is refused with
+    NOT_IMPLEMENTED_ERROR on the host (grids above 2^20 cells are scanned by
+    several host threads), and an untouched one passes the check (it then
+    fails only where no GPU is visible, with the CUDA error)."""
+    from hydrofv_gb300.problems import shear_layer
+    p = shear_layer(side, steps=1)
+    with H.Simulation2D(p.nx, p.ny, p.g, (0, 1, 0, 1), p.gamma, p.W, p.U, bc=p.bc,
+                        slope_limiter=p.slope_limiter, cfl=p.cfl, tf=p.tf, max_steps=1) as sim:
+        n = (p.nx + 2 * p.g) * (p.ny + 2 * p.g)
+        vol = np.ctypeslib.as_array(sim.h.s.volume_, shape=(n,))
+        k = {"first": 1, "middle": n // 2 + 17, "last": n - 1}[where]
+        keep = vol[k]
+        vol[k] = keep * (1.0 + 1e-15)
+        code, msg, _, _ = sim.launch()
+        assert code == 6, msg   # NOT_IMPLEMENTED_ERROR
+        assert "uniform face areas and cell volumes" in msg
+        vol[k] = keep
+        if H.device_count() == 0:
+            code, msg, _, _ = sim.launch()
+            assert code != 6 and "CUDA" in msg, msg
