@@ -20,6 +20,11 @@ roofline: the step kernel against measured HBM bandwidth (64 algorithmic
   pipe roof measured by hydro_gpu_calibrate, which is the binding one.
 cpu_baseline: the CPU implementation of the same step on this host's cores,
   on a bounded sample (the first few steps of the same grid).
+forms: the FP32 form of the same steps (L1 error against FP64, its own
+  rooflines), and the other configurations, each at its own size and step
+  count: the 8192^2 point blast (K steps, FP64 and FP32), the 256-instance
+  four-quadrant ensemble (500 steps, FP64 and FP32) and the 1024^2 adjoint
+  (400 steps, backward cost, one dot-product and finite-difference check).
 
 Other workloads (--workload): point_blast (8192^2 with --size 8192), ensemble
 (256 four-quadrant grids), adjoint (1024^2 shear layer), snapshots, and sod:
@@ -289,6 +294,101 @@ def blast_leg(args, H, device: int, ws: int) -> dict:
                      "cfl": p.cfl, "boundaries": p.bc[0], "steps_per_run": args.steps,
                      "l2": "state larger than the 129 MB L2 (no flush needed)"}
     return out
+
+
+ENSEMBLE_STEPS = 500
+ADJOINT_SIDE, ADJOINT_STEPS, ADJOINT_K = 1024, 400, 50
+
+
+def ensemble_leg(args, H, device: int, ws: int) -> dict:
+    """The batched-ensemble configuration beside the headline: 256
+    four-quadrant problems (sides log-uniform in [128, 1024], minmod,
+    transmissive, CFL 0.8, per-instance dt), 500 steps each, one launch per
+    step for the whole batch, FP64 and FP32 on the same instances (W
+    warm-up steps and a rewind first); relative L1 of the FP32 state against
+    FP64 over all instances."""
+    from hydrofv_gb300.problems import four_quadrant_ensemble
+    probs = four_quadrant_ensemble(count=256, steps=ENSEMBLE_STEPS)
+    cells = sum(p.nx * p.ny for p in probs)
+    out, finals = {}, {}
+    for name, prec in (("fp64", H.PRECISION_FP64), ("fp32", H.PRECISION_FP32)):
+        with H.Batch2D(probs, options=H.default_options(device=device, precision=prec)) as b:
+            b.advance(args.warmup)
+            b.restart()
+            l0 = b.kernel_launches()
+            barrier(ws)
+            clk = ClockSampler(device)
+            with clk:
+                st, ms = b.advance(ENSEMBLE_STEPS)
+            launches = b.kernel_launches() - l0
+            assert all(x[0] == ENSEMBLE_STEPS for x in st)
+            finals[name] = b.download()
+        ms = max_over_ranks(ms, ws)
+        out[name] = {"value": ws * cells * ENSEMBLE_STEPS / (ms * 1e-3), "ms_per_step": ms / ENSEMBLE_STEPS,
+                     "gpu_launches": int(launches), "clocks": clk.summary()}
+    num = np.zeros(4)
+    den = np.zeros(4)
+    for (W64, _), (W32, _), p in zip(finals["fp64"], finals["fp32"], probs):
+        g = p.g
+        num += np.abs(W32[:, g:-g, g:-g] - W64[:, g:-g, g:-g]).sum(axis=(1, 2))
+        den += np.abs(W64[:, g:-g, g:-g]).sum(axis=(1, 2))
+    l1 = num / den
+    out["fp32"]["speedup_vs_fp64"] = out["fp32"]["value"] / out["fp64"]["value"]
+    out["fp32"]["rel_l1_vs_fp64"] = {"density": float(l1[0]), "velocity_x": float(l1[1]),
+                                     "velocity_y": float(l1[2]), "pressure": float(l1[3])}
+    out["config"] = {"workload": "ensemble_256x_four_quadrant", "instances": 256, "interior_cells": cells,
+                     "limiter": "minmod", "cfl": 0.8, "boundaries": "transmissive",
+                     "steps_per_instance": ENSEMBLE_STEPS}
+    return out
+
+
+def adjoint_leg(args, H, device: int) -> dict:
+    """The discrete-adjoint configuration beside the headline: the 1024^2
+    shear layer (MC, periodic), 400 steps, a checkpoint every 50; forward
+    pass, then dJ/dW0 for J = sum_{x > 0.5} rho^2 V (segment recomputation +
+    reverse sweep), device times; one seeded direction in (rho, p) checked
+    by the dot-product test against the tangent-linear model and by central
+    differences (eps 1e-6) of the branch-frozen replay."""
+    import math
+    from hydrofv_gb300.problems import right_half_density_squared, shear_layer
+    p = shear_layer(ADJOINT_SIDE, steps=ADJOINT_STEPS)
+    interior = np.zeros(p.W.shape[1:], dtype=bool)
+    interior[p.g:-p.g, p.g:-p.g] = True
+
+    def dot(a, b):
+        return math.fsum((a[:, interior] * b[:, interior]).ravel())
+
+    with H.Adjoint2D(p, steps=ADJOINT_STEPS, checkpoint_every=ADJOINT_K,
+                     options=H.default_options(device=device)) as ad:
+        WN = ad.forward()                      # warm-up pass
+        J, seed = right_half_density_squared(p, WN)
+        ad.backward(seed)
+        WN = ad.forward()
+        st_f = ad.stats()
+        J, seed = right_half_density_squared(p, WN)
+        grad = ad.backward(seed)
+        st = ad.stats()
+        back_ms = st["recompute_ms"] + st["vjp_ms"]
+        rng = np.random.default_rng(2024)
+        d = np.zeros_like(p.W)
+        d[0] = rng.normal(size=d[0].shape) * np.abs(p.W[0])
+        d[3] = rng.normal(size=d[3].shape) * np.abs(p.W[3])
+        d[:, ~interior] = 0.0
+        an = dot(grad, d)
+        _, dwN = ad.tangent(d)
+        eps = 1e-6
+        jp = right_half_density_squared(p, ad.replay_frozen(p.W + eps * d))[0]
+        jm = right_half_density_squared(p, ad.replay_frozen(p.W - eps * d))[0]
+    cells = p.nx * p.ny
+    return {"forward_ms": st_f["forward_ms"],
+            "forward_cell_updates_per_s": cells * ADJOINT_STEPS / (st_f["forward_ms"] * 1e-3),
+            "backward_ms": back_ms, "backward_vs_forward": back_ms / st_f["forward_ms"],
+            "recompute_mismatches": st["recompute_mismatches"],
+            "dot_product_rel": abs(dot(seed, dwN) - an) / abs(an),
+            "fd_frozen_rel": abs((jp - jm) / (2 * eps) - an) / abs(an), "eps": eps,
+            "config": {"workload": f"adjoint_shear_layer_{ADJOINT_SIDE}x{ADJOINT_SIDE}_mc_fp64",
+                       "steps": ADJOINT_STEPS, "checkpoint_every": ADJOINT_K,
+                       "objective": "sum_{x>0.5} rho^2 V at step N", "directions": 1}}
 
 
 def run_reference_arm(args) -> None:
@@ -669,7 +769,8 @@ def main() -> None:
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-blast", action="store_true",
-                    help="leave out the 8192^2 point-blast leg of the default line (profiling runs)")
+                    help="leave out the other configurations of the default line (the 8192^2 point "
+                         "blast, the 256-instance ensemble and the 1024^2 adjoint; profiling runs)")
     ap.add_argument("--size", type=int, default=N_SIDE,
                     help="grid side (the headline workload is 2048; smaller sizes are for profiling)")
     ap.add_argument("--precision", default="fp64", choices=["fp64", "fp32"],
@@ -794,10 +895,13 @@ def main() -> None:
     e2e_s, e2e_stats = sorted(e2e_calls, key=lambda c: c[0])[len(e2e_calls) // 2]
     e2e_value = ws * cells * args.steps / e2e_s
 
-    # ---- the precision study's grid beside the headline: 8192^2 point blast ----
-    blast = None
+    # ---- the other configurations beside the headline: the precision study's
+    #      8192^2 point blast, the 256-instance ensemble, the 1024^2 adjoint ----
+    blast = ensemble = adjoint = None
     if args.workload == "shear_layer" and not args.no_blast:
         blast = blast_leg(args, H, device, ws)
+        ensemble = ensemble_leg(args, H, device, ws)
+        adjoint = adjoint_leg(args, H, device)
 
     if rank != 0:
         return
@@ -857,6 +961,8 @@ def main() -> None:
     }
     if blast is not None:
         line["forms"]["point_blast_8192"] = blast
+        line["forms"]["ensemble_256"] = ensemble
+        line["forms"]["adjoint_1024"] = adjoint
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_sample(args.steps)
     print(json.dumps(line))

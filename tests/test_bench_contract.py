@@ -72,6 +72,12 @@ def test_gpu_arm_line(gpu_available, tmp_path):
     assert blast["fp64"]["value"] > 0 and blast["fp32"]["value"] > 0
     assert set(blast["fp32"]["rel_l1_vs_fp64"]) == {"density", "velocity_x", "velocity_y", "pressure"}
     assert blast["fp32"]["rel_l1_vs_fp64"]["density"] < 1e-4
+    ens = forms["ensemble_256"]
+    assert ens["fp64"]["value"] > 0 and ens["fp32"]["speedup_vs_fp64"] > 1.7
+    assert ens["fp32"]["rel_l1_vs_fp64"]["density"] < 1e-4
+    adj = forms["adjoint_1024"]
+    assert adj["backward_vs_forward"] <= 3.0 and adj["recompute_mismatches"] == 0
+    assert adj["dot_product_rel"] < 1e-11 and adj["fd_frozen_rel"] < 1e-6
     # the reference arm reports the same workload under the same config
     r = _run(["--impl", "reference", "--size", "256", "--steps", "5", "--warmup", "3"], tmp_path)
     assert r["config"] == d["config"] and r["warmup"] == d["warmup"] and r["steps"] == d["steps"]
