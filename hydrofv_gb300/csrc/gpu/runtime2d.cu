@@ -93,6 +93,7 @@ struct HydroRun2D {
     int custom_mask = 0;              /* bit s: side s (x_min, x_max, y_min, y_max) is custom */
     bool begun = false;
     bool have_initial = false;
+    bool pooled = true;               /* state memory from the device's pool (else cudaMalloc) */
     /* statistics */
     double h2d_ms = 0, step_ms = 0, d2h_ms = 0;
     long long step_launches = 0, kernel_launches = 0;
@@ -217,9 +218,18 @@ static cudaError_t device_pool(int dev, cudaMemPool_t *out)
     return cudaSuccess;
 }
 
-/* Stream-ordered allocation from the device's pool on the run's stream. */
+/* Stream-ordered allocation from the device's pool on the run's stream; on a
+ * device without memory pools, plain cudaMalloc (run->pooled = false, and
+ * the run's teardown frees with cudaFree). */
 static cudaError_t pool_alloc(HydroRun2D *run, void **p, size_t bytes)
 {
+    int supported = 0;
+    if (cudaDeviceGetAttribute(&supported, cudaDevAttrMemoryPoolsSupported, run->device) != cudaSuccess ||
+        !supported) {
+        cudaGetLastError();
+        run->pooled = false;
+        return cudaMalloc(p, bytes);
+    }
     cudaMemPool_t pool;
     const cudaError_t e = device_pool(run->device, &pool);
     if (e != cudaSuccess) return e;
@@ -1021,9 +1031,11 @@ extern "C" void hydro_run2d_destroy(HydroRun2D *run)
     bool idle = false;
     if (run->stream) {
         /* back to the pool, in stream order (the stream is idle here) */
-        if (run->slab) cudaFreeAsync(run->slab, run->stream);
-        if (run->init_slab) cudaFreeAsync(run->init_slab, run->stream);
-        if (run->stage_d) cudaFreeAsync(run->stage_d, run->stream);
+        for (void *m : { run->slab, run->init_slab, static_cast<void *>(run->stage_d) }) {
+            if (!m) continue;
+            if (run->pooled) cudaFreeAsync(m, run->stream);
+            else cudaFree(m);
+        }
         idle = cudaStreamSynchronize(run->stream) == cudaSuccess;
     }
     if (run->snap_h) cudaFreeHost(run->snap_h);
