@@ -246,3 +246,30 @@ def test_repeated_launches_reuse_device_memory(gpu_available, oracle_mod):
         assert np.array_equal(gpu.U, outs[0].U, equal_nan=True)
         assert np.array_equal(gpu.W, outs[0].W, equal_nan=True)   # corners: NaN
     assert_parity(p, outs[0], ref)
+
+
+def test_concurrent_launches_from_two_host_threads(gpu_available, oracle_mod):
+    """Two host threads calling the drop-in at once (ctypes releases the GIL
+    for the call) on different Systems: each run takes its own stream,
+    control blocks and pool memory, and both results equal the sequential
+    ones bit for bit."""
+    import threading
+    O = oracle_mod
+    probs = [O.shear_layer(160, steps=30), O.point_blast(144, steps=40)]
+    seq = [run_gpu(p) for p in probs]
+    out = [None, None]
+
+    def work(k):
+        out[k] = [run_gpu(probs[k]) for _ in range(3)]
+
+    threads = [threading.Thread(target=work, args=(k,)) for k in range(2)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    for k in range(2):
+        for r in out[k]:
+            assert r.code == 0, r.message
+            assert r.num_steps == seq[k].num_steps and r.t == seq[k].t
+            assert np.array_equal(r.U, seq[k].U, equal_nan=True)
+            assert np.array_equal(r.W, seq[k].W, equal_nan=True)
