@@ -273,3 +273,30 @@ def test_concurrent_launches_from_two_host_threads(gpu_available, oracle_mod):
             assert r.num_steps == seq[k].num_steps and r.t == seq[k].t
             assert np.array_equal(r.U, seq[k].U, equal_nan=True)
             assert np.array_equal(r.W, seq[k].W, equal_nan=True)
+
+
+@pytest.mark.parametrize("g", [3, 4])
+@pytest.mark.parametrize("limiter", ["minmod", "van_leer", "monotonized_central"])
+def test_wider_ghost_layers(gpu_available, oracle_mod, g, limiter):
+    """More ghost layers than MUSCL-Hancock needs (the reference allows any
+    G >= 2): the boundary remap of every built-in side and the one-sided
+    update of the first ghost layer at G = 3 and 4."""
+    O = oracle_mod
+    p = O.random_problem_2d(37, 29, 5 + g, ("reflective", "transmissive", "periodic", "periodic"),
+                            limiter, 15, g=g, smooth=True)
+    ref = O.load("oracle").run_2d(p)
+    gpu = run_gpu(p)
+    assert_parity(p, gpu, ref)
+
+
+@pytest.mark.parametrize("nx", [125, 126, 127, 252, 253])
+def test_strip_edges(gpu_available, oracle_mod, nx):
+    """Grid widths around the step kernel's strip width (126 interior
+    columns per CTA): a last strip of one, two or no extra columns, with a
+    short grid so the row chunks are ragged too."""
+    O = oracle_mod
+    p = O.random_problem_2d(nx, 21, nx, ("transmissive", "reflective", "none", "reflective"),
+                            "monotonized_central", 12, smooth=True)
+    ref = O.load("oracle").run_2d(p)
+    gpu = run_gpu(p)
+    assert_parity(p, gpu, ref)
