@@ -37,7 +37,9 @@ CUDA_SOURCES = [
     ("gpu/mh2d_lim_vanleer.cu", ["--fmad=false"]),
     ("gpu/mh2d_lim_mc.cu", ["--fmad=false"]),
     ("gpu/mh2d_lim_first_order.cu", ["--fmad=false"]),
-    ("gpu/mh2d_fp32.cu", []),
+    # the FP32 state form: approximate FP32 divide and square root (at most
+    # 2 ulp); the FP64 translation units are untouched
+    ("gpu/mh2d_fp32.cu", ["-prec-div=false", "-prec-sqrt=false"]),
     ("gpu/runtime2d.cu", []),
     ("gpu/runtime_batch.cu", []),
     ("gpu/host_numerics.cu", ["--fmad=false"]),

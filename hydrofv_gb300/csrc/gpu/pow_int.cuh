@@ -179,10 +179,15 @@ static __device__ __noinline__ double pow_dev(double x, double y)
 }  // namespace fx
 
 /* pow as the kernels use it: the integer form on the device for double
- * (the non-template overload), the library pow for every other type and on
- * the host. */
+ * (the non-template overload), the hardware exp2/log2 form (__powf) on the
+ * device for float -- the FP32 state form, whose other divides and square
+ * roots are approximate too --, the library pow on the host. */
 template <class R>
 FXHD R pw(R x, R y) { return pow(x, y); }
+
+#if defined(__CUDA_ARCH__)
+FXHD float pw(float x, float y) { return __powf(x, y); }
+#endif
 
 FXHD double pw(double x, double y)
 {
