@@ -288,12 +288,16 @@ __device__ __noinline__ void vacuum_flux_dev(const GasConst<R> &c, R rl, R ul, R
 
 /*
  * Solve faces 0..nF-1 of the batch in sm.FL / sm.FR (normal velocity in
- * slot 1) with the HLLC flux, as three dense passes over the CTA:
+ * slot 1) with the HLLC flux.  FP64: three dense passes over the CTA:
  * classify (sound speeds, vacuum test, guess regime), the expensive guesses
  * on compacted lists (two-rarefaction: three pow; two-shock: five divides
  * and two square roots), and the finish (wave speeds, S*, region flux).
  * Compaction keeps lanes busy where neighbouring faces fall into different
- * regimes, which the one-face-per-thread form serialises.  FP64: the
+ * regimes, which the one-face-per-thread form serialises.  FP32: one pass,
+ * one face per thread.  Its guesses are a few approximate operations, and
+ * the passes' shared-memory round trips and barriers cost more than the
+ * divergence they avoid (2048^2 shear layer 14.5 -> 15.1 G cell-updates/s,
+ * 8192^2 point blast 24.9 -> 27.6 G, the same results).  FP64: the
  * face's update term (flux * dt) * area replaces the left state in sm.FL
  * (faces [0, nXf) are x faces, area Ax, the rest y faces, Ay).  Both cells
  * of a face add or subtract this one product, so it is formed once per face;
@@ -309,6 +313,18 @@ __device__ __forceinline__ int solve_faces(Mh2dShared<R, NT> &sm, const GasConst
 {
     const int tid = threadIdx.x;
     int err = DEV_OK;
+    if constexpr (sizeof(R) == 4 && !TAPE) {
+        for (int f = tid; f < nF; f += NT) {
+            R F[4];
+            const int rc = hllc_flux_2d(gas, sm.FL[0][f], sm.FL[1][f], sm.FL[2][f], sm.FL[3][f],
+                                        sm.FR[0][f], sm.FR[1][f], sm.FR[2][f], sm.FR[3][f], F);
+            if (rc) err = rc;
+#pragma unroll
+            for (int q = 0; q < 4; q++) sm.FL[q][f] = F[q];
+        }
+        __syncthreads();
+        return err;
+    }
     for (int f = tid; f < nF; f += NT) {
         R aL, aR, ppv;
         const int reg = hllc_classify(gas, sm.FL[0][f], sm.FL[1][f], sm.FL[3][f],
