@@ -49,10 +49,11 @@
 
 /* Threads per 2D step CTA (a strip of threads - 2 interior columns) and the
  * CTAs per SM each state precision is compiled for (launch bounds).  FP64:
- * 4 CTAs of 128 threads (128 registers); FP32: 8 CTAs of 128 (64 registers,
- * a few spills; the FP32 form is latency bound, and at 8 per SM the 1088
- * work items of a 2048^2 grid run in one wave: 7.4 -> 10.5 G
- * cell-updates/s). */
+ * 4 CTAs of 128 threads (128 registers); FP32: 7 CTAs of 128 (72
+ * registers).  Measured with the one-pass FP32 face solve (2048^2 shear
+ * layer / 8192^2 point blast / 256-grid ensemble, G cell-updates/s): 8 CTAs
+ * 15.05 / 27.5 / 20.1, 7 CTAs 15.19 / 28.6 / 21.35, 6 CTAs 15.7 / 27.7 /
+ * 20.4. */
 #ifndef MH2D_THREADS_FP64
 #define MH2D_THREADS_FP64 128
 #endif
@@ -63,7 +64,7 @@
 #define MH2D_THREADS_FP32 128
 #endif
 #ifndef MH2D_CTAS_FP32
-#define MH2D_CTAS_FP32 8
+#define MH2D_CTAS_FP32 7
 #endif
 
 namespace hydro {
