@@ -555,6 +555,11 @@ __device__ __forceinline__ void mh2d_item(const Mh2dArgs<R> &a, Mh2dShared<R, NT
      * solve (2048^2 shear layer: 1276 -> 1292 M cell-updates/s).  FP32 keeps
      * them in registers (11.73 against 11.65 G in shared memory). */
     constexpr bool CARRY_SMEM = sizeof(R) == 8;
+    /* FP32 (no tape): each interior thread also solves the y face above its
+     * cell itself, from the two states it holds in registers, so y faces
+     * never pass through shared memory; only the x faces, whose states come
+     * from two threads, are batched there */
+    constexpr bool YREG = sizeof(R) == 4 && !TAPE;
     R ytop[4], gbot[4];         /* FP32 */
     R tmp_lo[4], prev_hi[4];
     if (inner) recon_y(r_begin - 1, tmp_lo, prev_hi);
@@ -563,34 +568,45 @@ __device__ __forceinline__ void mh2d_item(const Mh2dArgs<R> &a, Mh2dShared<R, NT
     if constexpr (RING == 4) load_row_async(r_begin + 2);
     if (tid == 0) { sm.nT = 0; sm.nS = 0; }
     __syncthreads();
-    if (inner) {
-        recon_y(r_begin, tmp_lo, ytop);
-        if constexpr (CARRY_SMEM) {
-#pragma unroll
-            for (int q = 0; q < 4; q++) sm.ytop[q][tid] = ytop[q];
+    if constexpr (YREG) {
+        /* FP32: the face below the chunk is solved by its column's thread */
+        if (inner) {
+            recon_y(r_begin, tmp_lo, ytop);
+            const int rc = hllc_flux_2d(a.gas, prev_hi[0], prev_hi[1], prev_hi[2], prev_hi[3],
+                                        tmp_lo[0], tmp_lo[1], tmp_lo[2], tmp_lo[3], gbot);
+            if (rc) err = rc;
         }
+        __syncthreads();
+    } else {
+        if (inner) {
+            recon_y(r_begin, tmp_lo, ytop);
+            if constexpr (CARRY_SMEM) {
 #pragma unroll
-        for (int q = 0; q < 4; q++) { sm.FL[q][tid - 1] = prev_hi[q]; sm.FR[q][tid - 1] = tmp_lo[q]; }
-    }
-    __syncthreads();
-    {
-        int rc;
-        if constexpr (TAPE) {
-            const TapeCtx<R> tc{ a.tape, a.tape_plane, a.pitch, 0, -1, r_begin - 1, c0 };
-            rc = solve_faces<R, NT, true>(sm, a.gas, sw, 0, dtr, Ax, Ay, tc);
-        } else {
-            rc = solve_faces<R, NT>(sm, a.gas, sw, 0, dtr, Ax, Ay);
-        }
-        if (rc) err = rc;
-    }
-    if (inner) {
+                for (int q = 0; q < 4; q++) sm.ytop[q][tid] = ytop[q];
+            }
 #pragma unroll
-        for (int q = 0; q < 4; q++) {
-            if constexpr (CARRY_SMEM) sm.gbot[q][tid] = sm.FL[q][tid - 1];
-            else gbot[q] = sm.FL[q][tid - 1];
+            for (int q = 0; q < 4; q++) { sm.FL[q][tid - 1] = prev_hi[q]; sm.FR[q][tid - 1] = tmp_lo[q]; }
         }
+        __syncthreads();
+        {
+            int rc;
+            if constexpr (TAPE) {
+                const TapeCtx<R> tc{ a.tape, a.tape_plane, a.pitch, 0, -1, r_begin - 1, c0 };
+                rc = solve_faces<R, NT, true>(sm, a.gas, sw, 0, dtr, Ax, Ay, tc);
+            } else {
+                rc = solve_faces<R, NT>(sm, a.gas, sw, 0, dtr, Ax, Ay);
+            }
+            if (rc) err = rc;
+        }
+        if (inner) {
+#pragma unroll
+            for (int q = 0; q < 4; q++) {
+                if constexpr (CARRY_SMEM) sm.gbot[q][tid] = sm.FL[q][tid - 1];
+                else gbot[q] = sm.FL[q][tid - 1];
+            }
+        }
+        __syncthreads();
     }
-    __syncthreads();
 
     /* ---- march up the rows ---- */
     /* FP32: the item's maxima of a + |u| and a + |v| in float (a maximum of
@@ -622,22 +638,29 @@ __device__ __forceinline__ void mh2d_item(const Mh2dArgs<R> &a, Mh2dShared<R, NT
         __syncthreads();
 
         R nhi[4];
+        R gy[4];                /* FP32: the flux of the y face above this row */
         if (inner) {
             R nlo[4];
             recon_y(r + 1, nlo, nhi);
-            const int f = nX + tid - 1;
             /* the face above this row: low state carried from below, high
              * state from the cell above, whose own high state is carried to
              * the next row (FP64: now; FP32: after the update) */
+            if constexpr (YREG) {
+                const int rc = hllc_flux_2d(a.gas, ytop[0], ytop[1], ytop[2], ytop[3],
+                                            nlo[0], nlo[1], nlo[2], nlo[3], gy);
+                if (rc) err = rc;
+            } else {
+                const int f = nX + tid - 1;
 #pragma unroll
-            for (int q = 0; q < 4; q++) {
-                if constexpr (CARRY_SMEM) {
-                    sm.FL[q][f] = sm.ytop[q][tid];
-                    sm.ytop[q][tid] = nhi[q];
-                } else {
-                    sm.FL[q][f] = ytop[q];
+                for (int q = 0; q < 4; q++) {
+                    if constexpr (CARRY_SMEM) {
+                        sm.FL[q][f] = sm.ytop[q][tid];
+                        sm.ytop[q][tid] = nhi[q];
+                    } else {
+                        sm.FL[q][f] = ytop[q];
+                    }
+                    sm.FR[q][f] = nlo[q];
                 }
-                sm.FR[q][f] = nlo[q];
             }
         }
         if (x_slot) {
@@ -659,7 +682,7 @@ __device__ __forceinline__ void mh2d_item(const Mh2dArgs<R> &a, Mh2dShared<R, NT
                 const TapeCtx<R> tc{ a.tape, a.tape_plane, a.pitch, nX, r, r, c0 };
                 rc = solve_faces<R, NT, true>(sm, a.gas, nX + sw, nX, dtr, Ax, Ay, tc);
             } else {
-                rc = solve_faces<R, NT>(sm, a.gas, nX + sw, nX, dtr, Ax, Ay);
+                rc = solve_faces<R, NT>(sm, a.gas, YREG ? nX : nX + sw, nX, dtr, Ax, Ay);
             }
             if (rc) err = rc;
         }
@@ -669,7 +692,7 @@ __device__ __forceinline__ void mh2d_item(const Mh2dArgs<R> &a, Mh2dShared<R, NT
             const long long idx = rowbase + col;
             R gtop[4];
 #pragma unroll
-            for (int q = 0; q < 4; q++) gtop[q] = sm.FL[q][nX + tid - 1];
+            for (int q = 0; q < 4; q++) gtop[q] = YREG ? gy[q] : sm.FL[q][nX + tid - 1];
             R Un[4];
 #pragma unroll
             for (int q = 0; q < 4; q++) {
