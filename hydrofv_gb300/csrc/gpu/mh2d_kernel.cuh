@@ -295,7 +295,9 @@ __device__ __noinline__ void vacuum_flux_dev(const GasConst<R> &c, R rl, R ul, R
  * and two square roots), and the finish (wave speeds, S*, region flux).
  * Compaction keeps lanes busy where neighbouring faces fall into different
  * regimes, which the one-face-per-thread form serialises.  FP32: one pass,
- * one face per thread.  Its guesses are a few approximate operations, and
+ * one face per thread (the FP32 step batches only its x faces here; each y
+ * face is solved in registers by its column's thread).  Its guesses are a
+ * few approximate operations, and
  * the passes' shared-memory round trips and barriers cost more than the
  * divergence they avoid (2048^2 shear layer 14.5 -> 15.1 G cell-updates/s,
  * 8192^2 point blast 24.9 -> 27.6 G, the same results).  FP64: the
