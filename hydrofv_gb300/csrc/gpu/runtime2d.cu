@@ -291,6 +291,11 @@ static bool keep_resources(HydroRun2D *run)
 
 extern "C" int hydro_gpu_trim_device_memory(int device)
 {
+    /* the device first: on failure the kept sets stay where they are */
+    if (cudaSetDevice(device) != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) {
+        cudaGetLastError();
+        return -1;
+    }
     std::vector<RunResources> kept;
     {
         std::lock_guard<std::mutex> lock(g_res_mutex);
@@ -301,10 +306,6 @@ extern "C" int hydro_gpu_trim_device_memory(int device)
         std::lock_guard<std::mutex> lock(g_pool_mutex);
         auto it = g_pools.find(device);
         if (it != g_pools.end()) pool = it->second;
-    }
-    if (cudaSetDevice(device) != cudaSuccess || cudaDeviceSynchronize() != cudaSuccess) {
-        cudaGetLastError();
-        return -1;
     }
     for (auto &r : kept) {
         for (auto e : r.ev) cudaEventDestroy(e);
