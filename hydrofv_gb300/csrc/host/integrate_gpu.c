@@ -101,13 +101,10 @@ static void bisection_warnings(const Settings *settings, const HydroRunOutcome *
  * time goes beyond the stepping. */
 static int trace_enabled(void)
 {
-    static int cached = -1;
-    if (cached < 0)
-    {
-        const char *v = getenv("HYDRO_GPU_TRACE");
-        cached = (v && v[0] && strcmp(v, "0") != 0) ? 1 : 0;
-    }
-    return cached;
+    /* read on every phase (six per launch): no shared cache between the
+     * threads that may launch concurrently */
+    const char *v = getenv("HYDRO_GPU_TRACE");
+    return (v && v[0] && strcmp(v, "0") != 0) ? 1 : 0;
 }
 
 static void trace_phase(const char *what, double *t_last)
