@@ -307,3 +307,30 @@ def test_verbose_run_prints_the_bisection_warnings(gpu_available, oracle_mod, ca
             assert _bisection_warnings(capfd.readouterr().err) == got
         finally:
             ref.lib.ref_set_verbose(0)
+
+
+@pytest.mark.parametrize("case,cfl", [("point_blast", 3.0), ("shear_layer", 2.0)])
+def test_fp32_form_reports_the_hllc_error_and_returns_its_last_state(gpu_available, oracle_mod, case, cfl):
+    """The FP32 state form meets the same device error on an unstable CFL
+    number, from either of its face paths (x faces batched in shared memory,
+    y faces in registers): the reference's code and message come back, the
+    run stops at the failing step, and the arrays hold the FP32 state after
+    the completed steps, bit for bit what a clean FP32 run of that many steps
+    returns."""
+    O = oracle_mod
+    p = (O.point_blast if case == "point_blast" else O.shear_layer)(32, steps=80)
+    p.cfl = cfl
+    opt = H.default_options(precision=H.PRECISION_FP32)
+    gpu = H.run_2d(p.nx, p.ny, p.g, (p.x_min, p.x_max, p.y_min, p.y_max), p.gamma, p.W, p.U,
+                   bc=p.bc, integrator=p.integrator, riemann_solver=p.riemann_solver,
+                   slope_limiter=p.slope_limiter, cfl=p.cfl, tf=p.tf, max_steps=p.max_steps, options=opt)
+    assert gpu.code == VALUE_ERROR, (gpu.code, gpu.message)
+    assert HLLC_MSG in gpu.message
+    assert 0 < gpu.num_steps < p.max_steps
+    clean = H.run_2d(p.nx, p.ny, p.g, (p.x_min, p.x_max, p.y_min, p.y_max), p.gamma, p.W, p.U,
+                     bc=p.bc, integrator=p.integrator, riemann_solver=p.riemann_solver,
+                     slope_limiter=p.slope_limiter, cfl=p.cfl, tf=p.tf, max_steps=gpu.num_steps,
+                     options=opt)
+    assert clean.code == 0 and clean.num_steps == gpu.num_steps
+    assert clean.t == gpu.t
+    assert same_bits(gpu.U, clean.U) and same_bits(gpu.W, clean.W)
