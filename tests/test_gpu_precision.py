@@ -69,3 +69,39 @@ def test_fp32_session_matches_one_shot(gpu_available):
         W, U = s.download()
     # corner ghost cells are 0/0 = NaN, as in the reference
     assert np.array_equal(U, r.U, equal_nan=True) and np.array_equal(W, r.W, equal_nan=True)
+
+
+FP32_CASES = [
+    # (nx, ny, bc x_min/x_max/y_min/y_max, limiter, integrator): widths around the
+    # 126-column strip (one strip, a full strip plus a few columns, several)
+    (126, 40, ("periodic",) * 4, "monotonized_central", "muscl_hancock_2d"),
+    (130, 37, ("reflective", "transmissive", "periodic", "periodic"), "van_leer", "muscl_hancock_2d"),
+    (253, 64, ("transmissive",) * 4, "minmod", "muscl_hancock_2d"),
+    (61, 131, ("none", "reflective", "transmissive", "none"), "minmod", "muscl_hancock_2d"),
+    (127, 50, ("reflective",) * 4, "minmod", "godunov_first_order_2d"),
+    (300, 33, ("periodic", "periodic", "reflective", "none"), "monotonized_central", "godunov_first_order_2d"),
+]
+
+
+@pytest.mark.parametrize("nx,ny,bc,limiter,integrator", FP32_CASES,
+                         ids=[f"{c[0]}x{c[1]}-{c[3]}-{c[4]}" for c in FP32_CASES])
+def test_fp32_form_on_every_path(gpu_available, nx, ny, bc, limiter, integrator):
+    """The FP32 form's face paths (x faces batched in shared memory, each y
+    face in registers by its column's thread) on every limiter, first-order
+    Godunov, every boundary kind and ragged grid widths, against the FP64
+    drop-in on smooth states: the same number of steps, and the density
+    within the form's L1 bar."""
+    from hydrofv_gb300.problems import random_problem_2d
+    p = random_problem_2d(nx, ny, 7, bc, limiter, 40, g=2 if integrator == "muscl_hancock_2d" else 1,
+                          integrator=integrator, smooth=True)
+
+    def go(precision):
+        return H.run_2d(p.nx, p.ny, p.g, (p.x_min, p.x_max, p.y_min, p.y_max), p.gamma, p.W, p.U,
+                        bc=p.bc, integrator=p.integrator, slope_limiter=p.slope_limiter, cfl=p.cfl,
+                        tf=p.tf, max_steps=p.max_steps, options=H.default_options(precision=precision))
+    r64, r32 = go(H.PRECISION_FP64), go(H.PRECISION_FP32)
+    assert r64.code == 0 and r32.code == 0, (r64.message, r32.message)
+    assert r32.num_steps == r64.num_steps == p.max_steps
+    l1 = rel_l1(r32.W, r64.W, p.g)
+    assert l1[0] <= L1_DENSITY_TOL, l1
+    assert np.all(np.isfinite(r32.U[:, p.g:-p.g, p.g:-p.g]))
