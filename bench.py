@@ -190,8 +190,10 @@ def barrier(ws: int):
         dist.barrier()
 
 
-def cpu_sample(steps_hint: int, budget_s: float = 12.0) -> dict:
-    """Time the CPU implementation on a bounded sample of the same workload."""
+def cpu_sample(steps_hint: int, budget_s: float = 12.0, max_steps: int = 2000) -> dict:
+    """Time the CPU implementation on a bounded sample of the same workload:
+    the first steps of the same grid, as many as fit in about budget_s seconds
+    (at least steps_hint, at most max_steps)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     if not os.path.exists(os.path.join(O.BUILD, "liboracle.so")):
@@ -202,7 +204,7 @@ def cpu_sample(steps_hint: int, budget_s: float = 12.0) -> dict:
     p = O.shear_layer(N_SIDE, steps=1)
     r = backend.run_2d(p)                        # probe: one step
     per_step = max(r.seconds, 1e-3)
-    n = int(max(2, min(steps_hint, budget_s / per_step)))
+    n = int(min(max_steps, max(steps_hint, 2, budget_s / per_step)))
     p = O.shear_layer(N_SIDE, steps=n)
     r = backend.run_2d(p)
     value = N_SIDE * N_SIDE * n / r.seconds
