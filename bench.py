@@ -882,7 +882,9 @@ def main() -> None:
     # region); the median is reported: the host side of the pageable copies
     # varies from call to call (one download seen at 7 ms against 1.5 ms).
     e2e_calls = []
-    n_calls = 3 if cells * args.steps <= 2_000_000_000 else 1   # long runs: one call
+    # the median of five calls (every call's time is reported): the copies are
+    # pageable-host traffic, which a busy host can slow for a while
+    n_calls = 5 if cells * args.steps <= 2_000_000_000 else 1   # long runs: one call
     with H.Simulation2D(p.nx, p.ny, p.g, bounds, p.gamma, p.W, p.U, bc=p.bc,
                         slope_limiter=p.slope_limiter, cfl=p.cfl, tf=p.tf, max_steps=args.steps,
                         options=H.default_options(device=device, precision=prec)) as sim:
