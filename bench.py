@@ -190,10 +190,12 @@ def barrier(ws: int):
         dist.barrier()
 
 
-def cpu_sample(steps_hint: int, budget_s: float = 12.0, max_steps: int = 2000) -> dict:
+def cpu_sample(steps_hint: int, budget_s: float = 20.0, max_steps: int = 2000) -> dict:
     """Time the CPU implementation on a bounded sample of the same workload:
-    the first steps of the same grid, as many as fit in about budget_s seconds
-    (at least steps_hint, at most max_steps)."""
+    the first steps of the same grid, as many as the one-step probe says fit in
+    budget_s seconds (the probe's step includes the threads' start-up, so the
+    sample takes about two thirds of that), at least steps_hint, at most
+    max_steps."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle as O
     if not os.path.exists(os.path.join(O.BUILD, "liboracle.so")):
