@@ -216,28 +216,48 @@ def cpu_sample(steps_hint: int, budget_s: float = 20.0, max_steps: int = 2000) -
             "seconds": r.seconds, "steps": n}
 
 
-def fp_roofline(prec, value, fp64_tflops, fp32_tflops, H, workload="shear_layer") -> dict:
-    """The arithmetic roof of the step kernel: its FP64 pipe (FP64 form) or
-    its FP32 pipe (FP32 form).  achieved = FP warp instructions issued per
+def fp_roofline(prec, value, fp64_tflops, fp32_tflops, H, workload="shear_layer",
+                sms: int = 0, sm_mhz: float = 0.0) -> dict:
+    """The binding roof of the step kernel beyond HBM.
+
+    FP64 form: its FP64 pipe.  achieved = FP64 warp instructions issued per
     second (ncu count per cell-update x measured cell-updates/s); peak = the
-    FMA rate hydro_gpu_calibrate measures in the same run, as warp
-    instructions per second (one FP64 or FP32 warp instruction takes one pipe
-    slot per lane).  The FP64 pipe binds the FP64 form; the FP32 form is
-    latency-bound below its FP32 roof (issue_active_pct)."""
+    FP64 FMA rate hydro_gpu_calibrate measures in the same run, as warp
+    instructions per second (one warp instruction takes one pipe slot per
+    lane).  FP32 form: instruction issue, which binds it (its FP32 pipe is
+    far from busy).  achieved = all warp instructions per second; peak = 4
+    per SM per clock at the SM clock sampled during the timed region.  Each
+    carries the other figure beside it."""
     fp64 = prec == H.PRECISION_FP64
     name = "fp64" if fp64 else "fp32"
     out = {"bound": f"{name}_pipe", "peak_tflops_fp64": fp64_tflops, "peak_tflops_fp32": fp32_tflops}
     counts = profile_counts(name)
-    if counts and workload == "shear_layer" and N_SIDE == 2048:
-        per_cell = counts[f"{name}_warp_inst_per_cell_update"]
-        achieved = value * per_cell
-        peak = (fp64_tflops if fp64 else fp32_tflops) * 1e12 / 2 / 32
-        out.update({"achieved": achieved, "peak": peak, "unit": f"{name.upper()} warp instructions/s",
-                    "frac": achieved / peak, "of": "measured (hydro_gpu_calibrate)",
-                    f"{name}_warp_inst_per_cell_update": per_cell,
-                    f"{name}_thread_inst_per_cell_update": counts[f"{name}_thread_inst_per_cell_update"],
-                    "issue_active_pct": counts.get("issue_active_pct"),
-                    "counts_source": counts["source"]})
+    if not (counts and workload == "shear_layer" and N_SIDE == 2048):
+        return out
+    per_cell = counts[f"{name}_warp_inst_per_cell_update"]
+    pipe_achieved = value * per_cell
+    pipe_peak = (fp64_tflops if fp64 else fp32_tflops) * 1e12 / 2 / 32
+    pipe = {"achieved": pipe_achieved, "peak": pipe_peak, "unit": f"{name.upper()} warp instructions/s",
+            "frac": pipe_achieved / pipe_peak, "of": "measured (hydro_gpu_calibrate)"}
+    issue = None
+    all_per_cell = counts.get("warp_inst_per_cell_update_all_pipes")
+    if all_per_cell and sms > 0 and sm_mhz > 0:
+        ia, ip = value * all_per_cell, 4.0 * sms * sm_mhz * 1e6
+        issue = {"achieved": ia, "peak": ip, "unit": "warp instructions/s", "frac": ia / ip,
+                 "of": f"4 per SM per clock, {sms} SMs at the sampled {sm_mhz:.0f} MHz",
+                 "warp_inst_per_cell_update": all_per_cell}
+    if fp64 or issue is None:
+        out.update(pipe)
+        if issue:
+            out["issue"] = issue
+    else:
+        out.update(issue)
+        out["bound"] = "issue"
+        out[f"{name}_pipe"] = pipe
+    out.update({f"{name}_warp_inst_per_cell_update": per_cell,
+                f"{name}_thread_inst_per_cell_update": counts[f"{name}_thread_inst_per_cell_update"],
+                "issue_active_pct": counts.get("issue_active_pct"),
+                "counts_source": counts["source"]})
     return out
 
 
@@ -915,6 +935,9 @@ def main() -> None:
     pk = peaks()
     per_launch_s = step_ms * 1e-3 / args.steps
     achieved_gbs = bytes_per_cell * cells / per_launch_s / 1e9
+    clocks = clk.summary()      # (reads and removes the sample file: once)
+    sms = H.sm_count(device)
+    clock_mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz") or 0.0
     fp64_tflops, fp32_tflops = H.calibrate(device)
     traffic = profile_traffic() if (prec == H.PRECISION_FP64 and args.workload == "shear_layer"
                                     and N_SIDE == 2048) else None
@@ -938,9 +961,11 @@ def main() -> None:
                      "unit": "GB/s", "frac": achieved_gbs / pk["hbm_gbs"],
                      "traffic": traffic, "peak_source": pk["source"],
                      "bytes_per_cell_update": bytes_per_cell,
-                     "note": "HBM is not the binding roof of this stencil: the step is bound by "
-                             "its FP64 (FP32) pipe, reported in fp_roofline"},
-        "fp_roofline": fp_roofline(prec, value, fp64_tflops, fp32_tflops, H, args.workload),
+                     "note": "HBM is not the binding roof of this stencil: the FP64 step is bound by "
+                             "its FP64 pipe, the FP32 form by instruction issue; fp_roofline reports "
+                             "them"},
+        "fp_roofline": fp_roofline(prec, value, fp64_tflops, fp32_tflops, H, args.workload,
+                                   sms=sms, sm_mhz=clock_mhz),
         "forms": {
             "fp64": {"value": cells * args.steps / (fp64_ms * 1e-3), "ms_per_step": fp64_ms / args.steps,
                      "conserved_drift": drift_main if prec == H.PRECISION_FP64 else drift_o},
@@ -950,7 +975,8 @@ def main() -> None:
                                         "velocity_y": l1[2], "pressure": l1[3]},
                      "conserved_drift": drift_main if prec == H.PRECISION_FP32 else drift_o,
                      "fp_roofline": fp_roofline(H.PRECISION_FP32, cells * args.steps / (fp32_ms * 1e-3),
-                                                fp64_tflops, fp32_tflops, H, args.workload),
+                                                fp64_tflops, fp32_tflops, H, args.workload,
+                                                sms=sms, sm_mhz=clock_mhz),
                      "roofline": hbm_roofline(cells * args.steps / (fp32_ms * 1e-3), BYTES_PER_CELL_FP64 // 2,
                                               pk, profile_traffic("fp32") if args.workload == "shear_layer"
                                               and N_SIDE == 2048 else None)},
@@ -963,7 +989,7 @@ def main() -> None:
                 "note": "hydro_gpu_launch_simulation on host System arrays: upload, K steps, "
                         "download (copies inside the timed call); median of the calls"},
         "gpu_launches": int(launches),
-        "clocks": clk.summary(),
+        "clocks": clocks,
     }
     if blast is not None:
         line["forms"]["point_blast_8192"] = blast

@@ -196,6 +196,7 @@ _SIGNATURES = {
                                            _dp, _P(C.c_int)]),
     "hydro_gpu_device_count": (C.c_int, []),
     "hydro_gpu_calibrate": (C.c_int, [C.c_int, _dp, _dp]),
+    "hydro_gpu_sm_count": (C.c_int, [C.c_int]),
     "hydro_gpu_chunk_plan": (C.c_int, [C.c_int] * 4 + [_P(C.c_int)] * 4 + [C.c_int]),
     "hydro_gpu_version": (C.c_char_p, []),
     "free_traceback": (None, [_P(ErrorStatus)]),
@@ -248,6 +249,11 @@ def _consume(lib: C.CDLL, e: ErrorStatus) -> tuple[int, str]:
 
 def device_count() -> int:
     return int(library().hydro_gpu_device_count())
+
+
+def sm_count(device: int = 0) -> int:
+    """Streaming multiprocessors of the device (0 when it cannot be queried)."""
+    return int(library().hydro_gpu_sm_count(device))
 
 
 def calibrate(device: int = 0) -> tuple[float, float]:

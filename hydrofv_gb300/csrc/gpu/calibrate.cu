@@ -56,6 +56,16 @@ int measure(int sms, int iters, double *tflops)
 
 }  // namespace
 
+extern "C" int hydro_gpu_sm_count(int device)
+{
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return sms;
+}
+
 extern "C" int hydro_gpu_calibrate(int device, double *fp64_tflops, double *fp32_tflops)
 {
     if (cudaSetDevice(device) != cudaSuccess) return -1;

@@ -176,6 +176,11 @@ void hydro_gpu_batch_destroy(HydroGpuBatch *batch);
  * for roofline reporting.  Returns 0 on success. */
 int hydro_gpu_calibrate(int device, double *fp64_tflops, double *fp32_tflops);
 
+/* Streaming multiprocessors of `device` (0 when it cannot be queried); with
+ * the SM clock it gives the instruction-issue roof (4 warp instructions per
+ * SM per clock) that roofline reporting uses for issue-bound kernels. */
+int hydro_gpu_sm_count(int device);
+
 /* The FP64 step's work items for an nx x ny grid (g ghost layers) on `slots`
  * resident CTAs: the guided row-chunk plan (h1-row items, then the last
  * `tail` rows in h2-row items) and, if rows is not NULL, each item's strip

@@ -67,7 +67,9 @@ def test_gpu_arm_line(gpu_available, tmp_path):
     # 8192^2 point blast rides along on the default workload
     forms = d["forms"]
     assert forms["fp32"]["roofline"]["bound"] == "hbm"
-    assert "bound" in forms["fp32"]["fp_roofline"]
+    assert forms["fp32"]["fp_roofline"]["bound"] == "issue"      # the FP32 form is issue-bound
+    assert "fp32_pipe" in forms["fp32"]["fp_roofline"]
+    assert d["fp_roofline"]["bound"] == "fp64_pipe" and "issue" in d["fp_roofline"]
     blast = forms["point_blast_8192"]
     assert blast["fp64"]["value"] > 0 and blast["fp32"]["value"] > 0
     assert set(blast["fp32"]["rel_l1_vs_fp64"]) == {"density", "velocity_x", "velocity_y", "pressure"}
