@@ -230,7 +230,8 @@ def fp_roofline(prec, value, fp64_tflops, fp32_tflops, H, workload="shear_layer"
     carries the other figure beside it."""
     fp64 = prec == H.PRECISION_FP64
     name = "fp64" if fp64 else "fp32"
-    out = {"bound": f"{name}_pipe", "peak_tflops_fp64": fp64_tflops, "peak_tflops_fp32": fp32_tflops}
+    out = {"bound": "fp64_pipe" if fp64 else "issue", "peak_tflops_fp64": fp64_tflops,
+           "peak_tflops_fp32": fp32_tflops}
     counts = profile_counts(name)
     if not (counts and workload == "shear_layer" and N_SIDE == 2048):
         return out
@@ -246,13 +247,13 @@ def fp_roofline(prec, value, fp64_tflops, fp32_tflops, H, workload="shear_layer"
         issue = {"achieved": ia, "peak": ip, "unit": "warp instructions/s", "frac": ia / ip,
                  "of": f"4 per SM per clock, {sms} SMs at the sampled {sm_mhz:.0f} MHz",
                  "warp_inst_per_cell_update": all_per_cell}
-    if fp64 or issue is None:
+    if fp64:
         out.update(pipe)
         if issue:
             out["issue"] = issue
     else:
-        out.update(issue)
-        out["bound"] = "issue"
+        if issue:
+            out.update(issue)
         out[f"{name}_pipe"] = pipe
     out.update({f"{name}_warp_inst_per_cell_update": per_cell,
                 f"{name}_thread_inst_per_cell_update": counts[f"{name}_thread_inst_per_cell_update"],
