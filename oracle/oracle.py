@@ -19,7 +19,7 @@ import os
 import sys
 import subprocess
 import time
-from dataclasses import dataclass, field
+from dataclasses import dataclass
 
 import numpy as np
 
