@@ -327,87 +327,88 @@ __device__ __forceinline__ int solve_faces(Mh2dShared<R, NT> &sm, const GasConst
         }
         __syncthreads();
         return err;
-    }
-    for (int f = tid; f < nF; f += NT) {
-        R aL, aR, ppv;
-        const int reg = hllc_classify(gas, sm.FL[0][f], sm.FL[1][f], sm.FL[3][f],
-                                      sm.FR[0][f], sm.FR[1][f], sm.FR[3][f], aL, aR, ppv);
-        sm.aL[f] = aL;
-        sm.aR[f] = aR;
-        sm.pg[f] = ppv;
-        sm.reg[f] = (unsigned char) reg;
-        if (reg == PREG_TRRS) sm.listT[atomicAdd(&sm.nT, 1)] = (short) f;
-        else if (reg == PREG_TSRS) sm.listS[atomicAdd(&sm.nS, 1)] = (short) f;
-    }
-    __syncthreads();
-    const int nT = sm.nT, nS = sm.nS;
-    for (int i = tid; i < nT + nS; i += NT) {
-        if constexpr (TAPE) {
-            R z0, z1;
-            int f;
-            if (i < nT) {
-                f = sm.listT[i];
-                sm.pg[f] = guess_p_trrs_z(gas, sm.FL[1][f], sm.FL[3][f], sm.aL[f],
-                                          sm.FR[1][f], sm.FR[3][f], sm.aR[f], z0, z1);
-            } else {
-                f = sm.listS[i - nT];
-                sm.pg[f] = guess_p_tsrs_g(gas, sm.FL[0][f], sm.FL[1][f], sm.FL[3][f],
-                                          sm.FR[0][f], sm.FR[1][f], sm.FR[3][f], sm.pg[f], z0, z1);
-            }
-            *tc.field(f, TAPE_Z0) = z0;
-            *tc.field(f, TAPE_Z1) = z1;
-        } else if (i < nT) {
-            const int f = sm.listT[i];
-            sm.pg[f] = guess_p_trrs(gas, sm.FL[1][f], sm.FL[3][f], sm.aL[f],
-                                    sm.FR[1][f], sm.FR[3][f], sm.aR[f]);
-        } else {
-            const int f = sm.listS[i - nT];
-            sm.pg[f] = guess_p_tsrs(gas, sm.FL[0][f], sm.FL[1][f], sm.FL[3][f],
-                                    sm.FR[0][f], sm.FR[1][f], sm.FR[3][f], sm.pg[f]);
+    } else {
+        for (int f = tid; f < nF; f += NT) {
+            R aL, aR, ppv;
+            const int reg = hllc_classify(gas, sm.FL[0][f], sm.FL[1][f], sm.FL[3][f],
+                                          sm.FR[0][f], sm.FR[1][f], sm.FR[3][f], aL, aR, ppv);
+            sm.aL[f] = aL;
+            sm.aR[f] = aR;
+            sm.pg[f] = ppv;
+            sm.reg[f] = (unsigned char) reg;
+            if (reg == PREG_TRRS) sm.listT[atomicAdd(&sm.nT, 1)] = (short) f;
+            else if (reg == PREG_TSRS) sm.listS[atomicAdd(&sm.nS, 1)] = (short) f;
         }
-    }
-    __syncthreads();
-    for (int f = tid; f < nF; f += NT) {
-        R F[4];
-        const R rl = sm.FL[0][f], ul = sm.FL[1][f], vl = sm.FL[2][f], pl = sm.FL[3][f];
-        const R rr = sm.FR[0][f], ur = sm.FR[1][f], vr = sm.FR[2][f], pr = sm.FR[3][f];
-        if constexpr (TAPE) {
-            const R v[11] = { rl, ul, vl, pl, rr, ur, vr, pr, sm.aL[f], sm.aR[f], sm.pg[f] };
-#pragma unroll
-            for (int q = 0; q < 11; q++) *tc.field(f, q) = v[q];
-            *tc.field(f, TAPE_REG) = (R) sm.reg[f];
-        }
-        if (sm.reg[f] == PREG_VACUUM) {
-            vacuum_flux_dev(gas, rl, ul, vl, pl, sm.aL[f], rr, ur, vr, pr, sm.aR[f], F);
+        __syncthreads();
+        const int nT = sm.nT, nS = sm.nS;
+        for (int i = tid; i < nT + nS; i += NT) {
             if constexpr (TAPE) {
-                *tc.field(f, TAPE_QL) = R(0);
-                *tc.field(f, TAPE_QR) = R(0);
-                *tc.field(f, TAPE_SS) = R(0);
+                R z0, z1;
+                int f;
+                if (i < nT) {
+                    f = sm.listT[i];
+                    sm.pg[f] = guess_p_trrs_z(gas, sm.FL[1][f], sm.FL[3][f], sm.aL[f],
+                                              sm.FR[1][f], sm.FR[3][f], sm.aR[f], z0, z1);
+                } else {
+                    f = sm.listS[i - nT];
+                    sm.pg[f] = guess_p_tsrs_g(gas, sm.FL[0][f], sm.FL[1][f], sm.FL[3][f],
+                                              sm.FR[0][f], sm.FR[1][f], sm.FR[3][f], sm.pg[f], z0, z1);
+                }
+                *tc.field(f, TAPE_Z0) = z0;
+                *tc.field(f, TAPE_Z1) = z1;
+            } else if (i < nT) {
+                const int f = sm.listT[i];
+                sm.pg[f] = guess_p_trrs(gas, sm.FL[1][f], sm.FL[3][f], sm.aL[f],
+                                        sm.FR[1][f], sm.FR[3][f], sm.aR[f]);
+            } else {
+                const int f = sm.listS[i - nT];
+                sm.pg[f] = guess_p_tsrs(gas, sm.FL[0][f], sm.FL[1][f], sm.FL[3][f],
+                                        sm.FR[0][f], sm.FR[1][f], sm.FR[3][f], sm.pg[f]);
             }
-        } else if constexpr (TAPE) {
-            R wave[3];
-            const int rc = hllc_finish(gas, rl, ul, vl, pl, sm.aL[f], rr, ur, vr, pr, sm.aR[f],
-                                       sm.pg[f], F, wave);
-            if (rc) err = rc;
-            *tc.field(f, TAPE_QL) = wave[0];
-            *tc.field(f, TAPE_QR) = wave[1];
-            *tc.field(f, TAPE_SS) = wave[2];
-        } else {
-            const int rc = hllc_finish(gas, rl, ul, vl, pl, sm.aL[f], rr, ur, vr, pr, sm.aR[f],
-                                       sm.pg[f], F);
-            if (rc) err = rc;
         }
-        if constexpr (sizeof(R) == 8) {
-            const R A = (f < nXf) ? Ax : Ay;
+        __syncthreads();
+        for (int f = tid; f < nF; f += NT) {
+            R F[4];
+            const R rl = sm.FL[0][f], ul = sm.FL[1][f], vl = sm.FL[2][f], pl = sm.FL[3][f];
+            const R rr = sm.FR[0][f], ur = sm.FR[1][f], vr = sm.FR[2][f], pr = sm.FR[3][f];
+            if constexpr (TAPE) {
+                const R v[11] = { rl, ul, vl, pl, rr, ur, vr, pr, sm.aL[f], sm.aR[f], sm.pg[f] };
 #pragma unroll
-            for (int q = 0; q < 4; q++) sm.FL[q][f] = (F[q] * dtr) * A;
-        } else {
+                for (int q = 0; q < 11; q++) *tc.field(f, q) = v[q];
+                *tc.field(f, TAPE_REG) = (R) sm.reg[f];
+            }
+            if (sm.reg[f] == PREG_VACUUM) {
+                vacuum_flux_dev(gas, rl, ul, vl, pl, sm.aL[f], rr, ur, vr, pr, sm.aR[f], F);
+                if constexpr (TAPE) {
+                    *tc.field(f, TAPE_QL) = R(0);
+                    *tc.field(f, TAPE_QR) = R(0);
+                    *tc.field(f, TAPE_SS) = R(0);
+                }
+            } else if constexpr (TAPE) {
+                R wave[3];
+                const int rc = hllc_finish(gas, rl, ul, vl, pl, sm.aL[f], rr, ur, vr, pr, sm.aR[f],
+                                           sm.pg[f], F, wave);
+                if (rc) err = rc;
+                *tc.field(f, TAPE_QL) = wave[0];
+                *tc.field(f, TAPE_QR) = wave[1];
+                *tc.field(f, TAPE_SS) = wave[2];
+            } else {
+                const int rc = hllc_finish(gas, rl, ul, vl, pl, sm.aL[f], rr, ur, vr, pr, sm.aR[f],
+                                           sm.pg[f], F);
+                if (rc) err = rc;
+            }
+            if constexpr (sizeof(R) == 8) {
+                const R A = (f < nXf) ? Ax : Ay;
 #pragma unroll
-            for (int q = 0; q < 4; q++) sm.FL[q][f] = F[q];
+                for (int q = 0; q < 4; q++) sm.FL[q][f] = (F[q] * dtr) * A;
+            } else {
+#pragma unroll
+                for (int q = 0; q < 4; q++) sm.FL[q][f] = F[q];
+            }
         }
+        __syncthreads();
+        return err;
     }
-    __syncthreads();
-    return err;
 }
 
 /*
